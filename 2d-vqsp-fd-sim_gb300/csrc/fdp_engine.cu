@@ -1,0 +1,564 @@
+// C ABI of the GB300 time-stepping engine (declared in include/fdp.h).
+//
+// A context holds one shot's grid resident in HBM: the eight wavefield
+// arrays, the medium, the PML profiles and memory variables, the bottom
+// history, the source time function and the receiver samples.  fdp_run
+// enqueues three kernels per time level on the context's stream; runs of
+// kChunk levels are captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fdp.h"
+#include "fdp_kernels.cuh"
+
+using fdp::Params;
+using fdp::kPadX;
+using fdp::kPadZ;
+
+namespace {
+
+constexpr int kChunk = 32;       // time levels per captured graph
+constexpr int kBlockX = 128;     // threads per block (x)
+
+std::string g_create_error;
+
+struct DevArr {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct fdp_ctx {
+  fdp_grid g{};
+  int prec = 4;
+  int MX = 0, MZ = 0, TPML = 0, PMLL = 0, PMLXH = 0, PMLZH = 0, NX = 0, NZ = 0, MX1 = 0;
+  int pitch = 0, rows_alloc = 0;
+  int tz = 16, ntz = 1;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // device memory
+  DevArr fields[8];
+  DevArr jm, coef, prof[24], mem[27], ab, hist, stf, rec, raw, itbase;
+  int jmnum = 0;
+  int mt2 = 0;
+  int mr = 0, rec_flags = 0;
+  bool have_medium = false, have_pml = false, have_nr = false, have_source = false;
+  // graph of kChunk levels
+  cudaGraphExec_t graph = nullptr;
+  bool params_dirty = true;
+  long long launches = 0;
+  int last_it = 0;  // highest level run so far
+};
+
+namespace {
+
+int fail(fdp_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf; else g_create_error = buf;
+  return code;
+}
+
+#define CK(c, call)                                                                         \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) return fail((c), FDP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+int dev_alloc(fdp_ctx* c, DevArr& a, size_t bytes) {
+  if (a.p) { cudaFree(a.p); a.p = nullptr; a.bytes = 0; }
+  if (bytes == 0) return FDP_OK;
+  cudaError_t e = cudaMalloc(&a.p, bytes);
+  if (e != cudaSuccess) return fail(c, FDP_ERR_ALLOC, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  a.bytes = bytes;
+  e = cudaMemsetAsync(a.p, 0, bytes, c->stream);
+  if (e != cudaSuccess) return fail(c, FDP_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+  return FDP_OK;
+}
+
+// Bounds (lx, ux, lz, uz) of every field id, as the reference allocates them.
+bool bounds_of(const fdp_ctx* c, int id, int b[4]) {
+  const int PMLL = c->PMLL, PMLXH = c->PMLXH, PMLZH = c->PMLZH, MX = c->MX, TPML = c->TPML;
+  auto set = [&](int a, int bb, int cc, int d) { b[0] = a; b[1] = bb; b[2] = cc; b[3] = d; return true; };
+  switch (id) {
+    case FDP_UM: case FDP_WM: case FDP_QX: case FDP_QZ:
+    case FDP_TXX: case FDP_TZZ: case FDP_TXZ: case FDP_PRES:
+    case FDP_QXP: case FDP_QZP:
+      return set(PMLL, PMLXH, 0, PMLZH);
+    case FDP_PZXL: return set(PMLL, 2, 0, PMLZH);
+    case FDP_PZXH: return set(MX, PMLXH, 0, PMLZH);
+    case FDP_PXXL: case FDP_OXXL: return set(PMLL, 1, 0, PMLZH);
+    case FDP_PXXH: case FDP_OXXH: return set(MX, PMLXH, 0, PMLZH);
+    case FDP_PXZH: return set(PMLL, PMLXH, 0, TPML + 1);
+    case FDP_PZZH: case FDP_OZZH: return set(PMLL, PMLXH, 0, TPML);
+    case FDP_RXXL: case FDP_SXXL: case FDP_GXXL: case FDP_HXXL: return set(PMLL, 3, 0, PMLZH);
+    case FDP_RXXH: case FDP_SXXH: case FDP_GXXH: case FDP_HXXH: return set(MX - 1, PMLXH, 0, PMLZH);
+    case FDP_RZXL: case FDP_GZXL: return set(PMLL, 2, 0, PMLZH);
+    case FDP_RZXH: case FDP_GZXH: return set(MX - 1, PMLXH, 0, PMLZH);
+    case FDP_RXZH: case FDP_GXZH: case FDP_RZZH: case FDP_SZZH: case FDP_GZZH: case FDP_HZZH:
+      return set(PMLL, PMLXH, 0, TPML);
+    case FDP_SZ_U: case FDP_SZ_W: case FDP_SZ_QX: case FDP_SZ_QZ:
+      return set(PMLL, PMLXH, 0, 2);
+    default: return false;
+  }
+}
+
+// All copies go through the context's stream (which does not synchronise
+// with the legacy default stream) and wait for completion.
+int copy_sync(fdp_ctx* c, void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+  if (bytes == 0) return FDP_OK;
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(c, FDP_ERR_CUDA, "copy of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  return FDP_OK;
+}
+
+int copy2d_sync(fdp_ctx* c, void* dst, size_t dpitch, const void* src, size_t spitch, size_t w, size_t h,
+                cudaMemcpyKind kind) {
+  cudaError_t e = cudaMemcpy2DAsync(dst, dpitch, src, spitch, w, h, kind, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(c, FDP_ERR_CUDA, "2-D copy: %s", cudaGetErrorString(e));
+  return FDP_OK;
+}
+
+size_t count_of(const int b[4]) { return (size_t)(b[1] - b[0] + 1) * (size_t)(b[3] - b[2] + 1); }
+
+template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
+  std::memset(&p, 0, sizeof p);
+  p.MX = c->MX; p.MZ = c->MZ; p.TPML = c->TPML; p.PMLL = c->PMLL; p.PMLXH = c->PMLXH; p.PMLZH = c->PMLZH;
+  p.NX = c->NX; p.NZ = c->NZ; p.MX1 = c->MX1; p.LIN_X = c->g.lin_x; p.LIN_Z = c->g.lin_z;
+  p.pitch = c->pitch; p.tz = c->tz; p.ntz = c->ntz;
+  // mod_auxil.F90:19-20 (default-real constants) and aux1.F90:44-46
+  const T H = (T)c->g.h;
+  p.A = (T)(-1.0f / 24.0f);
+  p.B = (T)(9.0f / 8.0f);
+  p.AH = p.A / H; p.BH = p.B / H; p.CH = T(1) / H;
+  p.BC = p.BH / p.CH;  // strain_uw_zz.F90:39
+  p.DT = (T)c->g.dt;
+  p.DTE = p.DT + (T)c->g.tau_eps;
+  const size_t off = (size_t)kPadZ * c->pitch + kPadX;
+  T** f[8] = {&p.UM, &p.WM, &p.QX, &p.QZ, &p.TXX, &p.TZZ, &p.TXZ, &p.PRES};
+  for (int k = 0; k < 8; ++k) *f[k] = (T*)c->fields[k].p + off;
+  p.JM = (const int32_t*)c->jm.p + off;
+  p.coef = (const T*)c->coef.p;
+  p.cld = c->jmnum + 1;
+  const T** pr[24] = {&p.ODA_XL, &p.ODB_XL, &p.ODC_XL, &p.ODD_XL, &p.ODA_XH, &p.ODB_XH, &p.ODC_XH, &p.ODD_XH,
+                      &p.ODA_ZH, &p.ODB_ZH, &p.ODC_ZH, &p.ODD_ZH,
+                      &p.ODA2_XL, &p.ODB2_XL, &p.ODC2_XL, &p.ODD2_XL, &p.ODA2_XH, &p.ODB2_XH, &p.ODC2_XH, &p.ODD2_XH,
+                      &p.ODA2_ZH, &p.ODB2_ZH, &p.ODC2_ZH, &p.ODD2_ZH};
+  for (int k = 0; k < 24; ++k) *pr[k] = (const T*)c->prof[k].p;
+  T** m[27] = {&p.PZXL, &p.PZXH, &p.PXXL, &p.PXXH, &p.OXXL, &p.OXXH, &p.PXZH, &p.PZZH, &p.OZZH,
+               &p.RXXL, &p.RXXH, &p.SXXL, &p.SXXH, &p.RZXL, &p.RZXH, &p.GXXL, &p.GXXH, &p.HXXL, &p.HXXH,
+               &p.GZXL, &p.GZXH, &p.RXZH, &p.GXZH, &p.RZZH, &p.SZZH, &p.GZZH, &p.HZZH};
+  for (int k = 0; k < 27; ++k) *m[k] = (T*)c->mem[k].p;
+  p.AB = (const T*)c->ab.p;
+  p.HIST = (T*)c->hist.p;
+  p.STF = (const T*)c->stf.p;
+  p.MT2 = c->mt2;
+  p.it_base = (const int*)c->itbase.p;
+  p.MR = c->mr;
+  p.REC = (const int*)c->rec.p;
+  p.RAW = (T*)c->raw.p;
+}
+
+template <class T, bool SI> int launch_level(fdp_ctx* c, const Params<T>& p, int it_off) {
+  const dim3 blk(kBlockX, 1, 1);
+  const dim3 grd((c->NX + kBlockX - 1) / kBlockX, c->ntz, 1);
+  fdp::k_stress<T, SI><<<grd, blk, 0, c->stream>>>(p, it_off);
+  fdp::k_velocity<T, SI><<<grd, blk, 0, c->stream>>>(p, it_off);
+  const int nedge = std::max(SI ? c->NX : 0, c->mr);
+  if (nedge > 0) {
+    fdp::k_edge<T, SI><<<(nedge + kBlockX - 1) / kBlockX, blk, 0, c->stream>>>(p, it_off);
+    c->launches += 1;
+  }
+  c->launches += 2;
+  return FDP_OK;
+}
+
+template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_off) {
+  return c->g.stress_imaging ? launch_level<T, true>(c, p, it_off) : launch_level<T, false>(c, p, it_off);
+}
+
+template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
+  Params<T> p;
+  fill_params<T>(c, p);
+  // levels per graph replay = kChunk; the graph reads the level from
+  // *it_base and advances it by kChunk at its end.
+  if (c->params_dirty && c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  c->params_dirty = false;
+  fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
+  c->launches += 1;
+  int it = it_begin;
+  const int nlev = it_end - it_begin + 1;
+  if (nlev >= kChunk && !c->graph) {
+    cudaGraph_t gr = nullptr;
+    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = c->launches;
+    for (int k = 0; k < kChunk; ++k) launch_level_any<T>(c, p, k);
+    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, kChunk);
+    c->launches = before;  // capture only records; replays are counted below
+    cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+    if (e != cudaSuccess) return fail(c, FDP_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) { c->graph = nullptr; return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+  }
+  const int per_level = 2 + ((std::max(c->g.stress_imaging ? c->NX : 0, c->mr) > 0) ? 1 : 0);
+  while (it_end - it + 1 >= kChunk && c->graph) {
+    CK(c, cudaGraphLaunch(c->graph, c->stream));
+    c->launches += (long long)kChunk * per_level + 1;
+    it += kChunk;
+  }
+  int k = 0;
+  for (; it <= it_end; ++it, ++k) launch_level_any<T>(c, p, k);
+  if (k > 0) {
+    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, k);
+    c->launches += 1;
+  }
+  CK(c, cudaGetLastError());
+  return FDP_OK;
+}
+
+template <class T>
+void derive_table(const int32_t jmnum, const T* tab, std::vector<T>& out) {
+  // table24 columns (.MO record order, read_model_par.F90:147-155)
+  enum { MU, SXX1, SXX2, SXX3, SZZ1, SZZ2, SZZ3, P1, P2, P3, R1U, R1W, R2U, R2W, R3U, R3W,
+         R1QX, R1QZ, R2QX, R2QZ, R3QX, R3QZ, AUXW, AUXQZ };
+  const size_t ld = (size_t)jmnum + 1;
+  out.assign(ld * fdp::C_NCOEF, T(0));
+  for (int j = 1; j <= jmnum; ++j) {
+    const T* r = tab + (size_t)(j - 1) * 24;
+    auto put = [&](int k, T v) { out[(size_t)k * ld + j] = v; };
+    put(fdp::C_MU, r[MU]);
+    put(fdp::C_SXX1, r[SXX1]); put(fdp::C_SXX2, r[SXX2]); put(fdp::C_SXX3, r[SXX3]);
+    put(fdp::C_SZZ1, r[SZZ1]); put(fdp::C_SZZ2, r[SZZ2]); put(fdp::C_SZZ3, r[SZZ3]);
+    put(fdp::C_P1, r[P1]); put(fdp::C_P2, r[P2]); put(fdp::C_P3, r[P3]);
+    // inh_qx_int.F90:44 and inh_v_uv_int.F90:46, evaluated per material
+    put(fdp::C_EQX, std::exp(-r[R3QX]));
+    put(fdp::C_CU, (r[R2U] / r[R3QX]) * (T(1) - std::exp(-r[R3QX])));
+    put(fdp::C_R1QX, r[R1QX]); put(fdp::C_R2QX, r[R2QX]);
+    put(fdp::C_R1U, r[R1U]); put(fdp::C_R3U, r[R3U]);
+    put(fdp::C_EQZ, std::exp(-r[R3QZ]));
+    put(fdp::C_CW, (r[R2W] / r[R3QZ]) * (T(1) - std::exp(-r[R3QZ])));
+    put(fdp::C_R1QZ, r[R1QZ]); put(fdp::C_R2QZ, r[R2QZ]);
+    put(fdp::C_R1W, r[R1W]); put(fdp::C_R3W, r[R3W]);
+    put(fdp::C_AUXW, r[AUXW]); put(fdp::C_AUXQZ, r[AUXQZ]);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdp_create(const fdp_grid* g, fdp_ctx** out) {
+  if (!g || !out) return fail(nullptr, FDP_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (g->precision != FDP_F32 && g->precision != FDP_F64)
+    return fail(nullptr, FDP_ERR_ARG, "precision must be FDP_F32 or FDP_F64");
+  if (g->mx < 8 || g->mz < 8 || g->tpml < 0)
+    return fail(nullptr, FDP_ERR_ARG, "need MX >= 8, MZ >= 8, TPML >= 0 (got %d, %d, %d)", g->mx, g->mz, g->tpml);
+  // The reference updates the source row with HPLANE_LIN_STRESS in addition
+  // to the row's own routine when LIN_Z lies outside the interior rows
+  // (time_loop.F90:93-124): such a source row is rejected.
+  if (g->lin_z < 2 || g->lin_z > g->mz - 2)
+    return fail(nullptr, FDP_ERR_ARG, "source row LIN_Z=%d must lie in 2..MZ-2=%d", g->lin_z, g->mz - 2);
+  if (!(g->h > 0) || !(g->dt > 0)) return fail(nullptr, FDP_ERR_ARG, "H and DT must be positive");
+  fdp_ctx* c = new fdp_ctx();
+  c->g = *g;
+  c->prec = g->precision;
+  c->MX = g->mx; c->MZ = g->mz; c->TPML = g->tpml;
+  c->MX1 = c->MX - 1;
+  c->PMLL = 1 - c->TPML; c->PMLXH = c->MX + c->TPML; c->PMLZH = c->MZ + c->TPML;
+  c->NX = c->PMLXH - c->PMLL + 1;
+  c->NZ = c->PMLZH + 1;
+  c->pitch = ((c->NX + 2 * kPadX + 31) / 32) * 32;
+  c->rows_alloc = c->NZ + 2 * kPadZ;
+  // z-tiles of tz rows; the last tile takes the remainder (>= tz rows)
+  const int nbx = (c->NX + kBlockX - 1) / kBlockX;
+  int tz = 16;
+  while (tz > 5 && (long long)nbx * (c->NZ / tz) < 4LL * 152) --tz;
+  if (tz > c->NZ) tz = c->NZ;
+  c->tz = tz;
+  c->ntz = std::max(1, c->NZ / tz);
+  auto bail = [&](int code) { g_create_error = c->err; fdp_destroy(c); return code; };
+  cudaError_t e = cudaSetDevice(g->device);
+  if (e != cudaSuccess) { c->err = std::string("cudaSetDevice: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { c->err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
+  const size_t es = (size_t)c->prec;
+  const size_t fbytes = (size_t)c->rows_alloc * c->pitch * es;
+  int rc;
+  for (int k = 0; k < 8; ++k)
+    if ((rc = dev_alloc(c, c->fields[k], fbytes)) != FDP_OK) return bail(rc);
+  if ((rc = dev_alloc(c, c->jm, (size_t)c->rows_alloc * c->pitch * sizeof(int32_t))) != FDP_OK) return bail(rc);
+  const int TP = c->TPML;
+  const size_t pshape[24] = {
+      (size_t)(TP + 1) * c->NZ, (size_t)(TP + 1) * c->NZ, (size_t)(TP + 1) * c->NZ, (size_t)(TP + 1) * c->NZ,
+      (size_t)(TP + 1) * c->NZ, (size_t)(TP + 1) * c->NZ, (size_t)(TP + 1) * c->NZ, (size_t)(TP + 1) * c->NZ,
+      (size_t)(TP + 1) * c->NX, (size_t)(TP + 1) * c->NX, (size_t)(TP + 1) * c->NX, (size_t)(TP + 1) * c->NX,
+      (size_t)(TP + 2) * c->NZ, (size_t)(TP + 2) * c->NZ, (size_t)(TP + 2) * c->NZ, (size_t)(TP + 2) * c->NZ,
+      (size_t)(TP + 2) * c->NZ, (size_t)(TP + 2) * c->NZ, (size_t)(TP + 2) * c->NZ, (size_t)(TP + 2) * c->NZ,
+      (size_t)(TP + 2) * c->NX, (size_t)(TP + 2) * c->NX, (size_t)(TP + 2) * c->NX, (size_t)(TP + 2) * c->NX};
+  for (int k = 0; k < 24; ++k)
+    if ((rc = dev_alloc(c, c->prof[k], pshape[k] * es)) != FDP_OK) return bail(rc);
+  for (int k = 0; k < 27; ++k) {
+    int b[4];
+    bounds_of(c, FDP_PZXL + k, b);
+    if ((rc = dev_alloc(c, c->mem[k], count_of(b) * es)) != FDP_OK) return bail(rc);
+  }
+  if ((rc = dev_alloc(c, c->ab, 16 * es)) != FDP_OK) return bail(rc);
+  if ((rc = dev_alloc(c, c->hist, (size_t)12 * c->NX * es)) != FDP_OK) return bail(rc);
+  if ((rc = dev_alloc(c, c->itbase, sizeof(int))) != FDP_OK) return bail(rc);
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) { c->err = std::string("init: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
+  *out = c;
+  return FDP_OK;
+}
+
+int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_t jmnum, const void* table24) {
+  if (!c || !jm || !table24) return fail(c, FDP_ERR_ARG, "null argument");
+  if (nx != c->NX || nz != c->NZ) return fail(c, FDP_ERR_ARG, "JM is %dx%d, grid is %dx%d", nx, nz, c->NX, c->NZ);
+  if (jmnum < 1) return fail(c, FDP_ERR_ARG, "JMNUM must be >= 1");
+  for (size_t k = 0; k < (size_t)nx * nz; ++k)
+    if (jm[k] < 1 || jm[k] > jmnum) return fail(c, FDP_ERR_ARG, "JM value %d at %zu outside 1..%d", jm[k], k, jmnum);
+  int rc;
+  CK(c, cudaStreamSynchronize(c->stream));
+  // JM into the padded field layout (padding holds material 1)
+  std::vector<int32_t> h((size_t)c->rows_alloc * c->pitch, 1);
+  for (int L = 0; L < c->NZ; ++L)
+    std::memcpy(&h[(size_t)(L + kPadZ) * c->pitch + kPadX], jm + (size_t)L * c->NX, (size_t)c->NX * sizeof(int32_t));
+  if ((rc = copy_sync(c, c->jm.p, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  if (c->prec == 8) {
+    std::vector<double> t;
+    derive_table<double>(jmnum, (const double*)table24, t);
+    if ((rc = dev_alloc(c, c->coef, t.size() * 8)) != FDP_OK) return rc;
+    if ((rc = copy_sync(c, c->coef.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  } else {
+    std::vector<float> t;
+    derive_table<float>(jmnum, (const float*)table24, t);
+    if ((rc = dev_alloc(c, c->coef, t.size() * 4)) != FDP_OK) return rc;
+    if ((rc = copy_sync(c, c->coef.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->jmnum = jmnum;
+  c->have_medium = true;
+  c->params_dirty = true;
+  return FDP_OK;
+}
+
+int fdp_set_pml(fdp_ctx* c, const void* const* prof) {
+  if (!c || !prof) return fail(c, FDP_ERR_ARG, "null argument");
+  const size_t es = (size_t)c->prec;
+  int rc;
+  CK(c, cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 24; ++k) {
+    if (!prof[k]) return fail(c, FDP_ERR_ARG, "profile %d is null", k);
+    const bool zprof = (k >= 8 && k < 12) || k >= 20;
+    if (!zprof) {
+      if ((rc = copy_sync(c, c->prof[k].p, prof[k], c->prof[k].bytes, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+    } else {
+      // (0:nj-1, PMLL:PMLXH) -> [J][I-PMLL]
+      const int nj = (k < 12) ? c->TPML + 1 : c->TPML + 2;
+      std::vector<unsigned char> t(c->prof[k].bytes);
+      const unsigned char* s = (const unsigned char*)prof[k];
+      for (int i = 0; i < c->NX; ++i)
+        for (int j = 0; j < nj; ++j)
+          std::memcpy(&t[((size_t)j * c->NX + i) * es], &s[((size_t)i * nj + j) * es], es);
+      if ((rc = copy_sync(c, c->prof[k].p, t.data(), t.size(), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+    }
+  }
+  c->have_pml = true;
+  return FDP_OK;
+}
+
+int fdp_set_bottom_nr(fdp_ctx* c, const void* ab16) {
+  if (!c || !ab16) return fail(c, FDP_ERR_ARG, "null argument");
+  int rc;
+  CK(c, cudaStreamSynchronize(c->stream));
+  if ((rc = copy_sync(c, c->ab.p, ab16, 16 * (size_t)c->prec, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  c->have_nr = true;
+  return FDP_OK;
+}
+
+int fdp_set_source(fdp_ctx* c, const void* sourtf, int32_t mt2) {
+  if (!c || !sourtf) return fail(c, FDP_ERR_ARG, "null argument");
+  if (mt2 < 1) return fail(c, FDP_ERR_ARG, "MT2 must be >= 1");
+  CK(c, cudaStreamSynchronize(c->stream));
+  int rc;
+  if ((rc = dev_alloc(c, c->stf, (size_t)2 * mt2 * c->prec)) != FDP_OK) return rc;
+  if ((rc = copy_sync(c, c->stf.p, sourtf, (size_t)2 * mt2 * c->prec, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  c->mt2 = mt2;
+  c->have_source = true;
+  c->params_dirty = true;
+  if (c->mr > 0) {
+    if ((rc = dev_alloc(c, c->raw, (size_t)c->mt2 * c->mr * 6 * c->prec)) != FDP_OK) return rc;
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
+  return FDP_OK;
+}
+
+int fdp_set_receivers(fdp_ctx* c, const int32_t* irecx, const int32_t* lrecx, const int32_t* irecz,
+                      const int32_t* lrecz, int32_t mr, int32_t flags) {
+  if (!c) return fail(c, FDP_ERR_ARG, "null context");
+  if (mr < 0 || (mr > 0 && (!irecx || !lrecx || !irecz || !lrecz))) return fail(c, FDP_ERR_ARG, "bad receiver arrays");
+  CK(c, cudaStreamSynchronize(c->stream));
+  std::vector<int32_t> r((size_t)4 * mr);
+  for (int j = 0; j < mr; ++j) { r[4 * j] = irecx[j]; r[4 * j + 1] = lrecx[j]; r[4 * j + 2] = irecz[j]; r[4 * j + 3] = lrecz[j]; }
+  int rc;
+  if ((rc = dev_alloc(c, c->rec, r.size() * sizeof(int32_t))) != FDP_OK) return rc;
+  if (mr > 0) if ((rc = copy_sync(c, c->rec.p, r.data(), r.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  c->mr = mr;
+  c->rec_flags = flags;
+  if (c->mt2 > 0 && mr > 0) {
+    if ((rc = dev_alloc(c, c->raw, (size_t)c->mt2 * mr * 6 * c->prec)) != FDP_OK) return rc;
+  }
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->params_dirty = true;
+  return FDP_OK;
+}
+
+int fdp_run(fdp_ctx* c, int32_t it_begin, int32_t it_end) {
+  if (!c) return fail(c, FDP_ERR_ARG, "null context");
+  if (!c->have_medium || !c->have_pml || !c->have_nr || !c->have_source)
+    return fail(c, FDP_ERR_STATE, "set medium, PML profiles, bottom coefficients and source before fdp_run");
+  if (it_begin < 1 || it_end > c->mt2 || it_end < it_begin - 1)
+    return fail(c, FDP_ERR_ARG, "levels %d..%d outside 1..MT2=%d", it_begin, it_end, c->mt2);
+  if (c->mr > 0 && !c->raw.p) return fail(c, FDP_ERR_STATE, "receiver buffer missing");
+  if (it_end < it_begin) return FDP_OK;
+  CK(c, cudaSetDevice(c->g.device));
+  int rc = (c->prec == 8) ? run_t<double>(c, it_begin, it_end) : run_t<float>(c, it_begin, it_end);
+  if (rc == FDP_OK && it_end > c->last_it) c->last_it = it_end;
+  return rc;
+}
+
+int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host) {
+  if (!c || (!host && n_levels > 0)) return fail(c, FDP_ERR_ARG, "null argument");
+  if (n_levels <= 0 || c->mr == 0) return FDP_OK;
+  if (it_first < 1 || it_first + n_levels - 1 > c->mt2) return fail(c, FDP_ERR_ARG, "levels outside 1..MT2");
+  CK(c, cudaStreamSynchronize(c->stream));
+  const int mr = c->mr;
+  const int lo = it_first - 1;  // also fetch the previous level for the time derivative
+  const int first_fetch = std::max(lo, 1);
+  const int nfetch = it_first + n_levels - first_fetch;
+  const size_t lev = (size_t)mr * 6;
+  auto body = [&](auto zero) -> int {
+    using T = decltype(zero);
+    std::vector<T> raw((size_t)nfetch * lev);
+    int rc = copy_sync(c, raw.data(), (const T*)c->raw.p + (size_t)(first_fetch - 1) * lev,
+                       raw.size() * sizeof(T), cudaMemcpyDeviceToHost);
+    if (rc != FDP_OK) return rc;
+    const T DT = (T)c->g.dt;
+    T* out = (T*)host;
+    for (int n = 0; n < n_levels; ++n) {
+      const int it = it_first + n;
+      const T* cur = &raw[(size_t)(it - first_fetch) * lev];
+      const T* prv = (it - 1 >= first_fetch) ? &raw[(size_t)(it - 1 - first_fetch) * lev] : nullptr;
+      for (int j = 0; j < mr; ++j) {
+        T* r = out + ((size_t)n * mr + j) * FDP_REC_VALUES;
+        const T* s = cur + (size_t)j * 6;
+        const T* q = prv ? prv + (size_t)j * 6 : nullptr;
+        auto prev = [&](int k) { return q ? q[k] : T(0); };
+        for (int k = 0; k < FDP_REC_VALUES; ++k) r[k] = T(0);
+        if (c->rec_flags & FDP_REC_TLV) {
+          // store_seismograms.F90:65-66,92-93: SPU=(S-SSU)/DT, SSU=S
+          r[0] = s[0]; r[1] = s[1];
+          r[2] = (s[0] - prev(0)) / DT; r[3] = (s[1] - prev(1)) / DT;
+          if (c->rec_flags & FDP_REC_TLQ) {
+            r[4] = s[2]; r[5] = s[3];
+            r[6] = (s[2] - prev(2)) / DT; r[7] = (s[3] - prev(3)) / DT;
+          }
+        }
+        if (c->rec_flags & FDP_REC_TLP) { r[8] = s[4]; r[9] = s[5]; }
+      }
+    }
+    return FDP_OK;
+  };
+  return c->prec == 8 ? body(0.0) : body(0.0f);
+}
+
+int fdp_field_bounds(fdp_ctx* c, int32_t id, int32_t* b4) {
+  if (!c || !b4) return fail(c, FDP_ERR_ARG, "null argument");
+  int b[4];
+  if (!bounds_of(c, id, b)) return fail(c, FDP_ERR_ARG, "unknown field id %d", id);
+  for (int k = 0; k < 4; ++k) b4[k] = b[k];
+  return FDP_OK;
+}
+
+static int field_copy(fdp_ctx* c, int32_t id, void* host, bool set) {
+  if (!c || !host) return fail(c, FDP_ERR_ARG, "null argument");
+  int b[4];
+  if (!bounds_of(c, id, b)) return fail(c, FDP_ERR_ARG, "unknown field id %d", id);
+  if (id == FDP_QXP || id == FDP_QZP) return fail(c, FDP_ERR_UNSUPPORTED, "QXP/QZP are not stored by this engine");
+  CK(c, cudaStreamSynchronize(c->stream));
+  const size_t es = (size_t)c->prec;
+  if (id <= FDP_PRES) {
+    char* dev = (char*)c->fields[id].p + ((size_t)kPadZ * c->pitch + kPadX) * es;
+    if (set)
+      return copy2d_sync(c, dev, c->pitch * es, host, c->NX * es, c->NX * es, c->NZ, cudaMemcpyHostToDevice);
+    else
+      return copy2d_sync(c, host, c->NX * es, dev, c->pitch * es, c->NX * es, c->NZ, cudaMemcpyDeviceToHost);
+    return FDP_OK;
+  }
+  void* dev;
+  if (id >= FDP_SZ_U) dev = (char*)c->hist.p + (size_t)(id - FDP_SZ_U) * 3 * c->NX * es;
+  else dev = c->mem[id - FDP_PZXL].p;
+  const size_t n = count_of(b) * es;
+  if (set) return copy_sync(c, dev, host, n, cudaMemcpyHostToDevice);
+  return copy_sync(c, host, dev, n, cudaMemcpyDeviceToHost);
+}
+
+int fdp_get_field(fdp_ctx* c, int32_t id, void* host) { return field_copy(c, id, host, false); }
+int fdp_set_field(fdp_ctx* c, int32_t id, const void* host) { return field_copy(c, id, (void*)host, true); }
+
+int fdp_get_snapshot(fdp_ctx* c, int32_t mask, void* host) {
+  if (!c || !host) return fail(c, FDP_ERR_ARG, "null argument");
+  const size_t n = (size_t)c->NX * c->NZ * c->prec;
+  char* out = (char*)host;
+  const int ids[4] = {FDP_UM, FDP_WM, FDP_QX, FDP_QZ};
+  for (int k = 0; k < 4; ++k) {
+    if (!(mask & (1 << k))) continue;
+    int rc = field_copy(c, ids[k], out, false);
+    if (rc != FDP_OK) return rc;
+    out += n;
+  }
+  return FDP_OK;
+}
+
+int fdp_synchronize(fdp_ctx* c) {
+  if (!c) return fail(c, FDP_ERR_ARG, "null context");
+  CK(c, cudaStreamSynchronize(c->stream));
+  return FDP_OK;
+}
+
+int64_t fdp_kernel_launches(fdp_ctx* c) { return c ? c->launches : 0; }
+
+const char* fdp_last_error(const fdp_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+void fdp_destroy(fdp_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  DevArr* all[] = {&c->jm, &c->coef, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase};
+  for (auto* a : all) if (a->p) cudaFree(a->p);
+  for (auto& a : c->fields) if (a.p) cudaFree(a.p);
+  for (auto& a : c->prof) if (a.p) cudaFree(a.p);
+  for (auto& a : c->mem) if (a.p) cudaFree(a.p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+}  // extern "C"

@@ -1,0 +1,605 @@
+// Fused time-stepping kernels for the 2-D velocity-stress Biot poroelastic
+// scheme.  One launch of k_stress performs the whole stress phase of a time
+// level (time_loop.F90:93-124), one launch of k_velocity the whole velocity
+// phase including the bottom non-reflecting row (time_loop.F90:133-179), and
+// k_edge the one step with a cross-column dependency (the stress-imaging
+// row 1, hplane_1_velocity.F90:61-76) plus receiver sampling
+// (store_seismograms.F90:47-104, store_seismograms_pressure.F90:45-58).
+//
+// Every row routine of the reference (strain_*, stress_*, inh_*, sto_*)
+// becomes a branch on the cell's row and column class inside these kernels;
+// the arithmetic of each branch is written in the reference's evaluation
+// order and the code is compiled without FMA contraction, so a kernel's
+// results equal a serial CPU evaluation of the same routines bit for bit.
+//
+// Layout (all arrays x-fastest, the reference's column-major order):
+//   fields   T[NZ + 2*PADZ][pitch], pointer p.F points at (I=PMLL, L=0)
+//   JM       int32 in the field layout
+//   medium   derived per-material table coef[k*cld + jm], jm = 1..JMNUM
+//   x-PML profiles [L][J] (the reference's own layout), z-PML profiles
+//            stored transposed [J][I-PMLL] so a warp reads them coalesced
+//   memory variables in the reference's own bounds (ppml.F90:85-112)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fdp {
+
+// Derived material coefficients (one column per k, indexed by JM).
+// The exponential-integrator factors EXP(-REL3_Q) and
+// (REL2/REL3_Q)*(1-EXP(-REL3_Q)) that the reference re-evaluates at every
+// cell and step (inh_qx_int.F90:44, inh_v_uv_int.F90:46) depend only on the
+// material, so they are evaluated once per material on the host with the
+// same expression and C library.
+enum Coef {
+  C_MU = 0, C_SXX1, C_SXX2, C_SXX3, C_SZZ1, C_SZZ2, C_SZZ3, C_P1, C_P2, C_P3,
+  C_EQX, C_CU, C_R1QX, C_R2QX, C_R1U, C_R3U,
+  C_EQZ, C_CW, C_R1QZ, C_R2QZ, C_R1W, C_R3W,
+  C_AUXW, C_AUXQZ,
+  C_NCOEF
+};
+
+constexpr int kPadX = 4;
+constexpr int kPadZ = 2;
+
+template <class T> struct Params {
+  int MX, MZ, TPML, PMLL, PMLXH, PMLZH, NX, NZ, MX1, LIN_X, LIN_Z;
+  int pitch;    // field row pitch in elements
+  int tz, ntz;  // rows per z-tile and number of z-tiles
+  T AH, BH, CH, BC, A, B, DT, DTE;
+  T *UM, *WM, *QX, *QZ, *TXX, *TZZ, *TXZ, *PRES;
+  const int32_t* JM;
+  const T* coef;
+  long long cld;
+  // x-PML profiles, [L][J]: OD* with J in 0..TPML, OD2* with J in 0..TPML+1
+  const T *ODA_XL, *ODB_XL, *ODC_XL, *ODD_XL, *ODA_XH, *ODB_XH, *ODC_XH, *ODD_XH;
+  const T *ODA2_XL, *ODB2_XL, *ODC2_XL, *ODD2_XL, *ODA2_XH, *ODB2_XH, *ODC2_XH, *ODD2_XH;
+  // z-PML profiles, [J][I-PMLL]
+  const T *ODA_ZH, *ODB_ZH, *ODC_ZH, *ODD_ZH, *ODA2_ZH, *ODB2_ZH, *ODC2_ZH, *ODD2_ZH;
+  // memory variables (reference bounds)
+  T *PZXL, *PZXH, *PXXL, *PXXH, *OXXL, *OXXH, *PXZH, *PZZH, *OZZH;
+  T *RXXL, *RXXH, *SXXL, *SXXH, *RZXL, *RZXH, *GXXL, *GXXH, *HXXL, *HXXH, *GZXL, *GZXH;
+  T *RXZH, *GXZH, *RZZH, *SZZH, *GZZH, *HZZH;
+  // bottom non-reflecting row: AB[0..7] = ABW01..ABW22, AB[8..15] = ABH01..ABH22
+  const T* AB;
+  T* HIST;  // [4][3][NX]: SZ_U, SZ_W, SZ_QX, SZ_QZ; row k = TIKMZk
+  // source
+  const T* STF;
+  int MT2;
+  const int* it_base;
+  // receivers: REC[4*j..] = IRECX LRECX IRECZ LRECZ; RAW[(it-1)*MR*6 + j*6 + c]
+  int MR;
+  const int* REC;
+  T* RAW;
+};
+
+#define FDP_F(ptr, I, L) (ptr)[(long long)(L) * p.pitch + ((I) - p.PMLL)]
+#define FDP_C(k, j) p.coef[(long long)(k) * p.cld + (j)]
+
+// ---------------------------------------------------------------------------
+// strain_uw_xx.F90:51-94 / strain_q_xx.F90:50-91 for one cell
+template <class T>
+__device__ __forceinline__ T strain_xx(const Params<T>& p, const T* U, T* ML, T* MH, int I, int L) {
+  const int TPML = p.TPML;
+  if (I <= 1) {
+    const int xi = (2 - I) + L * (TPML + 1);
+    const int mi = (I - p.PMLL) + L * (TPML + 1);
+    const T D = p.CH * (FDP_F(U, I + 1, L) - FDP_F(U, I, L));
+    const T m = ML[mi];
+    const T e = p.ODA_XL[xi] * (p.ODD_XL[xi] * D + m);
+    ML[mi] = p.ODB_XL[xi] * m + p.ODC_XL[xi] * D;
+    return e;
+  }
+  if (I == 2) return p.CH * (FDP_F(U, 3, L) - FDP_F(U, 2, L));
+  if (I <= p.MX - 2)
+    return p.AH * (FDP_F(U, I + 2, L) - FDP_F(U, I - 1, L)) + p.BH * (FDP_F(U, I + 1, L) - FDP_F(U, I, L));
+  if (I == p.MX1) return p.CH * (FDP_F(U, p.MX1 + 1, L) - FDP_F(U, p.MX1, L));
+  const int xi = (I - p.MX1) + L * (TPML + 1);
+  const int mi = (I - p.MX) + L * (TPML + 1);
+  const T D = p.CH * (FDP_F(U, I + 1, L) - FDP_F(U, I, L));
+  const T m = MH[mi];
+  const T e = p.ODA_XH[xi] * (p.ODD_XH[xi] * D + m);
+  MH[mi] = p.ODB_XH[xi] * m + p.ODC_XH[xi] * D;
+  return e;
+}
+
+// strain_uw_zz.F90:41-51 / strain_q_zz.F90:41-52 (interior and non-imaging row 1)
+template <class T>
+__device__ __forceinline__ T strain_zz(const Params<T>& p, const T* W, int I, int L) {
+  T e = (p.CH * (FDP_F(W, I, L + 1) - FDP_F(W, I, L)));
+  if (I >= 2 && I <= p.MX1) e = p.AH * (FDP_F(W, I, L + 2) - FDP_F(W, I, L - 1)) + p.BC * e;
+  return e;
+}
+
+// strain_uw_zz_2nd_pml.F90:55-65 / strain_q_zz_2nd_pml.F90:51-64
+template <class T>
+__device__ __forceinline__ T strain_zz_pml(const Params<T>& p, const T* W, T* M, int I, int L, int LL) {
+  const int zi = (I - p.PMLL) + LL * p.NX;
+  const T D = p.CH * (FDP_F(W, I, L + 1) - FDP_F(W, I, L));
+  const T m = M[zi];
+  const T e = p.ODA_ZH[zi] * (p.ODD_ZH[zi] * D + m);
+  M[zi] = p.ODB_ZH[zi] * m + p.ODC_ZH[zi] * D;
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+// Stress update of one cell (I, L): the row routines of hplane_ic_stress,
+// hplane_lin_stress, hplane_0/1_stress (non-imaging), hplane_mz1_stress,
+// hplane_pml_stress and hplane_pmlzh0_stress restricted to that cell.
+template <class T, bool SI>
+__device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, int it) {
+  const int TPML = p.TPML, MX = p.MX, MX1 = p.MX1;
+  const bool last = (L == p.PMLZH);
+  const bool pml = (L >= p.MZ) && !last;
+  const bool mz1 = (L == p.MZ - 1);
+  const bool r0 = (!SI) && (L == 0);
+  const bool r1 = (!SI) && (L == 1);
+
+  // ---------------- EXZ and TXZ: I = 2-TPML .. MX+TPML (stress_xz.F90:40)
+  if (I >= 2 - TPML && I <= MX + TPML) {
+    T exz;
+    if (r0) {
+      exz = T(0);  // hplane_0_stress.F90:58
+    } else if (pml || last) {
+      // strain_uw_xz_2nd_pml.F90:69-121
+      const int LL = last ? TPML + 1 : L - p.MZ + 1;
+      const T DZXA = p.CH * (FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
+      const T DXZA = p.CH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1));
+      const int zi = (I - p.PMLL) + LL * p.NX;
+      const T mz = p.PXZH[zi];
+      const T zpart = p.ODA2_ZH[zi] * (p.ODD2_ZH[zi] * DXZA + mz);
+      if (I <= 2) {
+        const int xi = (3 - I) + L * (TPML + 2);
+        const int mi = (I - p.PMLL) + L * (TPML + 2);
+        const T mx = p.PZXL[mi];
+        exz = zpart + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
+        p.PZXL[mi] = p.ODB2_XL[xi] * mx + p.ODC2_XL[xi] * DZXA;
+      } else if (I <= MX1) {
+        exz = zpart + DZXA;
+      } else {
+        const int xi = (I - MX1) + L * (TPML + 2);
+        const int mi = (I - MX) + L * (TPML + 1);
+        const T mx = p.PZXH[mi];
+        exz = zpart + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
+        p.PZXH[mi] = p.ODB2_XH[xi] * mx + p.ODC2_XH[xi] * DZXA;
+      }
+      p.PXZH[zi] = p.ODB2_ZH[zi] * mz + p.ODC2_ZH[zi] * DXZA;
+    } else if (I <= 2) {
+      // strain_uw_xz.F90:181-196 (and strain_uw_xz_1.F90:62-76)
+      const T DZXA = p.CH * (FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
+      const int xi = (3 - I) + L * (TPML + 2);
+      const int mi = (I - p.PMLL) + L * (TPML + 2);
+      const T mx = p.PZXL[mi];
+      exz = p.CH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1)) + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
+      p.PZXL[mi] = p.ODB2_XL[xi] * mx + p.ODC2_XL[xi] * DZXA;
+    } else if (I <= MX1) {
+      if (r1) {
+        // strain_uw_xz_1.F90:79-97 (AFDA_XZ undefined)
+        exz = p.AH * (FDP_F(p.WM, I + 1, 1) - FDP_F(p.WM, I - 2, 1)) + p.BH * (FDP_F(p.WM, I, 1) - FDP_F(p.WM, I - 1, 1))
+            + p.CH * (FDP_F(p.UM, I, 1) - FDP_F(p.UM, I, 0));
+      } else {
+        // strain_uw_xz.F90:198-206
+        exz = p.AH * (FDP_F(p.UM, I, L + 1) - FDP_F(p.UM, I, L - 2) + FDP_F(p.WM, I + 1, L) - FDP_F(p.WM, I - 2, L))
+            + p.BH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1) + FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
+      }
+    } else {
+      // strain_uw_xz.F90:209-223
+      const T DZXA = p.CH * (FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
+      const int xi = (I - MX1) + L * (TPML + 2);
+      const int mi = (I - MX) + L * (TPML + 1);
+      const T mx = p.PZXH[mi];
+      exz = p.CH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1)) + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
+      p.PZXH[mi] = p.ODB2_XH[xi] * mx + p.ODC2_XH[xi] * DZXA;
+    }
+    const int J = FDP_F(p.JM, I, L);
+    const T TXZv = FDP_C(C_MU, J) * exz;
+    FDP_F(p.TXZ, I, L) = FDP_F(p.TXZ, I, L) + p.DTE * TXZv;
+  }
+  if (last) return;  // hplane_pmlzh0_stress.F90 updates TXZ only
+
+  // ---------------- normal stresses: I = 2-TPML .. MX-1+TPML (stress_nn.F90:49)
+  if (I < 2 - TPML || I > MX1 + TPML) return;
+  T ezz, qzz;
+  if (r0) {
+    ezz = (p.CH * (FDP_F(p.WM, I, 1) - FDP_F(p.WM, I, 0)));  // strain_uw_zz_0.F90:45-49
+    qzz = (p.CH * (FDP_F(p.QZ, I, 1) - FDP_F(p.QZ, I, 0)));  // strain_q_zz_0.F90:40-44
+  } else if (pml || mz1) {
+    const int LL = mz1 ? 0 : L - p.MZ + 1;
+    ezz = strain_zz_pml(p, p.WM, p.PZZH, I, L, LL);
+    qzz = strain_zz_pml(p, p.QZ, p.OZZH, I, L, LL);
+  } else {
+    ezz = strain_zz(p, p.WM, I, L);
+    qzz = strain_zz(p, p.QZ, I, L);
+  }
+  const T exx = strain_xx(p, p.UM, p.PXXL, p.PXXH, I, L);
+  const T qxx = strain_xx(p, p.QX, p.OXXL, p.OXXH, I, L);
+  const int J = FDP_F(p.JM, I, L);
+  const T s1 = FDP_C(C_SXX1, J), s2 = FDP_C(C_SXX2, J), s3 = FDP_C(C_SXX3, J);
+  const T z1 = FDP_C(C_SZZ1, J), z2 = FDP_C(C_SZZ2, J), z3 = FDP_C(C_SZZ3, J);
+  const T q1 = FDP_C(C_P1, J), q2 = FDP_C(C_P2, J), q3 = FDP_C(C_P3, J);
+  const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
+  const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
+  const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
+  if (L == p.LIN_Z && I == p.LIN_X) {
+    // stress_lin_nn.F90:58-63; SOURSP/SOURFP are the previous level's values
+    const T SOURS = p.STF[2 * (it - 1)], SOURF = p.STF[2 * (it - 1) + 1];
+    const T SOURSP = it > 1 ? p.STF[2 * (it - 2)] : T(0);
+    const T SOURFP = it > 1 ? p.STF[2 * (it - 2) + 1] : T(0);
+    FDP_F(p.TXX, I, L) = FDP_F(p.TXX, I, L) + p.DTE * (TXXv - ((SOURS - SOURSP) / p.DT));
+    FDP_F(p.TZZ, I, L) = FDP_F(p.TZZ, I, L) + p.DTE * (TZZv - ((SOURS - SOURSP) / p.DT));
+    FDP_F(p.PRES, I, L) = FDP_F(p.PRES, I, L) + p.DTE * (PRv + ((SOURF - SOURFP) / p.DT));
+  } else {
+    FDP_F(p.TXX, I, L) = FDP_F(p.TXX, I, L) + p.DTE * TXXv;
+    FDP_F(p.TZZ, I, L) = FDP_F(p.TZZ, I, L) + p.DTE * TZZv;
+    FDP_F(p.PRES, I, L) = FDP_F(p.PRES, I, L) + p.DTE * PRv;
+  }
+}
+
+// One thread per column I, marching down the rows of one z-tile.
+template <class T, bool SI>
+__global__ void __launch_bounds__(128) k_stress(const __grid_constant__ Params<T> p, int it_off) {
+  const int I = p.PMLL + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (I > p.PMLXH) return;
+  const int t = blockIdx.y;
+  const int L0 = t * p.tz;
+  const int L1 = (t == p.ntz - 1) ? p.NZ : L0 + p.tz;
+  const int it = *p.it_base + it_off;
+  for (int L = (SI ? max(L0, 2) : L0); L < L1; ++L) stress_cell<T, SI>(p, I, L, it);
+  if (SI && t == 0) {
+    // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53, after rows 2..4
+    FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
+    FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
+    FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
+    FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
+    FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
+    FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
+    FDP_F(p.TXZ, I, 2) = T(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Velocity update of one cell (I, L), L < PMLZH: hplane_ic_velocity,
+// hplane_pml_velocity and, without stress imaging, hplane_0/1_velocity.
+// The old q at the cell stands in for QXP/QZP: STO_QXP/STO_QZP copy q right
+// after its update over exactly the columns and rows where u and w read the
+// copy (sto_qxp.F90:24, sto_qzp.F90:24), so QXP(I,L) always equals the q of
+// the previous level at that cell.
+template <class T, bool SI>
+__device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) {
+  const int TPML = p.TPML, MX = p.MX, MX1 = p.MX1;
+  const bool pml = (L >= p.MZ - 1);
+  const T A = p.A, B = p.B;
+
+  // ---------------- qx and u: I = 3-TPML .. MX-1+TPML
+  if (I >= 3 - TPML && I <= MX1 + TPML) {
+    const int J = FDP_F(p.JM, I, L);
+    const T E = FDP_C(C_EQX, J), Cu = FDP_C(C_CU, J);
+    const T R1 = FDP_C(C_R1QX, J), R2 = FDP_C(C_R2QX, J), R1u = FDP_C(C_R1U, J), R3u = FDP_C(C_R3U, J);
+    const T qx0 = FDP_F(p.QX, I, L);
+    const T u0 = FDP_F(p.UM, I, L);
+    T qx, u;
+    if (pml) {
+      // inh_qx_int_2nd_pml.F90 / inh_v_u_int_2nd_pml.F90
+      const int LL = L - p.MZ + 1;
+      const int zi = (I - p.PMLL) + LL * p.NX;
+      const T DXXXA = FDP_F(p.TXX, I, L) - FDP_F(p.TXX, I - 1, L);
+      const T DXZZA = FDP_F(p.TXZ, I, L + 1) - FDP_F(p.TXZ, I, L);
+      const T PXXXA = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L);
+      const T za = p.ODA_ZH[zi], zd = p.ODD_ZH[zi], zb = p.ODB_ZH[zi], zc = p.ODC_ZH[zi];
+      const T gz = p.GXZH[zi], rz = p.RXZH[zi];
+      if (I <= 3 || I >= MX1) {
+        int xi, mi;
+        const T *xa_, *xd_, *xb_, *xc_;
+        T *G, *H, *R, *S;
+        if (I <= 3) {
+          xi = (3 - I) + L * (TPML + 2); mi = (I - p.PMLL) + L * (TPML + 3);
+          xa_ = p.ODA2_XL; xd_ = p.ODD2_XL; xb_ = p.ODB2_XL; xc_ = p.ODC2_XL;
+          G = p.GXXL; H = p.HXXL; R = p.RXXL; S = p.SXXL;
+        } else {
+          xi = (I - MX1) + L * (TPML + 2); mi = (I - (MX - 1)) + L * (TPML + 2);
+          xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
+          G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
+        }
+        const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
+        const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
+        qx = E * qx0 - R1 * (xa * (xd * DXXXA + g)) - R1 * (za * (zd * DXZZA + gz)) - R2 * (xa * (xd * PXXXA + h));
+        u = u0 + Cu * qx0 + R1u * (xa * (xd * DXXXA + r) + za * (zd * DXZZA + rz)) + R3u * (xa * (xd * PXXXA + s));
+        G[mi] = xb * g + xc * DXXXA;
+        H[mi] = xb * h + xc * PXXXA;
+        R[mi] = xb * r + xc * DXXXA;
+        S[mi] = xb * s + xc * PXXXA;
+      } else {
+        qx = E * qx0 - R1 * (za * (zd * DXZZA + gz) + DXXXA) - R2 * (FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L));
+        u = u0 + Cu * qx0 + R1u * (DXXXA + za * (zd * DXZZA + rz)) + R3u * PXXXA;
+      }
+      p.GXZH[zi] = zb * gz + zc * DXZZA;
+      p.RXZH[zi] = zb * rz + zc * DXZZA;
+    } else if (SI || L >= 1) {
+      // interior rows, and row 1 without stress imaging (the same routines)
+      if (I <= 3 || I >= MX1) {
+        // inh_qx_2nd.F90 / inh_v_u_2nd.F90
+        int xi, mi;
+        const T *xa_, *xd_, *xb_, *xc_;
+        T *G, *H, *R, *S;
+        if (I <= 3) {
+          xi = (3 - I) + L * (TPML + 2); mi = (I - p.PMLL) + L * (TPML + 3);
+          xa_ = p.ODA2_XL; xd_ = p.ODD2_XL; xb_ = p.ODB2_XL; xc_ = p.ODC2_XL;
+          G = p.GXXL; H = p.HXXL; R = p.RXXL; S = p.SXXL;
+        } else {
+          xi = (I - MX1) + L * (TPML + 2); mi = (I - (MX - 1)) + L * (TPML + 2);
+          xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
+          G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
+        }
+        const T DXXXA = FDP_F(p.TXX, I, L) - FDP_F(p.TXX, I - 1, L);
+        const T PXXXA = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L);
+        const T txz1 = FDP_F(p.TXZ, I, L + 1), txz0 = FDP_F(p.TXZ, I, L);
+        const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
+        const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
+        qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1 - txz0) - R2 * (xa * (xd * PXXXA + h));
+        u = u0 + Cu * qx0 + R1u * (xa * (xd * DXXXA + r) + txz1 - txz0) + R3u * (xa * (xd * PXXXA + s));
+        G[mi] = xb * g + xc * DXXXA;
+        H[mi] = xb * h + xc * PXXXA;
+        R[mi] = xb * r + xc * DXXXA;
+        S[mi] = xb * s + xc * PXXXA;
+      } else {
+        // inh_qx_int.F90:40-54 / inh_v_uv_int.F90:41-56
+        const T X = A * (FDP_F(p.TXX, I + 1, L) - FDP_F(p.TXX, I - 2, L) + FDP_F(p.TXZ, I, L + 2) - FDP_F(p.TXZ, I, L - 1))
+                  + B * (FDP_F(p.TXX, I, L) - FDP_F(p.TXX, I - 1, L) + FDP_F(p.TXZ, I, L + 1) - FDP_F(p.TXZ, I, L));
+        const T P = A * (FDP_F(p.PRES, I + 1, L) - FDP_F(p.PRES, I - 2, L)) + B * (FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L));
+        qx = E * qx0 - R1 * X - R2 * P;
+        u = u0 + Cu * qx0 + R1u * X + R3u * P;
+      }
+    } else {
+      // row 0 without stress imaging: inh_qx_int_0.F90, inh_v_uv_int_0.F90,
+      // inh_qx_2nd_0.F90, inh_v_u_2nd_0.F90
+      if (I <= 3 || I >= MX1) {
+        int xi, mi;
+        const T *xa_, *xd_, *xb_, *xc_;
+        T *G, *H, *R, *S;
+        if (I <= 3) {
+          xi = (3 - I); mi = (I - p.PMLL);
+          xa_ = p.ODA2_XL; xd_ = p.ODD2_XL; xb_ = p.ODB2_XL; xc_ = p.ODC2_XL;
+          G = p.GXXL; H = p.HXXL; R = p.RXXL; S = p.SXXL;
+        } else {
+          xi = (I - MX1); mi = (I - (MX - 1));
+          xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
+          G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
+        }
+        const T DXXXA = FDP_F(p.TXX, I, 0) - FDP_F(p.TXX, I - 1, 0);
+        const T PXXXA = FDP_F(p.PRES, I, 0) - FDP_F(p.PRES, I - 1, 0);
+        const T txz1 = FDP_F(p.TXZ, I, 1);
+        const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
+        const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
+        qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1) - R2 * (xa * (xd * PXXXA + h));
+        u = u0 + Cu * qx0 + R1u * (xa * (xd * DXXXA + r) + txz1) + R3u * (xa * (xd * PXXXA + s));
+        G[mi] = xb * g + xc * DXXXA;
+        H[mi] = xb * h + xc * PXXXA;
+        R[mi] = xb * r + xc * DXXXA;
+        S[mi] = xb * s + xc * PXXXA;
+      } else {
+        const T X = A * (FDP_F(p.TXX, I + 1, 0) - FDP_F(p.TXX, I - 2, 0)) + B * (FDP_F(p.TXX, I, 0) - FDP_F(p.TXX, I - 1, 0))
+                  + T(17) / T(24) * FDP_F(p.TXZ, I, 1) + T(3) / T(8) * FDP_F(p.TXZ, I, 2)
+                  - T(5) / T(24) * FDP_F(p.TXZ, I, 3) + T(1) / T(24) * FDP_F(p.TXZ, I, 4);
+        const T P = A * (FDP_F(p.PRES, I + 1, 0) - FDP_F(p.PRES, I - 2, 0)) + B * (FDP_F(p.PRES, I, 0) - FDP_F(p.PRES, I - 1, 0));
+        qx = E * qx0 - R1 * X - R2 * P;
+        u = u0 + Cu * qx0 + R1u * X + R3u * P;
+      }
+    }
+    FDP_F(p.QX, I, L) = qx;
+    FDP_F(p.UM, I, L) = u;
+  }
+
+  // ---------------- qz and w: I = 2-TPML .. MX-1+TPML
+  if (I >= 2 - TPML && I <= MX1 + TPML) {
+    const int J = FDP_F(p.JM, I, L);
+    const T E = FDP_C(C_EQZ, J), Cw = FDP_C(C_CW, J);
+    const T R1 = FDP_C(C_R1QZ, J), R2 = FDP_C(C_R2QZ, J), R1w = FDP_C(C_R1W, J), R3w = FDP_C(C_R3W, J);
+    const T qz0 = FDP_F(p.QZ, I, L);
+    const T w0 = FDP_F(p.WM, I, L);
+    T qz, w;
+    if (pml) {
+      // inh_qz_int_2nd_pml.F90 / inh_v_w_int_2nd_pml.F90
+      const int LL = L - p.MZ + 1;
+      const int zi = (I - p.PMLL) + LL * p.NX;
+      const T DXZXA = FDP_F(p.TXZ, I + 1, L) - FDP_F(p.TXZ, I, L);
+      const T DZZZA = FDP_F(p.TZZ, I, L) - FDP_F(p.TZZ, I, L - 1);
+      const T PZZZA = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I, L - 1);
+      const T za = p.ODA2_ZH[zi], zd = p.ODD2_ZH[zi], zb = p.ODB2_ZH[zi], zc = p.ODC2_ZH[zi];
+      const T gz = p.GZZH[zi], hz = p.HZZH[zi], rz = p.RZZH[zi], sz = p.SZZH[zi];
+      if (I <= 2 || I >= MX1) {
+        int xi, mi;
+        const T *xa_, *xd_, *xb_, *xc_;
+        T *G, *R;
+        if (I <= 2) {
+          xi = (2 - I) + L * (TPML + 1); mi = (I - p.PMLL) + L * (TPML + 2);
+          xa_ = p.ODA_XL; xd_ = p.ODD_XL; xb_ = p.ODB_XL; xc_ = p.ODC_XL; G = p.GZXL; R = p.RZXL;
+        } else {
+          xi = (I - MX1) + L * (TPML + 1); mi = (I - (MX - 1)) + L * (TPML + 2);
+          xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; R = p.RZXH;
+        }
+        const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
+        const T g = G[mi], r = R[mi];
+        qz = E * qz0 - R1 * (za * (zd * DZZZA + gz)) - R1 * (xa * (xd * DXZXA + g)) - R2 * (za * (zd * PZZZA + hz));
+        w = w0 + Cw * qz0 + R1w * (za * (zd * DZZZA + rz) + xa * (xd * DXZXA + r)) + R3w * (za * (zd * PZZZA + sz));
+        G[mi] = xb * g + xc * DXZXA;
+        R[mi] = xb * r + xc * DXZXA;
+      } else {
+        qz = E * qz0 - R1 * (za * (zd * DZZZA + gz) + DXZXA) - R2 * (za * (zd * PZZZA + hz));
+        w = w0 + Cw * qz0 + R1w * (za * (zd * DZZZA + rz) + DXZXA) + R3w * (za * (zd * PZZZA + sz));
+      }
+      p.GZZH[zi] = zb * gz + zc * DZZZA;
+      p.HZZH[zi] = zb * hz + zc * PZZZA;
+      p.RZZH[zi] = zb * rz + zc * DZZZA;
+      p.SZZH[zi] = zb * sz + zc * PZZZA;
+    } else if (SI || L >= 1) {
+      if (I <= 2 || I >= MX1) {
+        // inh_qz_2nd.F90 / inh_v_w_2nd.F90 (also row 1 without stress imaging)
+        int xi, mi;
+        const T *xa_, *xd_, *xb_, *xc_;
+        T *G, *R;
+        if (I <= 2) {
+          xi = (2 - I) + L * (TPML + 1); mi = (I - p.PMLL) + L * (TPML + 2);
+          xa_ = p.ODA_XL; xd_ = p.ODD_XL; xb_ = p.ODB_XL; xc_ = p.ODC_XL; G = p.GZXL; R = p.RZXL;
+        } else {
+          xi = (I - MX1) + L * (TPML + 1); mi = (I - (MX - 1)) + L * (TPML + 2);
+          xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; R = p.RZXH;
+        }
+        const T DXZXA = FDP_F(p.TXZ, I + 1, L) - FDP_F(p.TXZ, I, L);
+        const T dzz = FDP_F(p.TZZ, I, L) - FDP_F(p.TZZ, I, L - 1);
+        const T dp = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I, L - 1);
+        const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
+        const T g = G[mi], r = R[mi];
+        qz = E * qz0 - R1 * (dzz + xa * (xd * DXZXA + g)) - R2 * dp;
+        w = w0 + Cw * qz0 + R1w * (dzz + xa * (xd * DXZXA + r)) + R3w * dp;
+        G[mi] = xb * g + xc * DXZXA;
+        R[mi] = xb * r + xc * DXZXA;
+      } else if (SI || L >= 2) {
+        // inh_qz_int.F90:41-55 / inh_v_w_int.F90:43-58
+        const T X = A * (FDP_F(p.TZZ, I, L + 1) - FDP_F(p.TZZ, I, L - 2) + FDP_F(p.TXZ, I + 2, L) - FDP_F(p.TXZ, I - 1, L))
+                  + B * (FDP_F(p.TZZ, I, L) - FDP_F(p.TZZ, I, L - 1) + FDP_F(p.TXZ, I + 1, L) - FDP_F(p.TXZ, I, L));
+        const T P = A * (FDP_F(p.PRES, I, L + 1) - FDP_F(p.PRES, I, L - 2)) + B * (FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I, L - 1));
+        qz = E * qz0 - R1 * X - R2 * P;
+        w = w0 + Cw * qz0 + R1w * X + R3w * P;
+      } else {
+        // row 1 without stress imaging: inh_v_qz_int_1.F90 / inh_v_w_int_1.F90
+        const T X = A * (FDP_F(p.TXZ, I + 2, 1) - FDP_F(p.TXZ, I - 1, 1)) + B * (FDP_F(p.TXZ, I + 1, 1) - FDP_F(p.TXZ, I, 1))
+                  - T(31) / T(24) * FDP_F(p.TZZ, I, 0) + T(29) / T(24) * FDP_F(p.TZZ, I, 1)
+                  - T(3) / T(40) * FDP_F(p.TZZ, I, 2) + T(1) / T(168) * FDP_F(p.TZZ, I, 3);
+        const T P = -T(31) / T(24) * FDP_F(p.PRES, I, 0) + T(29) / T(24) * FDP_F(p.PRES, I, 1)
+                  - T(3) / T(40) * FDP_F(p.PRES, I, 2) + T(1) / T(168) * FDP_F(p.PRES, I, 3);
+        qz = E * qz0 - R1 * X - R2 * P;
+        w = w0 + Cw * qz0 + R1w * X + R3w * P;
+      }
+    } else {
+      // row 0 without stress imaging: inh_qz_int_0.F90, inh_v_w_int_0.F90,
+      // inh_qz_2nd_0.F90, inh_v_w_2nd_0.F90
+      T X, P;
+      if (I <= 2 || I >= MX1) {
+        X = T(3) * FDP_F(p.TZZ, I, 0) - T(1) / T(3) * FDP_F(p.TZZ, I, 1);
+        P = T(3) * FDP_F(p.PRES, I, 0) - T(1) / T(3) * FDP_F(p.PRES, I, 1);
+      } else {
+        X = T(35) / T(8) * FDP_F(p.TZZ, I, 0) - T(35) / T(24) * FDP_F(p.TZZ, I, 1)
+          + T(21) / T(40) * FDP_F(p.TZZ, I, 2) - T(5) / T(56) * FDP_F(p.TZZ, I, 3);
+        P = T(35) / T(8) * FDP_F(p.PRES, I, 0) - T(35) / T(24) * FDP_F(p.PRES, I, 1)
+          + T(21) / T(40) * FDP_F(p.PRES, I, 2) - T(5) / T(56) * FDP_F(p.PRES, I, 3);
+      }
+      qz = E * qz0 - R1 * X - R2 * P;
+      w = w0 + Cw * qz0 + R1w * X + R3w * P;
+    }
+    FDP_F(p.QZ, I, L) = qz;
+    FDP_F(p.WM, I, L) = w;
+  }
+}
+
+// One thread per column I, marching down the rows of one z-tile.  The last
+// tile holds at least the rows PMLZH-2..PMLZH, so the bottom row's inputs
+// (the new rows PMLZH-1 and PMLZH-2, and their values before this phase)
+// are all produced by the same thread.
+template <class T, bool SI>
+__global__ void __launch_bounds__(128) k_velocity(const __grid_constant__ Params<T> p, int it_off) {
+  (void)it_off;
+  const int I = p.PMLL + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (I > p.PMLXH) return;
+  const int t = blockIdx.y;
+  const int L0 = t * p.tz;
+  const bool lastTile = (t == p.ntz - 1);
+  const int L1 = lastTile ? p.NZ : L0 + p.tz;
+  const int Lstop = lastTile ? p.PMLZH : L1;
+  T h[3][4];  // old rows PMLZH (k=0), PMLZH-1 (k=1), PMLZH-2 (k=2) for u, w, qx, qz
+  for (int L = (SI ? max(L0, 2) : L0); L < Lstop; ++L) {
+    if (lastTile && L >= p.PMLZH - 2) {
+      const int k = p.PMLZH - L;
+      h[k][0] = FDP_F(p.UM, I, L); h[k][1] = FDP_F(p.WM, I, L);
+      h[k][2] = FDP_F(p.QX, I, L); h[k][3] = FDP_F(p.QZ, I, L);
+    }
+    velocity_cell<T, SI>(p, I, L);
+  }
+  if (lastTile) {
+    // time_loop.F90:133-155 and hplane_pmlzh0_velocity.F90:34-63
+    const int LST = p.PMLZH;
+    h[0][0] = FDP_F(p.UM, I, LST); h[0][1] = FDP_F(p.WM, I, LST);
+    h[0][2] = FDP_F(p.QX, I, LST); h[0][3] = FDP_F(p.QZ, I, LST);
+    T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+    const int x = I - p.PMLL;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
+      T* hist = p.HIST + (long long)c * 3 * p.NX;
+      const T sp0 = hist[x], sp1 = hist[p.NX + x], sp2 = hist[2 * p.NX + x];
+      const T v = ab[0] * FDP_F(f[c], I, LST - 1) + ab[1] * FDP_F(f[c], I, LST - 2)
+                + ab[2] * h[0][c] + ab[3] * h[1][c] + ab[4] * h[2][c]
+                + ab[5] * sp0 + ab[6] * sp1 + ab[7] * sp2;
+      FDP_F(f[c], I, LST) = v;
+      hist[x] = h[0][c];
+      hist[p.NX + x] = h[1][c];
+      hist[2 * p.NX + x] = h[2][c];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stress-imaging row 1 (inh_v_qx_int_1_si.F90:26-31, inh_w_qz_int_1_si.F90:30-44),
+// from the final rows 2 and 3.  Returns the row-1 value of u (c=0), w (1),
+// qx (2) or qz (3) at column I, or the stored value where row 1 is not updated.
+template <class T>
+__device__ __forceinline__ T si_row1(const Params<T>& p, int c, int I) {
+  const int TPML = p.TPML, MX = p.MX;
+  auto u1 = [&](int i) { return FDP_F(p.UM, i, 2) + FDP_F(p.WM, i, 2) - FDP_F(p.WM, i - 1, 2); };
+  auto q1 = [&](int i) { return FDP_F(p.QX, i, 2) + FDP_F(p.QZ, i, 2) - FDP_F(p.QZ, i - 1, 2); };
+  if (c == 0) return (I >= 3 - TPML && I <= MX - 1 + TPML) ? u1(I) : FDP_F(p.UM, I, 1);
+  if (c == 2) return (I >= 3 - TPML && I <= MX - 1 + TPML) ? q1(I) : FDP_F(p.QX, I, 1);
+  if (I < 3 - TPML || I > MX - 2 + TPML) return c == 1 ? FDP_F(p.WM, I, 1) : FDP_F(p.QZ, I, 1);
+  const int J = FDP_F(p.JM, I, 0);
+  const T du = u1(I + 1) - u1(I) + FDP_F(p.UM, I + 1, 2) - FDP_F(p.UM, I, 2);
+  if (c == 1) return FDP_F(p.WM, I, 3) + FDP_C(C_AUXW, J) * du;
+  return FDP_F(p.QZ, I, 3) + FDP_C(C_AUXQZ, J) * du + (q1(I + 1) - q1(I) + FDP_F(p.QX, I + 1, 2) - FDP_F(p.QX, I, 2));
+}
+
+template <class T, bool SI>
+__device__ __forceinline__ T final_value(const Params<T>& p, int c, int I, int L) {
+  if (SI && L == 1) return si_row1(p, c, I);
+  const T* f = c == 0 ? p.UM : c == 1 ? p.WM : c == 2 ? p.QX : p.QZ;
+  return FDP_F(f, I, L);
+}
+
+// Row 1 under stress imaging (threads 0..NX-1) and receiver sampling
+// (threads 0..MR-1).  Sampling recomputes row-1 values instead of reading
+// them, so it does not depend on the order in which threads write row 1.
+template <class T, bool SI>
+__global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> p, int it_off) {
+  const int g = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (SI) {
+    const int I = p.PMLL + g;
+    if (I <= p.PMLXH && I >= 3 - p.TPML && I <= p.MX - 1 + p.TPML) {
+      const T u = si_row1(p, 0, I), qx = si_row1(p, 2, I);
+      T w = T(0), qz = T(0);
+      const bool wq = (I <= p.MX - 2 + p.TPML);
+      if (wq) { w = si_row1(p, 1, I); qz = si_row1(p, 3, I); }
+      // all reads of row 1 above come before any write; another thread's
+      // row-1 cells are recomputed from rows 2 and 3, never read
+      FDP_F(p.UM, I, 1) = u;
+      FDP_F(p.QX, I, 1) = qx;
+      if (wq) { FDP_F(p.WM, I, 1) = w; FDP_F(p.QZ, I, 1) = qz; }
+    }
+  }
+  if (g < p.MR) {
+    const int it = *p.it_base + it_off;
+    const int IX = p.REC[4 * g], LX = p.REC[4 * g + 1], IZ = p.REC[4 * g + 2], LZ = p.REC[4 * g + 3];
+    auto inside = [&](int i, int l) { return i >= p.PMLL && i <= p.PMLXH && l >= 0 && l <= p.PMLZH; };
+    T s[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    if (inside(IX, LX)) { s[0] = final_value<T, SI>(p, 0, IX, LX); s[2] = final_value<T, SI>(p, 2, IX, LX); }
+    if (inside(IZ, LZ)) { s[1] = -final_value<T, SI>(p, 1, IZ, LZ); s[3] = -final_value<T, SI>(p, 3, IZ, LZ); }
+    if (inside(IZ, LX)) { s[4] = FDP_F(p.PRES, IZ, LX); s[5] = -FDP_F(p.TXX, IZ, LX); }
+    T* out = p.RAW + ((long long)(it - 1) * p.MR + g) * 6;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) out[k] = s[k];
+  }
+}
+
+__global__ void k_set_base(int* base, int v) { *base = v; }
+__global__ void k_add_base(int* base, int v) { *base += v; }
+
+#undef FDP_F
+#undef FDP_C
+
+}  // namespace fdp

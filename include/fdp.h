@@ -1,0 +1,175 @@
+/*
+ * fdp.h -- C ABI of the GB300 time-stepping engine for the 2-D
+ * velocity-stress Biot poroelastic finite-difference simulator
+ * (drop-in for the TIME_LOOP body of David011/2D-VQSP-FD-Sim).
+ *
+ * The reference has no plugin or FFI API: its seam is the TIME_LOOP
+ * subroutine (time_loop.F90:3-209) and the module state it USEs
+ * (WAVEFIELD, STRESSFIELD, GRID_MEDIUM, PML, NONREF_BOUND, AUXIL,
+ * CONTROL_DATA).  Each entry point below replaces one piece of that
+ * seam; the comment on each names the reference code it stands in for.
+ *
+ * Conventions
+ *   - Every function returns FDP_OK (0) on success or a negative FDP_ERR_*
+ *     code; fdp_last_error() gives a one-line message.  Nothing throws.
+ *   - Host arrays use the reference's Fortran layout: column-major, x
+ *     fastest, with the Fortran lower bounds stated per argument (PMLL =
+ *     1-TPML may be negative, rows start at 0).  No transposition is needed
+ *     by a Fortran caller.
+ *   - Real-valued host arrays are in the precision selected at fdp_create
+ *     (FDP_F32 = REAL(4), FDP_F64 = REAL(8)); that is the reference's
+ *     working precision PP (mod_precision.F90:7,10).
+ *   - The context owns all device memory; the caller owns all host memory.
+ *   - One host thread per context; one CUDA stream per context.  fdp_run
+ *     only enqueues work; fdp_get_* and fdp_synchronize wait for it.
+ */
+#ifndef FDP_H
+#define FDP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDP_OK 0
+#define FDP_ERR_ARG (-1)         /* invalid argument or unsupported geometry   */
+#define FDP_ERR_CUDA (-2)        /* a CUDA runtime call failed                 */
+#define FDP_ERR_ALLOC (-3)       /* device or host allocation failed           */
+#define FDP_ERR_STATE (-4)       /* call out of order (e.g. run before set_*)  */
+#define FDP_ERR_UNSUPPORTED (-5) /* field not held by this engine              */
+
+#define FDP_F32 4
+#define FDP_F64 8
+
+/* Grid and control data.  Mirrors CONTROL_DATA/AUXIL after READ_OPEN and
+ * AUX1 (read_open.F90:245-272, aux1.F90:36-46): mz is the value after the
+ * stress-imaging shift MZ=MZ+2 (read_open.F90:250-252) and lin_z the source
+ * row after the +2H shift (read_open.F90:266-270). */
+typedef struct fdp_grid {
+  int32_t mx, mz;          /* MX, MZ                                          */
+  int32_t tpml;            /* TPML, PML thickness in cells                    */
+  int32_t stress_imaging;  /* STRESS_IMAGING (1) or one-sided free surface (0) */
+  int32_t lin_x, lin_z;    /* source cell LIN_X, LIN_Z                        */
+  int32_t precision;       /* FDP_F32 or FDP_F64                              */
+  int32_t device;          /* CUDA device ordinal                             */
+  double h, dt, tau_eps;   /* H, DT, TAU_EPS (READ_OPEN forces TAU_EPS=0)     */
+} fdp_grid;
+
+typedef struct fdp_ctx fdp_ctx;
+
+/* Field identifiers for fdp_get_field / fdp_set_field / fdp_field_bounds.
+ * Bounds are those of the reference's arrays (ppml.F90:85-112,
+ * tl_alloc.F90:233-245, alloc_nr.F90:33-40). */
+enum fdp_field_id {
+  FDP_UM = 0, FDP_WM, FDP_QX, FDP_QZ, FDP_TXX, FDP_TZZ, FDP_TXZ, FDP_PRES,
+  FDP_PZXL, FDP_PZXH, FDP_PXXL, FDP_PXXH, FDP_OXXL, FDP_OXXH, FDP_PXZH, FDP_PZZH, FDP_OZZH,
+  FDP_RXXL, FDP_RXXH, FDP_SXXL, FDP_SXXH, FDP_RZXL, FDP_RZXH, FDP_GXXL, FDP_GXXH,
+  FDP_HXXL, FDP_HXXH, FDP_GZXL, FDP_GZXH, FDP_RXZH, FDP_GXZH, FDP_RZZH, FDP_SZZH,
+  FDP_GZZH, FDP_HZZH,
+  /* bottom-row history SZ_U/SZ_W/SZ_QX/SZ_QZ (mod_nr_bound.F90:43-47) as
+   * (PMLL:PMLXH, 0:2), row k holding component TIKMZk */
+  FDP_SZ_U, FDP_SZ_W, FDP_SZ_QX, FDP_SZ_QZ,
+  /* QXP/QZP (old-q copies): not stored by this engine, which reads the
+   * pre-update q at the same cell instead; get/set return FDP_ERR_UNSUPPORTED */
+  FDP_QXP, FDP_QZP,
+  FDP_FIELD_COUNT
+};
+
+/* Snapshot mask bits for fdp_get_snapshot. */
+#define FDP_SNAP_UM (1 << 0)
+#define FDP_SNAP_WM (1 << 1)
+#define FDP_SNAP_QX (1 << 2)
+#define FDP_SNAP_QZ (1 << 3)
+
+/* Receiver flags for fdp_set_receivers (KEYS namelist, read_open.F90:153). */
+#define FDP_REC_TLV (1 << 0) /* KEY_TLV: u, -w (store_seismograms.F90)        */
+#define FDP_REC_TLQ (1 << 1) /* KEY_TLQ: qx, -qz                              */
+#define FDP_REC_TLP (1 << 2) /* KEY_TLP: p, -txx (store_seismograms_pressure) */
+
+/* Number of values per receiver per time level returned by
+ * fdp_get_receivers, in this order:
+ *   SSU SSW SPU SPW        (REC_UW_<j>.asc columns 2-5, store_seismograms.F90:144)
+ *   SSQX SSQZ ZPU ZPW      (REC_Q_<j>.asc columns 2-5, store_seismograms.F90:150)
+ *   SSP SST                (REC_STRESS_<j>.asc columns 2-3, store_seismograms_pressure.F90:80) */
+#define FDP_REC_VALUES 10
+
+/* Creates a context and allocates the device state, zeroed as TL_ALLOC,
+ * PPML and ALLOC_NR do (tl_alloc.F90:253-265, ppml.F90:115-153,
+ * alloc_nr.F90:42-54).  Replaces the allocations of TL_ALLOC/PPML/ALLOC_NR. */
+int fdp_create(const fdp_grid* grid, fdp_ctx** out);
+
+/* Medium: JM(PMLL:PMLXH, 0:PMLZH) (nx = MX+2*TPML, nz = PMLZH+1) after
+ * READ_MODEL's row/column replication (read_model.F90:57-89), and the
+ * material table as READ_MODEL_PAR holds it after scaling
+ * (read_model_par.F90:147-169): table24[(jm-1)*24 + k], k in the .MO record
+ * order MU SIG_XX_1..3 SIG_ZZ_1..3 PRES_1..3 REL1_U REL1_W REL2_U REL2_W
+ * REL3_U REL3_W REL1_QX REL1_QZ REL2_QX REL2_QZ REL3_QX REL3_QZ AUXIL_W
+ * AUXIL_QZ, REL* already multiplied by DT and divided by H as
+ * read_model_par.F90:158-169 does. */
+int fdp_set_medium(fdp_ctx* ctx, const int32_t* jm, int32_t nx, int32_t nz, int32_t jmnum,
+                   const void* table24);
+
+/* PML damping profiles from PPML (ppml.F90:156-306), 24 arrays in this order:
+ *   ODA_XL ODB_XL ODC_XL ODD_XL ODA_XH ODB_XH ODC_XH ODD_XH      (0:TPML,   0:PMLZH)
+ *   ODA_ZH ODB_ZH ODC_ZH ODD_ZH                                  (0:TPML,   PMLL:PMLXH)
+ *   ODA2_XL ODB2_XL ODC2_XL ODD2_XL ODA2_XH ODB2_XH ODC2_XH ODD2_XH (0:TPML+1, 0:PMLZH)
+ *   ODA2_ZH ODB2_ZH ODC2_ZH ODD2_ZH                              (0:TPML+1, PMLL:PMLXH) */
+int fdp_set_pml(fdp_ctx* ctx, const void* const* profiles24);
+
+/* Bottom non-reflecting coefficients from PRE_NR_COEF1 (pre_nr_coef1.F90:187-202):
+ * ABW01 ABW02 ABW10 ABW11 ABW12 ABW20 ABW21 ABW22 ABH01 ... ABH22. */
+int fdp_set_bottom_nr(fdp_ctx* ctx, const void* ab16);
+
+/* Source time function SOURTF_A(2, MT2) (open_sr_file.F90:41-110), column-major:
+ * sourtf[2*(it-1)] = solid part, sourtf[2*(it-1)+1] = fluid part. */
+int fdp_set_source(fdp_ctx* ctx, const void* sourtf, int32_t mt2);
+
+/* Receivers IRECX, LRECX, IRECZ, LRECZ (read_open.F90:326-337) and the
+ * FDP_REC_* flags (KEY_TLV/KEY_TLQ/KEY_TLP).  Replaces the sampling part of
+ * STORE_SEISMOGRAMS / STORE_SEISMOGRAMS_PRESSURE. */
+int fdp_set_receivers(fdp_ctx* ctx, const int32_t* irecx, const int32_t* lrecx, const int32_t* irecz,
+                      const int32_t* lrecz, int32_t mr, int32_t flags);
+
+/* Advances time levels it_begin..it_end (1-based, inclusive, it_end <= MT2):
+ * the body of DO ITILE = MT1, MT2 (time_loop.F90:65-206) without its file
+ * output.  Asynchronous. */
+int fdp_run(fdp_ctx* ctx, int32_t it_begin, int32_t it_end);
+
+/* Copies receiver values of levels it_first..it_first+n_levels-1 (already
+ * run) to host: n_levels * MR * FDP_REC_VALUES values, level-major.  The
+ * values are exactly what STORE_SEISMOGRAMS(_PRESSURE) write in a serial
+ * build; columns of a disabled flag are zero. */
+int fdp_get_receivers(fdp_ctx* ctx, int32_t it_first, int32_t n_levels, void* host);
+
+/* Copies the current wavefield to host for snapshots (store_snapshots.F90:173-190):
+ * for each bit set in field_mask, in the order UM WM QX QZ, one
+ * (PMLL:PMLXH, 0:PMLZH) column-major array. */
+int fdp_get_snapshot(fdp_ctx* ctx, int32_t field_mask, void* host);
+
+/* Full-state access (checkpoint/resume and testing): bounds of a field as
+ * {lx, ux, lz, uz}, and copies of it in that Fortran layout. */
+int fdp_field_bounds(fdp_ctx* ctx, int32_t id, int32_t* bounds4);
+int fdp_get_field(fdp_ctx* ctx, int32_t id, void* host);
+int fdp_set_field(fdp_ctx* ctx, int32_t id, const void* host);
+
+/* Waits for all work of the context. */
+int fdp_synchronize(fdp_ctx* ctx);
+
+/* Number of CUDA kernel launches this context has enqueued since creation
+ * (graph-launched kernels counted individually). */
+int64_t fdp_kernel_launches(fdp_ctx* ctx);
+
+/* Last error message of the context (or of the last failed fdp_create when
+ * ctx is NULL). */
+const char* fdp_last_error(const fdp_ctx* ctx);
+
+/* Frees the context and all its device memory (the DEALLOCATEs the
+ * reference leaves to program exit). */
+void fdp_destroy(fdp_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDP_H */

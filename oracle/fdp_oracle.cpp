@@ -1,0 +1,1192 @@
+// =====================================================================
+// TEST INFRASTRUCTURE ONLY -- the CPU oracle for the time-stepping path.
+//
+// A line-by-line C++ restatement of the Fortran reference's TIME_LOOP
+// body (time_loop.F90:63-206) and every row routine it calls.  It is the
+// checker the CUDA kernels are compared against; nothing in the product
+// links it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline leg may load it.
+//
+// PARITY UNPINNED: the reference ships no tests, fixtures or golden
+// vectors and there is no Fortran compiler on this machine, so this
+// restatement could not be checked against a run of the reference itself.
+// Its fidelity rests on reading the reference (each routine cites the
+// file:line it follows) and on the physics checks in tests/.
+//
+// Arithmetic semantics (what a serial PP=DP or PP=SP build of the
+// reference computes, without FMA contraction -- build with
+// -ffp-contract=off):
+//   * every expression is evaluated left to right with Fortran
+//     precedence and the reference's own parentheses;
+//   * default-real literals in PP expressions stay single precision
+//     (mod_auxil.F90:20 A=-1./24. is a single-precision constant even
+//     when PP is double);
+//   * EXP/SQRT/LOG are the C library's exp/expf, sqrt/sqrtf, log/logf.
+// Compile-time macros of the reference are taken at their defaults:
+// SECOND, SEDOND, AFDA_XZ, AFDA_ZZ and USE_MPI all undefined.
+// =====================================================================
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct BoundsError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#ifdef ORACLE_CHECK
+#define OCHK(c, what) do { if (!(c)) throw BoundsError(what); } while (0)
+#else
+#define OCHK(c, what) do { } while (0)
+#endif
+
+// Fortran-style 2-D array A(lx:ux, lz:uz), column-major (x fastest).
+template <class T> struct FA2 {
+  int lx = 0, ux = -1, lz = 0, uz = -1;
+  long nx = 0;
+  std::vector<T> v;
+  void alloc(int lx_, int ux_, int lz_, int uz_) {
+    lx = lx_; ux = ux_; lz = lz_; uz = uz_;
+    nx = ux - lx + 1;
+    v.assign((size_t)nx * (size_t)(uz - lz + 1), T(0));
+  }
+  inline T& operator()(int i, int k) {
+    OCHK(i >= lx && i <= ux && k >= lz && k <= uz, "FA2 index out of bounds");
+    return v[(size_t)(i - lx) + (size_t)(k - lz) * (size_t)nx];
+  }
+  size_t size() const { return v.size(); }
+};
+
+// Fortran-style 1-D array A(l:u).
+template <class T> struct FA1 {
+  int l = 0, u = -1;
+  std::vector<T> v;
+  void alloc(int l_, int u_) { l = l_; u = u_; v.assign((size_t)(u - l + 1), T(0)); }
+  inline T& operator()(int i) {
+    OCHK(i >= l && i <= u, "FA1 index out of bounds");
+    return v[(size_t)(i - l)];
+  }
+};
+
+template <class T> static inline T fexp(T x) { return std::exp(x); }
+
+// Per-row strain buffers EXX, EZZ, EXZ, QXX, QZZ (mod_strainfield.F90:7-9).
+// Every element a row routine reads is written earlier in the same row
+// (checked against strain_*.F90 loop ranges), so thread-private copies
+// give the same results as the reference's module arrays.
+template <class T> struct Strain {
+  FA1<T> EXX, EZZ, EXZ, QXX, QZZ;
+  void alloc(int l, int u) { EXX.alloc(l, u); EZZ.alloc(l, u); EXZ.alloc(l, u); QXX.alloc(l, u); QZZ.alloc(l, u); }
+};
+
+enum FieldId {
+  F_UM = 0, F_WM, F_QX, F_QZ, F_TXX, F_TZZ, F_TXZ, F_PRES,
+  F_PZXL, F_PZXH, F_PXXL, F_PXXH, F_OXXL, F_OXXH, F_PXZH, F_PZZH, F_OZZH,
+  F_RXXL, F_RXXH, F_SXXL, F_SXXH, F_RZXL, F_RZXH, F_GXXL, F_GXXH, F_HXXL, F_HXXH,
+  F_GZXL, F_GZXH, F_RXZH, F_GXZH, F_RZZH, F_SZZH, F_GZZH, F_HZZH,
+  F_SZ_U, F_SZ_W, F_SZ_QX, F_SZ_QZ,
+  F_QXP, F_QZP,
+  F_COUNT
+};
+
+template <class T> struct Sim {
+  // ---- CONTROL_DATA / AUXIL (mod_contr_data.F90, mod_auxil.F90, aux1.F90:36-46)
+  int MX, MZ, TPML, LIN_X, LIN_Z;
+  bool SI;
+  T DT, TAU_EPS, H;
+  int PMLL, PMLXH, PMLZH, PMLZH1, PMLZH2, MX1;
+  T A, B, AH, BH, CH;
+  int MT2 = 0;
+  // ---- fields (mod_wavefield.F90:19-20, mod_stressfield.F90:7-8)
+  FA2<T> UM, WM, QX, QZ, QXP, QZP, TXX, TZZ, TXZ, PRES;
+  // ---- medium (mod_grid_med.F90)
+  FA2<int32_t> JM;
+  int JMNUM = 0;
+  std::vector<T> MU, SIG_XX_1, SIG_XX_2, SIG_XX_3, SIG_ZZ_1, SIG_ZZ_2, SIG_ZZ_3,
+      PRES_1, PRES_2, PRES_3, REL1_U, REL2_U, REL3_U, REL1_W, REL2_W, REL3_W,
+      REL1_QX, REL2_QX, REL3_QX, REL1_QZ, REL2_QZ, REL3_QZ, AUXIL_W, AUXIL_QZ;
+  // ---- PML profiles and memory variables (mod_pml.F90, ppml.F90:60-112)
+  FA2<T> ODA_XL, ODB_XL, ODC_XL, ODD_XL, ODA_XH, ODB_XH, ODC_XH, ODD_XH;
+  FA2<T> ODA_ZH, ODB_ZH, ODC_ZH, ODD_ZH;
+  FA2<T> ODA2_XL, ODB2_XL, ODC2_XL, ODD2_XL, ODA2_XH, ODB2_XH, ODC2_XH, ODD2_XH;
+  FA2<T> ODA2_ZH, ODB2_ZH, ODC2_ZH, ODD2_ZH;
+  FA2<T> PZXL, PZXH, PXXL, PXXH, OXXL, OXXH, PXZH, PZZH, OZZH;
+  FA2<T> RXXL, RXXH, SXXL, SXXH, RZXL, RZXH, GXXL, GXXH, HXXL, HXXH, GZXL, GZXH;
+  FA2<T> RXZH, GXZH, RZZH, SZZH, GZZH, HZZH;
+  // ---- bottom non-reflecting row (mod_nr_bound.F90); row k of SZ_* = TIKMZk
+  T ABW01, ABW02, ABW10, ABW11, ABW12, ABW20, ABW21, ABW22;
+  T ABH01, ABH02, ABH10, ABH11, ABH12, ABH20, ABH21, ABH22;
+  FA2<T> SZ_U, SZ_W, SZ_QX, SZ_QZ, SZ_UP, SZ_WP, SZ_QXP, SZ_QZP;
+  // ---- source (auxil SOURTF_A(2,MT2), control_data SOURSP/SOURFP)
+  std::vector<T> SOURTF;  // [2*(it-1) + k]
+  T SOURSP = 0, SOURFP = 0;
+  // ---- receivers (mod_contr_data.F90, mod_wavefield.F90:8-13)
+  int MR = 0;
+  bool KEY_TLQ = false;
+  std::vector<int> IRECX, LRECX, IRECZ, LRECZ;
+  std::vector<T> SSU, SSW, SSQX, SSQZ;
+  int nthreads = 1;
+
+  FA2<T>* field(int id) {
+    switch (id) {
+      case F_UM: return &UM; case F_WM: return &WM; case F_QX: return &QX; case F_QZ: return &QZ;
+      case F_TXX: return &TXX; case F_TZZ: return &TZZ; case F_TXZ: return &TXZ; case F_PRES: return &PRES;
+      case F_PZXL: return &PZXL; case F_PZXH: return &PZXH; case F_PXXL: return &PXXL; case F_PXXH: return &PXXH;
+      case F_OXXL: return &OXXL; case F_OXXH: return &OXXH; case F_PXZH: return &PXZH; case F_PZZH: return &PZZH;
+      case F_OZZH: return &OZZH;
+      case F_RXXL: return &RXXL; case F_RXXH: return &RXXH; case F_SXXL: return &SXXL; case F_SXXH: return &SXXH;
+      case F_RZXL: return &RZXL; case F_RZXH: return &RZXH; case F_GXXL: return &GXXL; case F_GXXH: return &GXXH;
+      case F_HXXL: return &HXXL; case F_HXXH: return &HXXH; case F_GZXL: return &GZXL; case F_GZXH: return &GZXH;
+      case F_RXZH: return &RXZH; case F_GXZH: return &GXZH; case F_RZZH: return &RZZH; case F_SZZH: return &SZZH;
+      case F_GZZH: return &GZZH; case F_HZZH: return &HZZH;
+      case F_SZ_U: return &SZ_U; case F_SZ_W: return &SZ_W; case F_SZ_QX: return &SZ_QX; case F_SZ_QZ: return &SZ_QZ;
+      case F_QXP: return &QXP; case F_QZP: return &QZP;
+      default: return nullptr;
+    }
+  }
+
+  void init(int mx, int mz, int tpml, int si, T h, T dt, T tau_eps, int lin_x, int lin_z) {
+    MX = mx; MZ = mz; TPML = tpml; SI = si != 0; H = h; DT = dt; TAU_EPS = tau_eps;
+    LIN_X = lin_x; LIN_Z = lin_z;
+    // mod_auxil.F90:19-20 -- default-real constant expressions
+    A = (T)(-1.0f / 24.0f);
+    B = (T)(9.0f / 8.0f);
+    // aux1.F90:36-46
+    MX1 = MX - 1;
+    PMLL = 1 - TPML; PMLXH = MX + TPML;
+    PMLZH = MZ + TPML; PMLZH1 = MZ + TPML - 1; PMLZH2 = MZ + TPML - 2;
+    AH = A / H; BH = B / H; CH = T(1) / H;
+    // tl_alloc.F90:233-265
+    FA2<T>* f[] = {&UM, &WM, &QX, &QZ, &QXP, &QZP, &TXX, &TZZ, &TXZ, &PRES};
+    for (auto* a : f) a->alloc(PMLL, PMLXH, 0, PMLZH);
+    JM.alloc(PMLL, PMLXH, 0, PMLZH);
+    // ppml.F90:60-112 (shapes); zero-initialised as ppml.F90:115-153
+    FA2<T>* px[] = {&ODA_XL, &ODB_XL, &ODC_XL, &ODD_XL, &ODA_XH, &ODB_XH, &ODC_XH, &ODD_XH};
+    for (auto* a : px) a->alloc(0, TPML, 0, PMLZH);
+    FA2<T>* pz[] = {&ODA_ZH, &ODB_ZH, &ODC_ZH, &ODD_ZH};
+    for (auto* a : pz) a->alloc(0, TPML, PMLL, PMLXH);
+    FA2<T>* px2[] = {&ODA2_XL, &ODB2_XL, &ODC2_XL, &ODD2_XL, &ODA2_XH, &ODB2_XH, &ODC2_XH, &ODD2_XH};
+    for (auto* a : px2) a->alloc(0, TPML + 1, 0, PMLZH);
+    FA2<T>* pz2[] = {&ODA2_ZH, &ODB2_ZH, &ODC2_ZH, &ODD2_ZH};
+    for (auto* a : pz2) a->alloc(0, TPML + 1, PMLL, PMLXH);
+    PZXL.alloc(PMLL, 2, 0, PMLZH); PZXH.alloc(MX, PMLXH, 0, PMLZH);
+    PXXL.alloc(PMLL, 1, 0, PMLZH); OXXL.alloc(PMLL, 1, 0, PMLZH);
+    PXXH.alloc(MX, PMLXH, 0, PMLZH); OXXH.alloc(MX, PMLXH, 0, PMLZH);
+    PXZH.alloc(PMLL, PMLXH, 0, TPML + 1);
+    PZZH.alloc(PMLL, PMLXH, 0, TPML); OZZH.alloc(PMLL, PMLXH, 0, TPML);
+    RXXL.alloc(PMLL, 3, 0, PMLZH); RXXH.alloc(MX - 1, PMLXH, 0, PMLZH);
+    SXXL.alloc(PMLL, 3, 0, PMLZH); SXXH.alloc(MX - 1, PMLXH, 0, PMLZH);
+    GXXL.alloc(PMLL, 3, 0, PMLZH); GXXH.alloc(MX - 1, PMLXH, 0, PMLZH);
+    HXXL.alloc(PMLL, 3, 0, PMLZH); HXXH.alloc(MX - 1, PMLXH, 0, PMLZH);
+    RZXL.alloc(PMLL, 2, 0, PMLZH); RZXH.alloc(MX - 1, PMLXH, 0, PMLZH);
+    GZXL.alloc(PMLL, 2, 0, PMLZH); GZXH.alloc(MX - 1, PMLXH, 0, PMLZH);
+    FA2<T>* zb[] = {&RXZH, &GXZH, &RZZH, &SZZH, &GZZH, &HZZH};
+    for (auto* a : zb) a->alloc(PMLL, PMLXH, 0, TPML);
+    // alloc_nr.F90:33-54
+    FA2<T>* sz[] = {&SZ_U, &SZ_W, &SZ_QX, &SZ_QZ, &SZ_UP, &SZ_WP, &SZ_QXP, &SZ_QZP};
+    for (auto* a : sz) a->alloc(PMLL, PMLXH, 0, 2);
+    ABW01 = ABW02 = ABW10 = ABW11 = ABW12 = ABW20 = ABW21 = ABW22 = 0;
+    ABH01 = ABH02 = ABH10 = ABH11 = ABH12 = ABH20 = ABH21 = ABH22 = 0;
+    SOURSP = 0; SOURFP = 0;  // alloc_t_seis.F90:76-77
+  }
+
+  // ================= stress-phase row kernels =========================
+
+  // strain_uw_xz.F90:181-223
+  void strain_uw_xz(Strain<T>& s, int L) {
+    const int L1 = L - 1, L2 = L - 2, LP1 = L + 1;
+    for (int I = 2 - TPML; I <= 2; ++I) {
+      T DZXA = CH * (WM(I, L) - WM(I - 1, L));
+      s.EXZ(I) = CH * (UM(I, L) - UM(I, L1)) + ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DZXA + PZXL(I, L));
+      PZXL(I, L) = ODB2_XL(3 - I, L) * PZXL(I, L) + ODC2_XL(3 - I, L) * DZXA;
+    }
+    for (int I = 3; I <= MX1; ++I) {
+      s.EXZ(I) = AH * (UM(I, LP1) - UM(I, L2) + WM(I + 1, L) - WM(I - 2, L))
+               + BH * (UM(I, L) - UM(I, L1) + WM(I, L) - WM(I - 1, L));
+    }
+    for (int I = MX; I <= MX + TPML; ++I) {
+      T DZXA = CH * (WM(I, L) - WM(I - 1, L));
+      s.EXZ(I) = CH * (UM(I, L) - UM(I, L1)) + ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DZXA + PZXH(I, L));
+      PZXH(I, L) = ODB2_XH(I - MX1, L) * PZXH(I, L) + ODC2_XH(I - MX1, L) * DZXA;
+    }
+  }
+
+  // strain_uw_xz_1.F90:62-114 (non-imaging free surface, row 1; AFDA_XZ undefined)
+  void strain_uw_xz_1(Strain<T>& s) {
+    const int L = 1, L1 = 0;
+    for (int I = PMLL + 1; I <= 2; ++I) {
+      T DZXA = CH * (WM(I, L) - WM(I - 1, L));
+      s.EXZ(I) = CH * (UM(I, L) - UM(I, L1)) + ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DZXA + PZXL(I, L));
+      PZXL(I, L) = ODB2_XL(3 - I, L) * PZXL(I, L) + ODC2_XL(3 - I, L) * DZXA;
+    }
+    for (int I = 3; I <= MX - 1; ++I) {
+      s.EXZ(I) = AH * (WM(I + 1, L) - WM(I - 2, L)) + BH * (WM(I, L) - WM(I - 1, L)) + CH * (UM(I, 1) - UM(I, 0));
+    }
+    for (int I = MX; I <= PMLXH; ++I) {
+      T DZXA = CH * (WM(I, L) - WM(I - 1, L));
+      s.EXZ(I) = CH * (UM(I, L) - UM(I, L1)) + ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DZXA + PZXH(I, L));
+      PZXH(I, L) = ODB2_XH(I - MX1, L) * PZXH(I, L) + ODC2_XH(I - MX1, L) * DZXA;
+    }
+  }
+
+  // strain_uw_zz.F90:33-51 and strain_q_zz.F90:33-52
+  void strain_zz(FA1<T>& E, FA2<T>& W, int L) {
+    const T BC = BH / CH;
+    for (int I = 2 - TPML; I <= MX1 + TPML; ++I) E(I) = (CH * (W(I, L + 1) - W(I, L)));
+    for (int I = 2; I <= MX1; ++I) E(I) = AH * (W(I, L + 2) - W(I, L - 1)) + BC * E(I);
+  }
+
+  // strain_uw_zz_0.F90:38-49, strain_q_zz_0.F90:33-44 (AFDA_ZZ undefined)
+  void strain_zz_0(FA1<T>& E, FA2<T>& W) {
+    for (int I = 2 - TPML; I <= MX1 + TPML; ++I) E(I) = (CH * (W(I, 1) - W(I, 0)));
+  }
+
+  // strain_uw_zz_2nd_pml.F90:51-65 and strain_q_zz_2nd_pml.F90:47-64
+  void strain_zz_2nd_pml(FA1<T>& E, FA2<T>& W, FA2<T>& M, int L, int LL) {
+    for (int I = 2 - TPML; I <= MX1 + TPML; ++I) {
+      T DZZA = CH * (W(I, L + 1) - W(I, L));
+      E(I) = ODA_ZH(LL, I) * (ODD_ZH(LL, I) * DZZA + M(I, LL));
+      M(I, LL) = ODB_ZH(LL, I) * M(I, LL) + ODC_ZH(LL, I) * DZZA;
+    }
+  }
+
+  // strain_uw_xx.F90:48-94 and strain_q_xx.F90:47-91
+  void strain_xx(FA1<T>& E, FA2<T>& U, FA2<T>& ML, FA2<T>& MH, int L) {
+    for (int I = 2 - TPML; I <= 1; ++I) {
+      T DXXA = CH * (U(I + 1, L) - U(I, L));
+      E(I) = ODA_XL(2 - I, L) * (ODD_XL(2 - I, L) * DXXA + ML(I, L));
+      ML(I, L) = ODB_XL(2 - I, L) * ML(I, L) + ODC_XL(2 - I, L) * DXXA;
+    }
+    E(2) = CH * (U(3, L) - U(2, L));
+    for (int I = 3; I <= MX - 2; ++I) E(I) = AH * (U(I + 2, L) - U(I - 1, L)) + BH * (U(I + 1, L) - U(I, L));
+    E(MX1) = CH * (U(MX1 + 1, L) - U(MX1, L));
+    for (int I = MX; I <= MX1 + TPML; ++I) {
+      T DXXA = CH * (U(I + 1, L) - U(I, L));
+      E(I) = ODA_XH(I - MX1, L) * (ODD_XH(I - MX1, L) * DXXA + MH(I, L));
+      MH(I, L) = ODB_XH(I - MX1, L) * MH(I, L) + ODC_XH(I - MX1, L) * DXXA;
+    }
+  }
+
+  // strain_uw_xz_2nd_pml.F90:62-121
+  void strain_uw_xz_2nd_pml(Strain<T>& s, int L, int LL) {
+    const int L1 = L - 1;
+    for (int I = 2 - TPML; I <= 2; ++I) {
+      T DZXA = CH * (WM(I, L) - WM(I - 1, L));
+      T DXZA = CH * (UM(I, L) - UM(I, L1));
+      s.EXZ(I) = ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DXZA + PXZH(I, LL))
+               + ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DZXA + PZXL(I, L));
+      PXZH(I, LL) = ODB2_ZH(LL, I) * PXZH(I, LL) + ODC2_ZH(LL, I) * DXZA;
+      PZXL(I, L) = ODB2_XL(3 - I, L) * PZXL(I, L) + ODC2_XL(3 - I, L) * DZXA;
+    }
+    for (int I = 3; I <= MX1; ++I) {
+      T DZXA = CH * (WM(I, L) - WM(I - 1, L));
+      T DXZA = CH * (UM(I, L) - UM(I, L1));
+      s.EXZ(I) = ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DXZA + PXZH(I, LL)) + DZXA;
+      PXZH(I, LL) = ODB2_ZH(LL, I) * PXZH(I, LL) + ODC2_ZH(LL, I) * DXZA;
+    }
+    for (int I = MX; I <= MX + TPML; ++I) {
+      T DZXA = CH * (WM(I, L) - WM(I - 1, L));
+      T DXZA = CH * (UM(I, L) - UM(I, L1));
+      s.EXZ(I) = ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DXZA + PXZH(I, LL))
+               + ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DZXA + PZXH(I, L));
+      PXZH(I, LL) = ODB2_ZH(LL, I) * PXZH(I, LL) + ODC2_ZH(LL, I) * DXZA;
+      PZXH(I, L) = ODB2_XH(I - MX1, L) * PZXH(I, L) + ODC2_XH(I - MX1, L) * DZXA;
+    }
+  }
+
+  // stress_xz.F90:40-47
+  void stress_xz(Strain<T>& s, int L) {
+    for (int I = 2 - TPML; I <= MX + TPML; ++I) {
+      int JM1 = JM(I, L);
+      T TXZv = MU[JM1] * s.EXZ(I);
+      TXZ(I, L) = TXZ(I, L) + (DT + TAU_EPS) * TXZv;
+    }
+  }
+
+  // stress_nn.F90:49-61 and, with the source, stress_lin_nn.F90:49-70
+  void stress_nn(Strain<T>& s, int L, bool lin, T SOURS, T SOURF) {
+    for (int I = 2 - TPML; I <= MX - 1 + TPML; ++I) {
+      int JM1 = JM(I, L);
+      T TXXv = SIG_XX_1[JM1] * s.EXX(I) + SIG_XX_2[JM1] * s.EZZ(I) + SIG_XX_3[JM1] * s.QXX(I) + SIG_XX_3[JM1] * s.QZZ(I);
+      T TZZv = SIG_ZZ_1[JM1] * s.EXX(I) + SIG_ZZ_2[JM1] * s.EZZ(I) + SIG_ZZ_3[JM1] * s.QXX(I) + SIG_ZZ_3[JM1] * s.QZZ(I);
+      T PRv = PRES_1[JM1] * s.EXX(I) + PRES_2[JM1] * s.EZZ(I) + PRES_3[JM1] * s.QXX(I) + PRES_3[JM1] * s.QZZ(I);
+      if (lin && I == LIN_X) {
+        TXX(I, L) = TXX(I, L) + (DT + TAU_EPS) * (TXXv - ((SOURS - SOURSP) / DT));
+        TZZ(I, L) = TZZ(I, L) + (DT + TAU_EPS) * (TZZv - ((SOURS - SOURSP) / DT));
+        PRES(I, L) = PRES(I, L) + (DT + TAU_EPS) * (PRv + ((SOURF - SOURFP) / DT));
+        SOURSP = SOURS;
+        SOURFP = SOURF;
+      } else {
+        TXX(I, L) = TXX(I, L) + (DT + TAU_EPS) * TXXv;
+        TZZ(I, L) = TZZ(I, L) + (DT + TAU_EPS) * TZZv;
+        PRES(I, L) = PRES(I, L) + (DT + TAU_EPS) * PRv;
+      }
+    }
+  }
+
+  // hplane_ic_stress.F90:48-117; hplane_lin_stress.F90:55-127 when lin
+  void hplane_ic_stress(Strain<T>& s, int L, bool lin = false, T SOURS = 0, T SOURF = 0) {
+    strain_uw_xz(s, L);
+    strain_zz(s.EZZ, WM, L);
+    strain_zz(s.QZZ, QZ, L);
+    strain_xx(s.EXX, UM, PXXL, PXXH, L);
+    strain_xx(s.QXX, QX, OXXL, OXXH, L);
+    stress_xz(s, L);
+    stress_nn(s, L, lin, SOURS, SOURF);
+  }
+
+  // hplane_0_stress.F90:47-120
+  void hplane_0_stress(Strain<T>& s) {
+    if (SI) {
+      for (int I = PMLL; I <= PMLXH; ++I) {
+        TXZ(I, 0) = -TXZ(I, 4);
+        TZZ(I, 0) = -TZZ(I, 3);
+        PRES(I, 0) = -PRES(I, 3);
+      }
+    } else {
+      for (int I = PMLL; I <= PMLXH; ++I) s.EXZ(I) = T(0);
+      strain_zz_0(s.EZZ, WM);
+      strain_zz_0(s.QZZ, QZ);
+      strain_xx(s.EXX, UM, PXXL, PXXH, 0);
+      strain_xx(s.QXX, QX, OXXL, OXXH, 0);
+      stress_xz(s, 0);
+      stress_nn(s, 0, false, 0, 0);
+    }
+  }
+
+  // hplane_1_stress.F90:44-126
+  void hplane_1_stress(Strain<T>& s) {
+    if (SI) {
+      for (int I = PMLL; I <= PMLXH; ++I) {
+        TXZ(I, 1) = -TXZ(I, 3);
+        TZZ(I, 1) = -TZZ(I, 2);
+        PRES(I, 1) = -PRES(I, 2);
+        TXZ(I, 2) = T(0);
+      }
+    } else {
+      strain_uw_xz_1(s);
+      strain_zz(s.EZZ, WM, 1);
+      strain_zz(s.QZZ, QZ, 1);
+      strain_xx(s.EXX, UM, PXXL, PXXH, 1);
+      strain_xx(s.QXX, QX, OXXL, OXXH, 1);
+      stress_xz(s, 1);
+      stress_nn(s, 1, false, 0, 0);
+    }
+  }
+
+  // hplane_mz1_stress.F90:50-130 (L = MZ-1, LL = 0)
+  void hplane_mz1_stress(Strain<T>& s) {
+    const int L = MZ - 1, LL = 0;
+    strain_uw_xz(s, L);
+    strain_zz_2nd_pml(s.EZZ, WM, PZZH, L, LL);
+    strain_zz_2nd_pml(s.QZZ, QZ, OZZH, L, LL);
+    strain_xx(s.EXX, UM, PXXL, PXXH, L);
+    strain_xx(s.QXX, QX, OXXL, OXXH, L);
+    stress_xz(s, L);
+    stress_nn(s, L, false, 0, 0);
+  }
+
+  // hplane_pml_stress.F90:53-134
+  void hplane_pml_stress(Strain<T>& s, int L, int LL) {
+    strain_uw_xz_2nd_pml(s, L, LL);
+    strain_zz_2nd_pml(s.EZZ, WM, PZZH, L, LL);
+    strain_zz_2nd_pml(s.QZZ, QZ, OZZH, L, LL);
+    strain_xx(s.EXX, UM, PXXL, PXXH, L);
+    strain_xx(s.QXX, QX, OXXL, OXXH, L);
+    stress_xz(s, L);
+    stress_nn(s, L, false, 0, 0);
+  }
+
+  // hplane_pmlzh0_stress.F90:43-68
+  void hplane_pmlzh0_stress(Strain<T>& s) {
+    const int L = MZ + TPML, LL = TPML + 1;
+    strain_uw_xz_2nd_pml(s, L, LL);
+    stress_xz(s, L);
+  }
+
+  // ================= velocity-phase row kernels =======================
+
+  T ecoef(T r3) { return fexp(-r3); }
+  T ccoef(T r2, T r3) { return (r2 / r3) * (T(1) - fexp(-r3)); }
+
+  // inh_qx_int.F90:35-54
+  void inh_qx_int(int L) {
+    const int IN1 = L - 1, IN2 = L, IN3 = L + 1, IN4 = L + 2;
+    for (int I = 4; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (A * (TXX(I + 1, L) - TXX(I - 2, L) + TXZ(I, IN4) - TXZ(I, IN1))
+                               + B * (TXX(I, L) - TXX(I - 1, L) + TXZ(I, IN3) - TXZ(I, IN2)))
+                 - REL2_QX[J] * (A * (PRES(I + 1, L) - PRES(I - 2, L)) + B * (PRES(I, L) - PRES(I - 1, L)));
+    }
+  }
+  // inh_qz_int.F90:35-55
+  void inh_qz_int(int L) {
+    const int IN1 = L - 2, IN2 = L - 1, IN3 = L, IN4 = L + 1;
+    for (int I = 3; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (A * (TZZ(I, IN4) - TZZ(I, IN1) + TXZ(I + 2, L) - TXZ(I - 1, L))
+                               + B * (TZZ(I, IN3) - TZZ(I, IN2) + TXZ(I + 1, L) - TXZ(I, L)))
+                 - REL2_QZ[J] * (A * (PRES(I, IN4) - PRES(I, IN1)) + B * (PRES(I, IN3) - PRES(I, IN2)));
+    }
+  }
+  // inh_v_uv_int.F90:36-56
+  void inh_v_uv_int(int L) {
+    const int IN1 = L - 1, IN2 = L, IN3 = L + 1, IN4 = L + 2;
+    for (int I = 4; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (A * (TXX(I + 1, L) - TXX(I - 2, L) + TXZ(I, IN4) - TXZ(I, IN1))
+                              + B * (TXX(I, L) - TXX(I - 1, L) + TXZ(I, IN3) - TXZ(I, IN2)))
+                 + REL3_U[J] * (A * (PRES(I + 1, L) - PRES(I - 2, L)) + B * (PRES(I, L) - PRES(I - 1, L)));
+    }
+  }
+  // inh_v_w_int.F90:37-58
+  void inh_v_w_int(int L) {
+    const int IN1 = L - 2, IN2 = L - 1, IN3 = L, IN4 = L + 1;
+    for (int I = 3; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (A * (TZZ(I, IN4) - TZZ(I, IN1) + TXZ(I + 2, L) - TXZ(I - 1, L))
+                              + B * (TZZ(I, IN3) - TZZ(I, IN2) + TXZ(I + 1, L) - TXZ(I, L)))
+                 + REL3_W[J] * (A * (PRES(I, IN4) - PRES(I, IN1)) + B * (PRES(I, IN3) - PRES(I, IN2)));
+    }
+  }
+
+  // inh_qx_2nd.F90:50-103
+  void inh_qx_2nd(int L) {
+    const int IN2 = L, IN3 = L + 1;
+    for (int I = 3 - TPML; I <= 3; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DXXXA + GXXL(I, L)) + TXZ(I, IN3) - TXZ(I, IN2))
+                 - REL2_QX[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * PXXXA + HXXL(I, L)));
+      GXXL(I, L) = ODB2_XL(3 - I, L) * GXXL(I, L) + ODC2_XL(3 - I, L) * DXXXA;
+      HXXL(I, L) = ODB2_XL(3 - I, L) * HXXL(I, L) + ODC2_XL(3 - I, L) * PXXXA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DXXXA + GXXH(I, L)) + TXZ(I, IN3) - TXZ(I, IN2))
+                 - REL2_QX[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * PXXXA + HXXH(I, L)));
+      GXXH(I, L) = ODB2_XH(I - MX1, L) * GXXH(I, L) + ODC2_XH(I - MX1, L) * DXXXA;
+      HXXH(I, L) = ODB2_XH(I - MX1, L) * HXXH(I, L) + ODC2_XH(I - MX1, L) * PXXXA;
+    }
+  }
+  // inh_qz_2nd.F90:45-88
+  void inh_qz_2nd(int L) {
+    const int IN2 = L - 1, IN3 = L;
+    for (int I = 2 - TPML; I <= 2; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (TZZ(I, IN3) - TZZ(I, IN2) + ODA_XL(2 - I, L) * (ODD_XL(2 - I, L) * DXZXA + GZXL(I, L)))
+                 - REL2_QZ[J] * (PRES(I, IN3) - PRES(I, IN2));
+      GZXL(I, L) = ODB_XL(2 - I, L) * GZXL(I, L) + ODC_XL(2 - I, L) * DXZXA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (TZZ(I, IN3) - TZZ(I, IN2) + ODA_XH(I - MX1, L) * (ODD_XH(I - MX1, L) * DXZXA + GZXH(I, L)))
+                 - REL2_QZ[J] * (PRES(I, IN3) - PRES(I, IN2));
+      GZXH(I, L) = ODB_XH(I - MX1, L) * GZXH(I, L) + ODC_XH(I - MX1, L) * DXZXA;
+    }
+  }
+  // inh_v_u_2nd.F90:52-104
+  void inh_v_u_2nd(int L) {
+    const int IN2 = L, IN3 = L + 1;
+    for (int I = 3 - TPML; I <= 3; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DXXXA + RXXL(I, L)) + TXZ(I, IN3) - TXZ(I, IN2))
+                 + REL3_U[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * PXXXA + SXXL(I, L)));
+      RXXL(I, L) = ODB2_XL(3 - I, L) * RXXL(I, L) + ODC2_XL(3 - I, L) * DXXXA;
+      SXXL(I, L) = ODB2_XL(3 - I, L) * SXXL(I, L) + ODC2_XL(3 - I, L) * PXXXA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DXXXA + RXXH(I, L)) + TXZ(I, IN3) - TXZ(I, IN2))
+                 + REL3_U[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * PXXXA + SXXH(I, L)));
+      RXXH(I, L) = ODB2_XH(I - MX1, L) * RXXH(I, L) + ODC2_XH(I - MX1, L) * DXXXA;
+      SXXH(I, L) = ODB2_XH(I - MX1, L) * SXXH(I, L) + ODC2_XH(I - MX1, L) * PXXXA;
+    }
+  }
+  // inh_v_w_2nd.F90:48-91
+  void inh_v_w_2nd(int L) {
+    const int IN2 = L - 1, IN3 = L;
+    for (int I = 2 - TPML; I <= 2; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (TZZ(I, IN3) - TZZ(I, IN2) + ODA_XL(2 - I, L) * (ODD_XL(2 - I, L) * DXZXA + RZXL(I, L)))
+                 + REL3_W[J] * (PRES(I, IN3) - PRES(I, IN2));
+      RZXL(I, L) = ODB_XL(2 - I, L) * RZXL(I, L) + ODC_XL(2 - I, L) * DXZXA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (TZZ(I, IN3) - TZZ(I, IN2) + ODA_XH(I - MX1, L) * (ODD_XH(I - MX1, L) * DXZXA + RZXH(I, L)))
+                 + REL3_W[J] * (PRES(I, IN3) - PRES(I, IN2));
+      RZXH(I, L) = ODB_XH(I - MX1, L) * RZXH(I, L) + ODC_XH(I - MX1, L) * DXZXA;
+    }
+  }
+  // sto_qxp.F90:24-28, sto_qzp.F90:24-28
+  void sto_qxp(int L) { for (int I = 3 - TPML; I <= MX1 + TPML; ++I) QXP(I, L) = QX(I, L); }
+  void sto_qzp(int L) { for (int I = 2 - TPML; I <= MX1 + TPML; ++I) QZP(I, L) = QZ(I, L); }
+
+  // hplane_ic_velocity.F90:59-202 (the STO_BOR side histories are never
+  // read anywhere in the reference and are left out)
+  void hplane_ic_velocity(int L) {
+    inh_qx_int(L);
+    inh_qz_int(L);
+    inh_v_uv_int(L);
+    inh_v_w_int(L);
+    inh_qx_2nd(L);
+    inh_qz_2nd(L);
+    inh_v_u_2nd(L);
+    inh_v_w_2nd(L);
+    sto_qxp(L);
+    sto_qzp(L);
+  }
+
+  // ---- non-imaging free surface, row 0 (hplane_0_velocity.F90)
+  // inh_qx_int_0.F90 (SECOND undefined branch)
+  void inh_qx_int_0() {
+    const int L = 0;
+    for (int I = 4; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (A * (TXX(I + 1, L) - TXX(I - 2, L)) + B * (TXX(I, L) - TXX(I - 1, L))
+                               + T(17) / T(24) * TXZ(I, 1) + T(3) / T(8) * TXZ(I, 2)
+                               - T(5) / T(24) * TXZ(I, 3) + T(1) / T(24) * TXZ(I, 4))
+                 - REL2_QX[J] * (A * (PRES(I + 1, L) - PRES(I - 2, L)) + B * (PRES(I, L) - PRES(I - 1, L)));
+    }
+  }
+  // inh_v_uv_int_0.F90 (SECOND undefined branch)
+  void inh_v_uv_int_0() {
+    const int L = 0;
+    for (int I = 4; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (A * (TXX(I + 1, L) - TXX(I - 2, L)) + B * (TXX(I, L) - TXX(I - 1, L))
+                              + T(17) / T(24) * TXZ(I, 1) + T(3) / T(8) * TXZ(I, 2)
+                              - T(5) / T(24) * TXZ(I, 3) + T(1) / T(24) * TXZ(I, 4))
+                 + REL3_U[J] * (A * (PRES(I + 1, L) - PRES(I - 2, L)) + B * (PRES(I, L) - PRES(I - 1, L)));
+    }
+  }
+  // inh_qz_int_0.F90
+  void inh_qz_int_0() {
+    const int L = 0;
+    for (int I = 3; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (T(35) / T(8) * TZZ(I, 0) - T(35) / T(24) * TZZ(I, 1)
+                               + T(21) / T(40) * TZZ(I, 2) - T(5) / T(56) * TZZ(I, 3))
+                 - REL2_QZ[J] * (T(35) / T(8) * PRES(I, 0) - T(35) / T(24) * PRES(I, 1)
+                               + T(21) / T(40) * PRES(I, 2) - T(5) / T(56) * PRES(I, 3));
+    }
+  }
+  // inh_v_w_int_0.F90
+  void inh_v_w_int_0() {
+    const int L = 0;
+    for (int I = 3; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (T(35) / T(8) * TZZ(I, 0) - T(35) / T(24) * TZZ(I, 1)
+                              + T(21) / T(40) * TZZ(I, 2) - T(5) / T(56) * TZZ(I, 3))
+                 + REL3_W[J] * (T(35) / T(8) * PRES(I, 0) - T(35) / T(24) * PRES(I, 1)
+                              + T(21) / T(40) * PRES(I, 2) - T(5) / T(56) * PRES(I, 3));
+    }
+  }
+  // inh_qx_2nd_0.F90
+  void inh_qx_2nd_0() {
+    const int L = 0, IN3 = 1;
+    for (int I = 3 - TPML; I <= 3; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DXXXA + GXXL(I, L)) + TXZ(I, IN3))
+                 - REL2_QX[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * PXXXA + HXXL(I, L)));
+      GXXL(I, L) = ODB2_XL(3 - I, L) * GXXL(I, L) + ODC2_XL(3 - I, L) * DXXXA;
+      HXXL(I, L) = ODB2_XL(3 - I, L) * HXXL(I, L) + ODC2_XL(3 - I, L) * PXXXA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DXXXA + GXXH(I, L)) + TXZ(I, IN3))
+                 - REL2_QX[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * PXXXA + HXXH(I, L)));
+      GXXH(I, L) = ODB2_XH(I - MX1, L) * GXXH(I, L) + ODC2_XH(I - MX1, L) * DXXXA;
+      HXXH(I, L) = ODB2_XH(I - MX1, L) * HXXH(I, L) + ODC2_XH(I - MX1, L) * PXXXA;
+    }
+  }
+  // inh_v_u_2nd_0.F90
+  void inh_v_u_2nd_0() {
+    const int L = 0, IN3 = 1;
+    for (int I = 3 - TPML; I <= 3; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DXXXA + RXXL(I, L)) + TXZ(I, IN3))
+                 + REL3_U[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * PXXXA + SXXL(I, L)));
+      RXXL(I, L) = ODB2_XL(3 - I, L) * RXXL(I, L) + ODC2_XL(3 - I, L) * DXXXA;
+      SXXL(I, L) = ODB2_XL(3 - I, L) * SXXL(I, L) + ODC2_XL(3 - I, L) * PXXXA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DXXXA + RXXH(I, L)) + TXZ(I, IN3))
+                 + REL3_U[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * PXXXA + SXXH(I, L)));
+      RXXH(I, L) = ODB2_XH(I - MX1, L) * RXXH(I, L) + ODC2_XH(I - MX1, L) * DXXXA;
+      SXXH(I, L) = ODB2_XH(I - MX1, L) * SXXH(I, L) + ODC2_XH(I - MX1, L) * PXXXA;
+    }
+  }
+  // inh_qz_2nd_0.F90 / inh_v_w_2nd_0.F90 (no x-memory update on row 0)
+  void inh_qz_w_2nd_0() {
+    const int L = 0;
+    auto one = [&](int I) {
+      int J = JM(I, L);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (T(3) * TZZ(I, 0) - T(1) / T(3) * TZZ(I, 1))
+                 - REL2_QZ[J] * (T(3) * PRES(I, 0) - T(1) / T(3) * PRES(I, 1));
+    };
+    auto onew = [&](int I) {
+      int J = JM(I, L);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (T(3) * TZZ(I, 0) - T(1) / T(3) * TZZ(I, 1))
+                 + REL3_W[J] * (T(3) * PRES(I, 0) - T(1) / T(3) * PRES(I, 1));
+    };
+    // the reference calls INH_QZ_2ND_0 (left, right) and then INH_V_W_2ND_0
+    for (int I = 2 - TPML; I <= 2; ++I) one(I);
+    for (int I = MX1; I <= MX1 + TPML; ++I) one(I);
+    for (int I = 2 - TPML; I <= 2; ++I) onew(I);
+    for (int I = MX1; I <= MX1 + TPML; ++I) onew(I);
+  }
+  // hplane_0_velocity.F90:62-179 (non-imaging only)
+  void hplane_0_velocity() {
+    inh_qx_int_0();
+    inh_v_uv_int_0();
+    inh_qz_int_0();
+    inh_v_w_int_0();
+    inh_qx_2nd_0();
+    inh_v_u_2nd_0();
+    inh_qz_w_2nd_0();
+    sto_qxp(0);
+    sto_qzp(0);
+  }
+
+  // inh_v_qz_int_1.F90 and inh_v_w_int_1.F90 (SEDOND undefined branch)
+  void inh_v_qz_w_int_1() {
+    const int L = 1, IN2 = 0, IN3 = 1, IN4 = 2, IN1 = 3;
+    for (int I = 3; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (A * (TXZ(I + 2, L) - TXZ(I - 1, L)) + B * (TXZ(I + 1, L) - TXZ(I, L))
+                               - T(31) / T(24) * TZZ(I, IN2) + T(29) / T(24) * TZZ(I, IN3)
+                               - T(3) / T(40) * TZZ(I, IN4) + T(1) / T(168) * TZZ(I, IN1))
+                 - REL2_QZ[J] * (-T(31) / T(24) * PRES(I, IN2) + T(29) / T(24) * PRES(I, IN3)
+                               - T(3) / T(40) * PRES(I, IN4) + T(1) / T(168) * PRES(I, IN1));
+    }
+    for (int I = 3; I <= MX - 2; ++I) {
+      int J = JM(I, L);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (A * (TXZ(I + 2, L) - TXZ(I - 1, L)) + B * (TXZ(I + 1, L) - TXZ(I, L))
+                              - T(31) / T(24) * TZZ(I, IN2) + T(29) / T(24) * TZZ(I, IN3)
+                              - T(3) / T(40) * TZZ(I, IN4) + T(1) / T(168) * TZZ(I, IN1))
+                 + REL3_W[J] * (-T(31) / T(24) * PRES(I, IN2) + T(29) / T(24) * PRES(I, IN3)
+                              - T(3) / T(40) * PRES(I, IN4) + T(1) / T(168) * PRES(I, IN1));
+    }
+  }
+
+  // hplane_1_velocity.F90:59-222
+  void hplane_1_velocity() {
+    if (SI) {
+      // inh_v_qx_int_1_si.F90:24-31
+      for (int I = 3 - TPML; I <= MX - 1 + TPML; ++I) {
+        UM(I, 1) = UM(I, 2) + WM(I, 2) - WM(I - 1, 2);
+        QX(I, 1) = QX(I, 2) + QZ(I, 2) - QZ(I - 1, 2);
+      }
+      // inh_w_qz_int_1_si.F90:28-44
+      for (int I = 3 - TPML; I <= MX - 2 + TPML; ++I) {
+        int J = JM(I, 0);
+        WM(I, 1) = WM(I, 3) + AUXIL_W[J] * (UM(I + 1, 1) - UM(I, 1) + UM(I + 1, 2) - UM(I, 2));
+        QZ(I, 1) = QZ(I, 3) + AUXIL_QZ[J] * (UM(I + 1, 1) - UM(I, 1) + UM(I + 1, 2) - UM(I, 2))
+                   + (QX(I + 1, 1) - QX(I, 1) + QX(I + 1, 2) - QX(I, 2));
+      }
+    } else {
+      inh_qx_int(1);
+      inh_v_uv_int(1);
+      inh_v_qz_w_int_1();
+      inh_qx_2nd(1);
+      inh_v_u_2nd(1);
+      inh_qz_2nd(1);
+      inh_v_w_2nd(1);
+    }
+    sto_qxp(1);
+    sto_qzp(1);
+  }
+
+  // ---- bottom PML rows (hplane_pml_velocity.F90:64-180)
+  // inh_qx_int_2nd_pml.F90
+  void inh_qx_int_2nd_pml(int L, int LL) {
+    const int IN2 = L, IN3 = L + 1;
+    for (int I = 3 - TPML; I <= 3; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T DXZZA = TXZ(I, IN3) - TXZ(I, IN2);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DXXXA + GXXL(I, L)))
+                 - REL1_QX[J] * (ODA_ZH(LL, I) * (ODD_ZH(LL, I) * DXZZA + GXZH(I, LL)))
+                 - REL2_QX[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * PXXXA + HXXL(I, L)));
+      GXXL(I, L) = ODB2_XL(3 - I, L) * GXXL(I, L) + ODC2_XL(3 - I, L) * DXXXA;
+      HXXL(I, L) = ODB2_XL(3 - I, L) * HXXL(I, L) + ODC2_XL(3 - I, L) * PXXXA;
+      GXZH(I, LL) = ODB_ZH(LL, I) * GXZH(I, LL) + ODC_ZH(LL, I) * DXZZA;
+    }
+    for (int I = 4; I <= MX1 - 1; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T DXZZA = TXZ(I, IN3) - TXZ(I, IN2);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (ODA_ZH(LL, I) * (ODD_ZH(LL, I) * DXZZA + GXZH(I, LL)) + DXXXA)
+                 - REL2_QX[J] * (PRES(I, L) - PRES(I - 1, L));
+      GXZH(I, LL) = ODB_ZH(LL, I) * GXZH(I, LL) + ODC_ZH(LL, I) * DXZZA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T DXZZA = TXZ(I, IN3) - TXZ(I, IN2);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      QX(I, L) = fexp(-REL3_QX[J]) * QX(I, L)
+                 - REL1_QX[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DXXXA + GXXH(I, L)))
+                 - REL1_QX[J] * (ODA_ZH(LL, I) * (ODD_ZH(LL, I) * DXZZA + GXZH(I, LL)))
+                 - REL2_QX[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * PXXXA + HXXH(I, L)));
+      GXXH(I, L) = ODB2_XH(I - MX1, L) * GXXH(I, L) + ODC2_XH(I - MX1, L) * DXXXA;
+      HXXH(I, L) = ODB2_XH(I - MX1, L) * HXXH(I, L) + ODC2_XH(I - MX1, L) * PXXXA;
+      GXZH(I, LL) = ODB_ZH(LL, I) * GXZH(I, LL) + ODC_ZH(LL, I) * DXZZA;
+    }
+  }
+  // inh_v_u_int_2nd_pml.F90
+  void inh_v_u_int_2nd_pml(int L, int LL) {
+    const int IN2 = L, IN3 = L + 1;
+    for (int I = 3 - TPML; I <= 3; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T DXZZA = TXZ(I, IN3) - TXZ(I, IN2);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * DXXXA + RXXL(I, L))
+                              + ODA_ZH(LL, I) * (ODD_ZH(LL, I) * DXZZA + RXZH(I, LL)))
+                 + REL3_U[J] * (ODA2_XL(3 - I, L) * (ODD2_XL(3 - I, L) * PXXXA + SXXL(I, L)));
+      RXXL(I, L) = ODB2_XL(3 - I, L) * RXXL(I, L) + ODC2_XL(3 - I, L) * DXXXA;
+      SXXL(I, L) = ODB2_XL(3 - I, L) * SXXL(I, L) + ODC2_XL(3 - I, L) * PXXXA;
+      RXZH(I, LL) = ODB_ZH(LL, I) * RXZH(I, LL) + ODC_ZH(LL, I) * DXZZA;
+    }
+    for (int I = 4; I <= MX1 - 1; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T DXZZA = TXZ(I, IN3) - TXZ(I, IN2);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (DXXXA + ODA_ZH(LL, I) * (ODD_ZH(LL, I) * DXZZA + RXZH(I, LL)))
+                 + REL3_U[J] * PXXXA;
+      RXZH(I, LL) = ODB_ZH(LL, I) * RXZH(I, LL) + ODC_ZH(LL, I) * DXZZA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXXXA = TXX(I, L) - TXX(I - 1, L);
+      T DXZZA = TXZ(I, IN3) - TXZ(I, IN2);
+      T PXXXA = PRES(I, L) - PRES(I - 1, L);
+      UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
+                 + REL1_U[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * DXXXA + RXXH(I, L))
+                              + ODA_ZH(LL, I) * (ODD_ZH(LL, I) * DXZZA + RXZH(I, LL)))
+                 + REL3_U[J] * (ODA2_XH(I - MX1, L) * (ODD2_XH(I - MX1, L) * PXXXA + SXXH(I, L)));
+      RXXH(I, L) = ODB2_XH(I - MX1, L) * RXXH(I, L) + ODC2_XH(I - MX1, L) * DXXXA;
+      SXXH(I, L) = ODB2_XH(I - MX1, L) * SXXH(I, L) + ODC2_XH(I - MX1, L) * PXXXA;
+      RXZH(I, LL) = ODB_ZH(LL, I) * RXZH(I, LL) + ODC_ZH(LL, I) * DXZZA;
+    }
+  }
+  // inh_qz_int_2nd_pml.F90
+  void inh_qz_int_2nd_pml(int L, int LL) {
+    const int IN2 = L - 1, IN3 = L;
+    for (int I = 2 - TPML; I <= 2; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      T DZZZA = TZZ(I, IN3) - TZZ(I, IN2);
+      T PZZZA = PRES(I, IN3) - PRES(I, IN2);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DZZZA + GZZH(I, LL)))
+                 - REL1_QZ[J] * (ODA_XL(2 - I, L) * (ODD_XL(2 - I, L) * DXZXA + GZXL(I, L)))
+                 - REL2_QZ[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * PZZZA + HZZH(I, LL)));
+      GZXL(I, L) = ODB_XL(2 - I, L) * GZXL(I, L) + ODC_XL(2 - I, L) * DXZXA;
+      GZZH(I, LL) = ODB2_ZH(LL, I) * GZZH(I, LL) + ODC2_ZH(LL, I) * DZZZA;
+      HZZH(I, LL) = ODB2_ZH(LL, I) * HZZH(I, LL) + ODC2_ZH(LL, I) * PZZZA;
+    }
+    for (int I = 3; I <= MX1 - 1; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      T DZZZA = TZZ(I, IN3) - TZZ(I, IN2);
+      T PZZZA = PRES(I, IN3) - PRES(I, IN2);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DZZZA + GZZH(I, LL)) + DXZXA)
+                 - REL2_QZ[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * PZZZA + HZZH(I, LL)));
+      GZZH(I, LL) = ODB2_ZH(LL, I) * GZZH(I, LL) + ODC2_ZH(LL, I) * DZZZA;
+      HZZH(I, LL) = ODB2_ZH(LL, I) * HZZH(I, LL) + ODC2_ZH(LL, I) * PZZZA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      T DZZZA = TZZ(I, IN3) - TZZ(I, IN2);
+      T PZZZA = PRES(I, IN3) - PRES(I, IN2);
+      QZ(I, L) = fexp(-REL3_QZ[J]) * QZ(I, L)
+                 - REL1_QZ[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DZZZA + GZZH(I, LL)))
+                 - REL1_QZ[J] * (ODA_XH(I - MX1, L) * (ODD_XH(I - MX1, L) * DXZXA + GZXH(I, L)))
+                 - REL2_QZ[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * PZZZA + HZZH(I, LL)));
+      GZXH(I, L) = ODB_XH(I - MX1, L) * GZXH(I, L) + ODC_XH(I - MX1, L) * DXZXA;
+      GZZH(I, LL) = ODB2_ZH(LL, I) * GZZH(I, LL) + ODC2_ZH(LL, I) * DZZZA;
+      HZZH(I, LL) = ODB2_ZH(LL, I) * HZZH(I, LL) + ODC2_ZH(LL, I) * PZZZA;
+    }
+  }
+  // inh_v_w_int_2nd_pml.F90
+  void inh_v_w_int_2nd_pml(int L, int LL) {
+    const int IN2 = L - 1, IN3 = L;
+    for (int I = 2 - TPML; I <= 2; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      T DZZZA = TZZ(I, IN3) - TZZ(I, IN2);
+      T PZZZA = PRES(I, IN3) - PRES(I, IN2);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DZZZA + RZZH(I, LL))
+                              + ODA_XL(2 - I, L) * (ODD_XL(2 - I, L) * DXZXA + RZXL(I, L)))
+                 + REL3_W[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * PZZZA + SZZH(I, LL)));
+      RZXL(I, L) = ODB_XL(2 - I, L) * RZXL(I, L) + ODC_XL(2 - I, L) * DXZXA;
+      RZZH(I, LL) = ODB2_ZH(LL, I) * RZZH(I, LL) + ODC2_ZH(LL, I) * DZZZA;
+      SZZH(I, LL) = ODB2_ZH(LL, I) * SZZH(I, LL) + ODC2_ZH(LL, I) * PZZZA;
+    }
+    for (int I = 3; I <= MX1 - 1; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      T DZZZA = TZZ(I, IN3) - TZZ(I, IN2);
+      T PZZZA = PRES(I, IN3) - PRES(I, IN2);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DZZZA + RZZH(I, LL)) + DXZXA)
+                 + REL3_W[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * PZZZA + SZZH(I, LL)));
+      RZZH(I, LL) = ODB2_ZH(LL, I) * RZZH(I, LL) + ODC2_ZH(LL, I) * DZZZA;
+      SZZH(I, LL) = ODB2_ZH(LL, I) * SZZH(I, LL) + ODC2_ZH(LL, I) * PZZZA;
+    }
+    for (int I = MX1; I <= MX1 + TPML; ++I) {
+      int J = JM(I, L);
+      T DXZXA = TXZ(I + 1, L) - TXZ(I, L);
+      T DZZZA = TZZ(I, IN3) - TZZ(I, IN2);
+      T PZZZA = PRES(I, IN3) - PRES(I, IN2);
+      WM(I, L) = WM(I, L) + (REL2_W[J] / REL3_QZ[J]) * (T(1) - fexp(-REL3_QZ[J])) * QZP(I, L)
+                 + REL1_W[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * DZZZA + RZZH(I, LL))
+                              + ODA_XH(I - MX1, L) * (ODD_XH(I - MX1, L) * DXZXA + RZXH(I, L)))
+                 + REL3_W[J] * (ODA2_ZH(LL, I) * (ODD2_ZH(LL, I) * PZZZA + SZZH(I, LL)));
+      RZXH(I, L) = ODB_XH(I - MX1, L) * RZXH(I, L) + ODC_XH(I - MX1, L) * DXZXA;
+      RZZH(I, LL) = ODB2_ZH(LL, I) * RZZH(I, LL) + ODC2_ZH(LL, I) * DZZZA;
+      SZZH(I, LL) = ODB2_ZH(LL, I) * SZZH(I, LL) + ODC2_ZH(LL, I) * PZZZA;
+    }
+  }
+  void hplane_pml_velocity(int L, int LL) {
+    inh_qx_int_2nd_pml(L, LL);
+    inh_v_u_int_2nd_pml(L, LL);
+    inh_qz_int_2nd_pml(L, LL);
+    inh_v_w_int_2nd_pml(L, LL);
+    sto_qxp(L);
+    sto_qzp(L);
+  }
+
+  // hplane_pmlzh0_velocity.F90:30-63
+  void hplane_pmlzh0_velocity() {
+    const int LST = MZ + TPML, LST1 = LST - 1, LST2 = LST - 2;
+    for (int I = 1 - TPML; I <= MX + TPML; ++I) {
+      UM(I, LST) = ABH01 * UM(I, LST1) + ABH02 * UM(I, LST2)
+                   + ABH10 * SZ_U(I, 0) + ABH11 * SZ_U(I, 1) + ABH12 * SZ_U(I, 2)
+                   + ABH20 * SZ_UP(I, 0) + ABH21 * SZ_UP(I, 1) + ABH22 * SZ_UP(I, 2);
+      WM(I, LST) = ABW01 * WM(I, LST1) + ABW02 * WM(I, LST2)
+                   + ABW10 * SZ_W(I, 0) + ABW11 * SZ_W(I, 1) + ABW12 * SZ_W(I, 2)
+                   + ABW20 * SZ_WP(I, 0) + ABW21 * SZ_WP(I, 1) + ABW22 * SZ_WP(I, 2);
+      QX(I, LST) = ABH01 * QX(I, LST1) + ABH02 * QX(I, LST2)
+                   + ABH10 * SZ_QX(I, 0) + ABH11 * SZ_QX(I, 1) + ABH12 * SZ_QX(I, 2)
+                   + ABH20 * SZ_QXP(I, 0) + ABH21 * SZ_QXP(I, 1) + ABH22 * SZ_QXP(I, 2);
+      QZ(I, LST) = ABW01 * QZ(I, LST1) + ABW02 * QZ(I, LST2)
+                   + ABW10 * SZ_QZ(I, 0) + ABW11 * SZ_QZ(I, 1) + ABW12 * SZ_QZ(I, 2)
+                   + ABW20 * SZ_QZP(I, 0) + ABW21 * SZ_QZP(I, 1) + ABW22 * SZ_QZP(I, 2);
+    }
+  }
+
+  // time_loop.F90:133-155
+  void store_bottom() {
+    SZ_UP = SZ_U; SZ_WP = SZ_W; SZ_QXP = SZ_QX; SZ_QZP = SZ_QZ;
+    for (int I = PMLL; I <= PMLXH; ++I) {
+      SZ_U(I, 2) = UM(I, PMLZH2); SZ_W(I, 2) = WM(I, PMLZH2); SZ_QX(I, 2) = QX(I, PMLZH2); SZ_QZ(I, 2) = QZ(I, PMLZH2);
+      SZ_U(I, 1) = UM(I, PMLZH1); SZ_W(I, 1) = WM(I, PMLZH1); SZ_QX(I, 1) = QX(I, PMLZH1); SZ_QZ(I, 1) = QZ(I, PMLZH1);
+      SZ_U(I, 0) = UM(I, PMLZH); SZ_W(I, 0) = WM(I, PMLZH); SZ_QX(I, 0) = QX(I, PMLZH); SZ_QZ(I, 0) = QZ(I, PMLZH);
+    }
+  }
+
+  // store_seismograms.F90:47-104,138-154 and store_seismograms_pressure.F90:45-58,76-83
+  // One record of 10 values per receiver: SSU SSW SPU SPW SSQX SSQZ ZPU ZPW SSP SST.
+  void store_seismograms(T* rec) {
+    for (int J = 0; J < MR; ++J) {
+      T* r = rec + (size_t)J * 10;
+      for (int k = 0; k < 10; ++k) r[k] = 0;
+      int IR = IRECX[J], LR = LRECX[J];
+      T SPU = 0, ZPU = 0, SPW = 0, ZPW = 0;
+      if (PMLL <= IR && IR <= PMLXH && 0 <= LR && LR <= PMLZH) {
+        T S = UM(IR, LR);
+        SPU = (S - SSU[J]) / DT;
+        SSU[J] = S;
+        if (KEY_TLQ) {
+          T Z = QX(IR, LR);
+          ZPU = (Z - SSQX[J]) / DT;
+          SSQX[J] = Z;
+        }
+      }
+      IR = IRECZ[J]; LR = LRECZ[J];
+      if (PMLL <= IR && IR <= PMLXH && 0 <= LR && LR <= PMLZH) {
+        T S = -WM(IR, LR);
+        SPW = (S - SSW[J]) / DT;
+        SSW[J] = S;
+        if (KEY_TLQ) {
+          T Z = -QZ(IR, LR);
+          ZPW = (Z - SSQZ[J]) / DT;
+          SSQZ[J] = Z;
+        }
+      }
+      r[0] = SSU[J]; r[1] = SSW[J]; r[2] = SPU; r[3] = SPW;
+      r[4] = SSQX[J]; r[5] = SSQZ[J]; r[6] = ZPU; r[7] = ZPW;
+      IR = IRECZ[J]; LR = LRECX[J];
+      if (PMLL <= IR && IR <= PMLXH && 0 <= LR && LR <= PMLZH) {
+        r[8] = PRES(IR, LR);
+        r[9] = -TXX(IR, LR);
+      }
+    }
+  }
+
+  // One time level ITILE of time_loop.F90:65-206 (serial build).
+  void step(int ITILE, T* rec) {
+    const int Z_MIN = 0, Z_MAX = PMLZH;
+    T SOURS = 0, SOURF = 0;
+    if (ITILE >= 1 && ITILE <= MT2) {
+      SOURS = SOURTF[2 * (size_t)(ITILE - 1)];
+      SOURF = SOURTF[2 * (size_t)(ITILE - 1) + 1];
+    }
+    auto rows = [&](int lo, int hi, auto&& fn) {
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads)
+      {
+        Strain<T> s;
+        s.alloc(PMLL, PMLXH);
+#pragma omp for schedule(static)
+        for (int L = lo; L <= hi; ++L) fn(s, L);
+      }
+#else
+      Strain<T> s;
+      s.alloc(PMLL, PMLXH);
+      for (int L = lo; L <= hi; ++L) fn(s, L);
+#endif
+    };
+    Strain<T> s;
+    s.alloc(PMLL, PMLXH);
+    // ---- UPDATE STRESS FIELD (time_loop.F90:93-124)
+    rows(std::max(Z_MIN, 2), std::min(Z_MAX, LIN_Z - 1), [&](Strain<T>& ss, int L) { hplane_ic_stress(ss, L); });
+    if (Z_MIN <= LIN_Z && LIN_Z <= Z_MAX) hplane_ic_stress(s, LIN_Z, true, SOURS, SOURF);
+    rows(std::max(Z_MIN, LIN_Z + 1), std::min(Z_MAX, MZ - 2), [&](Strain<T>& ss, int L) { hplane_ic_stress(ss, L); });
+    hplane_0_stress(s);
+    hplane_1_stress(s);
+    hplane_mz1_stress(s);
+    rows(std::max(Z_MIN, MZ), std::min(Z_MAX, PMLZH1), [&](Strain<T>& ss, int L) { hplane_pml_stress(ss, L, L - MZ + 1); });
+    hplane_pmlzh0_stress(s);
+    // ---- STORE BOTTOM BOUNDARY (time_loop.F90:133-155)
+    store_bottom();
+    // ---- UPDATE VELOCITY FIELD (time_loop.F90:159-179)
+    rows(std::max(Z_MIN, 2), std::min(Z_MAX, MZ - 2), [&](Strain<T>&, int L) { hplane_ic_velocity(L); });
+    if (SI) {
+      hplane_1_velocity();
+    } else {
+      hplane_0_velocity();
+      hplane_1_velocity();
+    }
+    rows(std::max(Z_MIN, MZ - 1), std::min(Z_MAX, PMLZH1), [&](Strain<T>&, int L) { hplane_pml_velocity(L, L - MZ + 1); });
+    hplane_pmlzh0_velocity();
+    // ---- STORE RESULTS (time_loop.F90:194-200)
+    if (rec) store_seismograms(rec);
+  }
+};
+
+struct Handle {
+  int prec;  // 4 or 8
+  Sim<float>* f = nullptr;
+  Sim<double>* d = nullptr;
+  std::string err;
+};
+
+template <class T> static void set_medium(Sim<T>* s, const int32_t* jm, int jmnum, const T* tab) {
+  s->JMNUM = jmnum;
+  std::vector<T>* cols[24] = {&s->MU, &s->SIG_XX_1, &s->SIG_XX_2, &s->SIG_XX_3, &s->SIG_ZZ_1, &s->SIG_ZZ_2,
+                              &s->SIG_ZZ_3, &s->PRES_1, &s->PRES_2, &s->PRES_3, &s->REL1_U, &s->REL1_W,
+                              &s->REL2_U, &s->REL2_W, &s->REL3_U, &s->REL3_W, &s->REL1_QX, &s->REL1_QZ,
+                              &s->REL2_QX, &s->REL2_QZ, &s->REL3_QX, &s->REL3_QZ, &s->AUXIL_W, &s->AUXIL_QZ};
+  // read_model_par.F90:147-155 record order; index 1..JMNUM (slot 0 unused)
+  for (int c = 0; c < 24; ++c) cols[c]->assign((size_t)jmnum + 1, T(0));
+  for (int j = 1; j <= jmnum; ++j)
+    for (int c = 0; c < 24; ++c) (*cols[c])[j] = tab[(size_t)(j - 1) * 24 + c];
+  std::memcpy(s->JM.v.data(), jm, s->JM.v.size() * sizeof(int32_t));
+  for (int32_t v : s->JM.v)
+    if (v < 1 || v > jmnum) throw BoundsError("JM value outside 1..JMNUM");
+}
+
+template <class T> static void set_profiles(Sim<T>* s, const T* const* p) {
+  FA2<T>* a[24] = {&s->ODA_XL, &s->ODB_XL, &s->ODC_XL, &s->ODD_XL, &s->ODA_XH, &s->ODB_XH, &s->ODC_XH, &s->ODD_XH,
+                   &s->ODA_ZH, &s->ODB_ZH, &s->ODC_ZH, &s->ODD_ZH,
+                   &s->ODA2_XL, &s->ODB2_XL, &s->ODC2_XL, &s->ODD2_XL, &s->ODA2_XH, &s->ODB2_XH, &s->ODC2_XH, &s->ODD2_XH,
+                   &s->ODA2_ZH, &s->ODB2_ZH, &s->ODC2_ZH, &s->ODD2_ZH};
+  for (int k = 0; k < 24; ++k) std::memcpy(a[k]->v.data(), p[k], a[k]->v.size() * sizeof(T));
+}
+
+template <class T> static void set_nr(Sim<T>* s, const T* ab) {
+  // order: ABW01 ABW02 ABW10 ABW11 ABW12 ABW20 ABW21 ABW22, then ABH in the same order
+  T* w[16] = {&s->ABW01, &s->ABW02, &s->ABW10, &s->ABW11, &s->ABW12, &s->ABW20, &s->ABW21, &s->ABW22,
+              &s->ABH01, &s->ABH02, &s->ABH10, &s->ABH11, &s->ABH12, &s->ABH20, &s->ABH21, &s->ABH22};
+  for (int k = 0; k < 16; ++k) *w[k] = ab[k];
+}
+
+}  // namespace
+
+#define ORC_TRY(h, body)                               \
+  try { body; return 0; }                              \
+  catch (const std::exception& e) { if (h) ((Handle*)h)->err = e.what(); return -1; }
+
+extern "C" {
+
+void* orc_create(int prec, int mx, int mz, int tpml, int si, double h, double dt, double tau_eps, int lin_x, int lin_z) {
+  Handle* hd = new Handle();
+  hd->prec = prec;
+  if (prec == 8) { hd->d = new Sim<double>(); hd->d->init(mx, mz, tpml, si, h, dt, tau_eps, lin_x, lin_z); }
+  else { hd->f = new Sim<float>(); hd->f->init(mx, mz, tpml, si, (float)h, (float)dt, (float)tau_eps, lin_x, lin_z); }
+  return hd;
+}
+
+void orc_destroy(void* h) {
+  Handle* hd = (Handle*)h;
+  delete hd->f; delete hd->d; delete hd;
+}
+
+const char* orc_error(void* h) { return ((Handle*)h)->err.c_str(); }
+
+int orc_set_threads(void* h, int n) {
+  Handle* hd = (Handle*)h;
+  if (hd->f) hd->f->nthreads = n; else hd->d->nthreads = n;
+  return 0;
+}
+
+int orc_set_medium(void* h, const int32_t* jm, int jmnum, const void* table24) {
+  Handle* hd = (Handle*)h;
+  ORC_TRY(h, if (hd->f) set_medium(hd->f, jm, jmnum, (const float*)table24);
+             else set_medium(hd->d, jm, jmnum, (const double*)table24));
+}
+
+int orc_set_profiles(void* h, const void* const* p) {
+  Handle* hd = (Handle*)h;
+  ORC_TRY(h, if (hd->f) set_profiles(hd->f, (const float* const*)p);
+             else set_profiles(hd->d, (const double* const*)p));
+}
+
+int orc_set_bottom_nr(void* h, const void* ab16) {
+  Handle* hd = (Handle*)h;
+  ORC_TRY(h, if (hd->f) set_nr(hd->f, (const float*)ab16); else set_nr(hd->d, (const double*)ab16));
+}
+
+int orc_set_source(void* h, const void* sourtf, int mt2) {
+  Handle* hd = (Handle*)h;
+  ORC_TRY(h, if (hd->f) { hd->f->MT2 = mt2; hd->f->SOURTF.assign((const float*)sourtf, (const float*)sourtf + 2 * (size_t)mt2); }
+             else { hd->d->MT2 = mt2; hd->d->SOURTF.assign((const double*)sourtf, (const double*)sourtf + 2 * (size_t)mt2); });
+}
+
+int orc_set_receivers(void* h, const int32_t* irecx, const int32_t* lrecx, const int32_t* irecz,
+                      const int32_t* lrecz, int mr, int key_tlq) {
+  Handle* hd = (Handle*)h;
+  auto setr = [&](auto* s) {
+    s->MR = mr; s->KEY_TLQ = key_tlq != 0;
+    s->IRECX.assign(irecx, irecx + mr); s->LRECX.assign(lrecx, lrecx + mr);
+    s->IRECZ.assign(irecz, irecz + mr); s->LRECZ.assign(lrecz, lrecz + mr);
+    s->SSU.assign(mr, 0); s->SSW.assign(mr, 0); s->SSQX.assign(mr, 0); s->SSQZ.assign(mr, 0);
+  };
+  ORC_TRY(h, if (hd->f) setr(hd->f); else setr(hd->d));
+}
+
+// Runs time levels it_begin..it_end (inclusive, 1-based).  rec_out, if not
+// null, receives MR*10 values per level in the precision of the run.
+int orc_run(void* h, int it_begin, int it_end, void* rec_out) {
+  Handle* hd = (Handle*)h;
+  ORC_TRY(h, {
+    for (int it = it_begin; it <= it_end; ++it) {
+      if (hd->f) {
+        float* r = rec_out ? (float*)rec_out + (size_t)(it - it_begin) * hd->f->MR * 10 : nullptr;
+        hd->f->step(it, r);
+      } else {
+        double* r = rec_out ? (double*)rec_out + (size_t)(it - it_begin) * hd->d->MR * 10 : nullptr;
+        hd->d->step(it, r);
+      }
+    }
+  });
+}
+
+int orc_field_bounds(void* h, int id, int* b4) {
+  Handle* hd = (Handle*)h;
+  if (hd->f) {
+    auto* a = hd->f->field(id);
+    if (!a) return -1;
+    b4[0] = a->lx; b4[1] = a->ux; b4[2] = a->lz; b4[3] = a->uz;
+  } else {
+    auto* a = hd->d->field(id);
+    if (!a) return -1;
+    b4[0] = a->lx; b4[1] = a->ux; b4[2] = a->lz; b4[3] = a->uz;
+  }
+  return 0;
+}
+
+// set != 0 copies buf into the field, else copies the field into buf.
+int orc_field(void* h, int id, void* buf, int set) {
+  Handle* hd = (Handle*)h;
+  if (hd->f) {
+    auto* a = hd->f->field(id);
+    if (!a) return -1;
+    if (set) std::memcpy(a->v.data(), buf, a->v.size() * 4); else std::memcpy(buf, a->v.data(), a->v.size() * 4);
+  } else {
+    auto* a = hd->d->field(id);
+    if (!a) return -1;
+    if (set) std::memcpy(a->v.data(), buf, a->v.size() * 8); else std::memcpy(buf, a->v.data(), a->v.size() * 8);
+  }
+  return 0;
+}
+
+}  // extern "C"
