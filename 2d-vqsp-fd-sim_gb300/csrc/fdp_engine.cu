@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -41,12 +42,16 @@ struct fdp_ctx {
   int prec = 4;
   int MX = 0, MZ = 0, TPML = 0, PMLL = 0, PMLXH = 0, PMLZH = 0, NX = 0, NZ = 0, MX1 = 0;
   int pitch = 0, rows_alloc = 0;
-  int tz = 16, ntz = 1;
+  int medium_mode = fdp::M_TABLE;
+  int src[fdp::C_NCOEF], neg[fdp::C_NCOEF];
+  double cval_d[fdp::C_NCOEF];
+  float cval_f[fdp::C_NCOEF];
+  int nplanes = 0;
   cudaStream_t stream = nullptr;
   std::string err;
   // device memory
   DevArr fields[8];
-  DevArr jm, coef, prof[24], mem[27], ab, hist, stf, rec, raw, itbase;
+  DevArr jm, coef, planes, aux, prof[24], mem[27], ab, hist, stf, rec, raw, itbase;
   int jmnum = 0;
   int mt2 = 0;
   int mr = 0, rec_flags = 0;
@@ -138,7 +143,7 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   std::memset(&p, 0, sizeof p);
   p.MX = c->MX; p.MZ = c->MZ; p.TPML = c->TPML; p.PMLL = c->PMLL; p.PMLXH = c->PMLXH; p.PMLZH = c->PMLZH;
   p.NX = c->NX; p.NZ = c->NZ; p.MX1 = c->MX1; p.LIN_X = c->g.lin_x; p.LIN_Z = c->g.lin_z;
-  p.pitch = c->pitch; p.tz = c->tz; p.ntz = c->ntz;
+  p.pitch = c->pitch;
   // mod_auxil.F90:19-20 (default-real constants) and aux1.F90:44-46
   const T H = (T)c->g.h;
   p.A = (T)(-1.0f / 24.0f);
@@ -150,9 +155,17 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   const size_t off = (size_t)kPadZ * c->pitch + kPadX;
   T** f[8] = {&p.UM, &p.WM, &p.QX, &p.QZ, &p.TXX, &p.TZZ, &p.TXZ, &p.PRES};
   for (int k = 0; k < 8; ++k) *f[k] = (T*)c->fields[k].p + off;
-  p.JM = (const int32_t*)c->jm.p + off;
+  p.JM = c->jm.p ? (const int32_t*)c->jm.p + off : nullptr;
   p.coef = (const T*)c->coef.p;
   p.cld = c->jmnum + 1;
+  p.planes = c->planes.p ? (const T*)c->planes.p + off : nullptr;
+  p.pstride = (long long)c->rows_alloc * c->pitch;
+  for (int k = 0; k < fdp::C_NCOEF; ++k) {
+    p.src[k] = c->src[k];
+    p.neg[k] = c->neg[k];
+    p.cval[k] = sizeof(T) == 8 ? (T)c->cval_d[k] : (T)c->cval_f[k];
+  }
+  p.AUX = (const T*)c->aux.p;
   const T** pr[24] = {&p.ODA_XL, &p.ODB_XL, &p.ODC_XL, &p.ODD_XL, &p.ODA_XH, &p.ODB_XH, &p.ODC_XH, &p.ODD_XH,
                       &p.ODA_ZH, &p.ODB_ZH, &p.ODC_ZH, &p.ODD_ZH,
                       &p.ODA2_XL, &p.ODB2_XL, &p.ODC2_XL, &p.ODD2_XL, &p.ODA2_XH, &p.ODB2_XH, &p.ODC2_XH, &p.ODD2_XH,
@@ -172,22 +185,32 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   p.RAW = (T*)c->raw.p;
 }
 
-template <class T, bool SI> int launch_level(fdp_ctx* c, const Params<T>& p, int it_off) {
-  const dim3 blk(kBlockX, 1, 1);
-  const dim3 grd((c->NX + kBlockX - 1) / kBlockX, c->ntz, 1);
-  fdp::k_stress<T, SI><<<grd, blk, 0, c->stream>>>(p, it_off);
-  fdp::k_velocity<T, SI><<<grd, blk, 0, c->stream>>>(p, it_off);
-  const int nedge = std::max(SI ? c->NX : 0, c->mr);
-  if (nedge > 0) {
-    fdp::k_edge<T, SI><<<(nedge + kBlockX - 1) / kBlockX, blk, 0, c->stream>>>(p, it_off);
-    c->launches += 1;
-  }
-  c->launches += 2;
-  return FDP_OK;
+dim3 cell_grid(const fdp_ctx* c) {
+  return dim3((c->NX + fdp::kBX - 1) / fdp::kBX, (c->NZ + fdp::kBZ - 1) / fdp::kBZ, 1);
+}
+
+int edge_threads(const fdp_ctx* c) { return std::max(c->g.stress_imaging ? c->NX : 0, c->mr); }
+
+// kind 0 = stress phase, 1 = velocity phase, 2 = edge (imaging row 1 and receivers)
+template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
+  const dim3 blk(fdp::kBX, fdp::kBZ, 1);
+  if (kind == 0) fdp::k_stress<T, SI, MODE><<<cell_grid(c), blk, 0, c->stream>>>(p, it_off);
+  else if (kind == 1) fdp::k_velocity<T, SI, MODE><<<cell_grid(c), blk, 0, c->stream>>>(p, it_off);
+  else fdp::k_edge<T, SI><<<(edge_threads(c) + kBlockX - 1) / kBlockX, kBlockX, 0, c->stream>>>(p, it_off);
+  c->launches += 1;
+}
+
+template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
+  const bool si = c->g.stress_imaging != 0, tab = c->medium_mode == fdp::M_TABLE;
+  if (si) tab ? launch_kind<T, true, fdp::M_TABLE>(c, p, kind, it_off) : launch_kind<T, true, fdp::M_PLANES>(c, p, kind, it_off);
+  else tab ? launch_kind<T, false, fdp::M_TABLE>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_PLANES>(c, p, kind, it_off);
 }
 
 template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_off) {
-  return c->g.stress_imaging ? launch_level<T, true>(c, p, it_off) : launch_level<T, false>(c, p, it_off);
+  launch<T>(c, p, 0, it_off);
+  launch<T>(c, p, 1, it_off);
+  if (edge_threads(c) > 0) launch<T>(c, p, 2, it_off);
+  return FDP_OK;
 }
 
 template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
@@ -217,7 +240,7 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) { c->graph = nullptr; return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
   }
-  const int per_level = 2 + ((std::max(c->g.stress_imaging ? c->NX : 0, c->mr) > 0) ? 1 : 0);
+  const int per_level = 2 + (edge_threads(c) > 0 ? 1 : 0);
   while (it_end - it + 1 >= kChunk && c->graph) {
     CK(c, cudaGraphLaunch(c->graph, c->stream));
     c->launches += (long long)kChunk * per_level + 1;
@@ -260,6 +283,96 @@ void derive_table(const int32_t jmnum, const T* tab, std::vector<T>& out) {
   }
 }
 
+// Materials at most this many use table mode when some coefficient varies;
+// a larger table (one material per cell) is expanded into per-cell planes.
+constexpr int kMaxTableMaterials = 4096;
+
+template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate) {
+  using U = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
+  const U sign = (U)1 << (sizeof(T) * 8 - 1);
+  for (size_t i = 0; i < n; ++i) {
+    U x, y;
+    std::memcpy(&x, &a[i], sizeof(T));
+    std::memcpy(&y, &b[i], sizeof(T));
+    if ((negate ? (x ^ sign) : x) != y) return false;
+  }
+  return true;
+}
+
+// Chooses the device representation of the medium and uploads it: the
+// derived coefficient columns are classified as constant (folded into the
+// kernel parameters), equal up to sign to an earlier column (shared plane),
+// or distinct; distinct columns become per-cell planes when the material
+// table is large, else the kernels index the table through JM.
+template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum, const T* table24) {
+  std::vector<T> t;
+  derive_table<T>(jmnum, table24, t);
+  const size_t ld = (size_t)jmnum + 1;
+  int rc;
+  // AUXIL_W / AUXIL_QZ of JM(I,0) (inh_w_qz_int_1_si.F90:32)
+  std::vector<T> aux((size_t)2 * c->NX);
+  for (int x = 0; x < c->NX; ++x) {
+    const int j = jm[x];
+    aux[x] = t[(size_t)fdp::C_AUXW * ld + j];
+    aux[(size_t)c->NX + x] = t[(size_t)fdp::C_AUXQZ * ld + j];
+  }
+  if ((rc = dev_alloc(c, c->aux, aux.size() * sizeof(T))) != FDP_OK) return rc;
+  if ((rc = copy_sync(c, c->aux.p, aux.data(), aux.size() * sizeof(T), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  // column classification (the AUXIL columns are served by `aux` above)
+  std::vector<int> plane_col;
+  for (int k = 0; k < fdp::C_NCOEF; ++k) {
+    c->src[k] = -1; c->neg[k] = 0; c->cval_d[k] = 0; c->cval_f[k] = 0;
+    if (k == fdp::C_AUXW || k == fdp::C_AUXQZ) continue;
+    const T* col = &t[(size_t)k * ld + 1];
+    bool constant = true;
+    for (int j = 1; j < jmnum && constant; ++j) constant = same_bits(&col[0], &col[j], 1, false);
+    if (constant) {
+      c->cval_d[k] = (double)col[0];
+      c->cval_f[k] = (float)col[0];
+      continue;
+    }
+    for (size_t q = 0; q < plane_col.size() && c->src[k] < 0; ++q) {
+      const T* other = &t[(size_t)plane_col[q] * ld + 1];
+      if (same_bits(other, col, (size_t)jmnum, false)) { c->src[k] = (int)q; c->neg[k] = 0; }
+      else if (same_bits(other, col, (size_t)jmnum, true)) { c->src[k] = (int)q; c->neg[k] = 1; }
+    }
+    if (c->src[k] < 0) { c->src[k] = (int)plane_col.size(); plane_col.push_back(k); }
+  }
+  c->nplanes = (int)plane_col.size();
+  const bool table_mode = c->nplanes > 0 && jmnum <= kMaxTableMaterials;
+  c->medium_mode = table_mode ? fdp::M_TABLE : fdp::M_PLANES;
+  const size_t cells = (size_t)c->rows_alloc * c->pitch;
+  if (table_mode) {
+    // JM into the padded field layout (padding holds material 1) and the table
+    std::vector<int32_t> h(cells, 1);
+    for (int L = 0; L < c->NZ; ++L)
+      std::memcpy(&h[(size_t)(L + kPadZ) * c->pitch + kPadX], jm + (size_t)L * c->NX, (size_t)c->NX * sizeof(int32_t));
+    if ((rc = dev_alloc(c, c->jm, h.size() * sizeof(int32_t))) != FDP_OK) return rc;
+    if ((rc = copy_sync(c, c->jm.p, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+    if ((rc = dev_alloc(c, c->coef, t.size() * sizeof(T))) != FDP_OK) return rc;
+    if ((rc = copy_sync(c, c->coef.p, t.data(), t.size() * sizeof(T), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+    dev_alloc(c, c->planes, 0);
+  } else {
+    dev_alloc(c, c->jm, 0);
+    dev_alloc(c, c->coef, 0);
+    if ((rc = dev_alloc(c, c->planes, std::max<size_t>(1, (size_t)c->nplanes * cells) * sizeof(T))) != FDP_OK) return rc;
+    std::vector<T> pl(cells);
+    for (int q = 0; q < c->nplanes; ++q) {
+      const T* col = &t[(size_t)plane_col[q] * ld];
+      std::fill(pl.begin(), pl.end(), col[1]);
+      for (int L = 0; L < c->NZ; ++L) {
+        T* dst = &pl[(size_t)(L + kPadZ) * c->pitch + kPadX];
+        const int32_t* src = jm + (size_t)L * c->NX;
+        for (int x = 0; x < c->NX; ++x) dst[x] = col[src[x]];
+      }
+      if ((rc = copy_sync(c, (T*)c->planes.p + (size_t)q * cells, pl.data(), cells * sizeof(T),
+                          cudaMemcpyHostToDevice)) != FDP_OK)
+        return rc;
+    }
+  }
+  return FDP_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -287,13 +400,6 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   c->NZ = c->PMLZH + 1;
   c->pitch = ((c->NX + 2 * kPadX + 31) / 32) * 32;
   c->rows_alloc = c->NZ + 2 * kPadZ;
-  // z-tiles of tz rows; the last tile takes the remainder (>= tz rows)
-  const int nbx = (c->NX + kBlockX - 1) / kBlockX;
-  int tz = 16;
-  while (tz > 5 && (long long)nbx * (c->NZ / tz) < 4LL * 152) --tz;
-  if (tz > c->NZ) tz = c->NZ;
-  c->tz = tz;
-  c->ntz = std::max(1, c->NZ / tz);
   auto bail = [&](int code) { g_create_error = c->err; fdp_destroy(c); return code; };
   cudaError_t e = cudaSetDevice(g->device);
   if (e != cudaSuccess) { c->err = std::string("cudaSetDevice: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
@@ -337,22 +443,9 @@ int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_
     if (jm[k] < 1 || jm[k] > jmnum) return fail(c, FDP_ERR_ARG, "JM value %d at %zu outside 1..%d", jm[k], k, jmnum);
   int rc;
   CK(c, cudaStreamSynchronize(c->stream));
-  // JM into the padded field layout (padding holds material 1)
-  std::vector<int32_t> h((size_t)c->rows_alloc * c->pitch, 1);
-  for (int L = 0; L < c->NZ; ++L)
-    std::memcpy(&h[(size_t)(L + kPadZ) * c->pitch + kPadX], jm + (size_t)L * c->NX, (size_t)c->NX * sizeof(int32_t));
-  if ((rc = copy_sync(c, c->jm.p, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
-  if (c->prec == 8) {
-    std::vector<double> t;
-    derive_table<double>(jmnum, (const double*)table24, t);
-    if ((rc = dev_alloc(c, c->coef, t.size() * 8)) != FDP_OK) return rc;
-    if ((rc = copy_sync(c, c->coef.p, t.data(), t.size() * 8, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
-  } else {
-    std::vector<float> t;
-    derive_table<float>(jmnum, (const float*)table24, t);
-    if ((rc = dev_alloc(c, c->coef, t.size() * 4)) != FDP_OK) return rc;
-    if ((rc = copy_sync(c, c->coef.p, t.data(), t.size() * 4, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
-  }
+  rc = (c->prec == 8) ? build_medium<double>(c, jm, jmnum, (const double*)table24)
+                      : build_medium<float>(c, jm, jmnum, (const float*)table24);
+  if (rc != FDP_OK) return rc;
   CK(c, cudaStreamSynchronize(c->stream));
   c->jmnum = jmnum;
   c->have_medium = true;
@@ -546,13 +639,63 @@ int fdp_synchronize(fdp_ctx* c) {
 
 int64_t fdp_kernel_launches(fdp_ctx* c) { return c ? c->launches : 0; }
 
+int fdp_get_stream(fdp_ctx* c, void** stream) {
+  if (!c || !stream) return fail(c, FDP_ERR_ARG, "null argument");
+  *stream = (void*)c->stream;
+  return FDP_OK;
+}
+
+int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out, int64_t* launches_out) {
+  if (!c || !ms_out || !launches_out) return fail(c, FDP_ERR_ARG, "null argument");
+  if (!c->have_medium || !c->have_pml || !c->have_nr || !c->have_source)
+    return fail(c, FDP_ERR_STATE, "set medium, PML profiles, bottom coefficients and source before profiling");
+  if (it_begin < 1 || it_end > c->mt2 || it_end < it_begin)
+    return fail(c, FDP_ERR_ARG, "levels %d..%d outside 1..MT2=%d", it_begin, it_end, c->mt2);
+  CK(c, cudaSetDevice(c->g.device));
+  for (int k = 0; k < 3; ++k) { ms_out[k] = 0.0; launches_out[k] = 0; }
+  auto body = [&](auto zero) -> int {
+    using T = decltype(zero);
+    Params<T> p;
+    fill_params<T>(c, p);
+    const int nedge = edge_threads(c);
+    cudaEvent_t ev[4];
+    for (auto& e : ev) CK(c, cudaEventCreate(&e));
+    fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
+    for (int it = it_begin; it <= it_end; ++it) {
+      const int off = it - it_begin;
+      CK(c, cudaEventRecord(ev[0], c->stream));
+      launch<T>(c, p, 0, off);
+      CK(c, cudaEventRecord(ev[1], c->stream));
+      launch<T>(c, p, 1, off);
+      CK(c, cudaEventRecord(ev[2], c->stream));
+      if (nedge > 0) launch<T>(c, p, 2, off);
+      CK(c, cudaEventRecord(ev[3], c->stream));
+      CK(c, cudaEventSynchronize(ev[3]));
+      float t;
+      for (int k = 0; k < 3; ++k) {
+        CK(c, cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+        ms_out[k] += t;
+      }
+      launches_out[0] += 1; launches_out[1] += 1; launches_out[2] += nedge > 0 ? 1 : 0;
+    }
+    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_end - it_begin + 1);
+    c->launches += 2;
+    for (auto& e : ev) cudaEventDestroy(e);
+    CK(c, cudaStreamSynchronize(c->stream));
+    CK(c, cudaGetLastError());
+    if (it_end > c->last_it) c->last_it = it_end;
+    return FDP_OK;
+  };
+  return c->prec == 8 ? body(0.0) : body(0.0f);
+}
+
 const char* fdp_last_error(const fdp_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
 
 void fdp_destroy(fdp_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  DevArr* all[] = {&c->jm, &c->coef, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase};
+  DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase};
   for (auto* a : all) if (a->p) cudaFree(a->p);
   for (auto& a : c->fields) if (a.p) cudaFree(a.p);
   for (auto& a : c->prof) if (a.p) cudaFree(a.p);

@@ -12,10 +12,17 @@
 // order and the code is compiled without FMA contraction, so a kernel's
 // results equal a serial CPU evaluation of the same routines bit for bit.
 //
+// Threads: one cell per thread, blocks of 32 (x) x 8 (z) cells; a warp is
+// 32 consecutive cells of one row, so every row class is warp-uniform.
+//
 // Layout (all arrays x-fastest, the reference's column-major order):
 //   fields   T[NZ + 2*PADZ][pitch], pointer p.F points at (I=PMLL, L=0)
-//   JM       int32 in the field layout
-//   medium   derived per-material table coef[k*cld + jm], jm = 1..JMNUM
+//   medium   either (table mode) JM int32 in the field layout and a derived
+//            per-material table coef[k*cld + jm], or (plane mode) one plane
+//            per distinct derived coefficient column in the field layout,
+//            with columns that are equal (or equal up to sign) across all
+//            materials stored once and columns that are constant folded
+//            into the kernel parameters
 //   x-PML profiles [L][J] (the reference's own layout), z-PML profiles
 //            stored transposed [J][I-PMLL] so a warp reads them coalesced
 //   memory variables in the reference's own bounds (ppml.F90:85-112)
@@ -41,16 +48,28 @@ enum Coef {
 
 constexpr int kPadX = 4;
 constexpr int kPadZ = 2;
+constexpr int kBX = 32;  // block width (cells along x)
+constexpr int kBZ = 8;   // block height (rows)
+
+enum MediumMode { M_TABLE = 0, M_PLANES = 1 };
 
 template <class T> struct Params {
   int MX, MZ, TPML, PMLL, PMLXH, PMLZH, NX, NZ, MX1, LIN_X, LIN_Z;
   int pitch;    // field row pitch in elements
-  int tz, ntz;  // rows per z-tile and number of z-tiles
   T AH, BH, CH, BC, A, B, DT, DTE;
   T *UM, *WM, *QX, *QZ, *TXX, *TZZ, *TXZ, *PRES;
+  // medium, table mode
   const int32_t* JM;
   const T* coef;
   long long cld;
+  // medium, plane mode: coefficient k is cval[k] when src[k] < 0, else plane
+  // src[k] (negated when neg[k]) at the cell's field offset
+  const T* planes;
+  long long pstride;
+  int src[C_NCOEF];
+  int neg[C_NCOEF];
+  T cval[C_NCOEF];
+  const T* AUX;  // [2][NX]: AUXIL_W and AUXIL_QZ of JM(I,0), for the imaging row 1
   // x-PML profiles, [L][J]: OD* with J in 0..TPML, OD2* with J in 0..TPML+1
   const T *ODA_XL, *ODB_XL, *ODC_XL, *ODD_XL, *ODA_XH, *ODB_XH, *ODC_XH, *ODD_XH;
   const T *ODA2_XL, *ODB2_XL, *ODC2_XL, *ODD2_XL, *ODA2_XH, *ODB2_XH, *ODC2_XH, *ODD2_XH;
@@ -74,7 +93,22 @@ template <class T> struct Params {
 };
 
 #define FDP_F(ptr, I, L) (ptr)[(long long)(L) * p.pitch + ((I) - p.PMLL)]
-#define FDP_C(k, j) p.coef[(long long)(k) * p.cld + (j)]
+// read-only load through the non-coherent path, for arrays no thread of the
+// running kernel writes (velocities in k_stress, stresses in k_velocity)
+#define FDP_R(ptr, I, L) __ldg(&FDP_F(ptr, I, L))
+
+// Material coefficient k of the cell at field offset `cell` (material J in
+// table mode).  Negation is exact, so a plane shared up to sign returns the
+// reference's value bit for bit.
+template <class T, int MODE>
+__device__ __forceinline__ T coef(const Params<T>& p, int k, long long cell, int J) {
+  if (MODE == M_TABLE) return __ldg(p.coef + (long long)k * p.cld + J);
+  const int s = p.src[k];
+  if (s < 0) return p.cval[k];
+  const T v = __ldg(p.planes + (long long)s * p.pstride + cell);
+  return p.neg[k] ? -v : v;
+}
+#define FDP_C(k) coef<T, MODE>(p, (k), cell_, J_)
 
 // ---------------------------------------------------------------------------
 // strain_uw_xx.F90:51-94 / strain_q_xx.F90:50-91 for one cell
@@ -84,19 +118,19 @@ __device__ __forceinline__ T strain_xx(const Params<T>& p, const T* U, T* ML, T*
   if (I <= 1) {
     const int xi = (2 - I) + L * (TPML + 1);
     const int mi = (I - p.PMLL) + L * (TPML + 1);
-    const T D = p.CH * (FDP_F(U, I + 1, L) - FDP_F(U, I, L));
+    const T D = p.CH * (FDP_R(U, I + 1, L) - FDP_R(U, I, L));
     const T m = ML[mi];
     const T e = p.ODA_XL[xi] * (p.ODD_XL[xi] * D + m);
     ML[mi] = p.ODB_XL[xi] * m + p.ODC_XL[xi] * D;
     return e;
   }
-  if (I == 2) return p.CH * (FDP_F(U, 3, L) - FDP_F(U, 2, L));
+  if (I == 2) return p.CH * (FDP_R(U, 3, L) - FDP_R(U, 2, L));
   if (I <= p.MX - 2)
-    return p.AH * (FDP_F(U, I + 2, L) - FDP_F(U, I - 1, L)) + p.BH * (FDP_F(U, I + 1, L) - FDP_F(U, I, L));
-  if (I == p.MX1) return p.CH * (FDP_F(U, p.MX1 + 1, L) - FDP_F(U, p.MX1, L));
+    return p.AH * (FDP_R(U, I + 2, L) - FDP_R(U, I - 1, L)) + p.BH * (FDP_R(U, I + 1, L) - FDP_R(U, I, L));
+  if (I == p.MX1) return p.CH * (FDP_R(U, p.MX1 + 1, L) - FDP_R(U, p.MX1, L));
   const int xi = (I - p.MX1) + L * (TPML + 1);
   const int mi = (I - p.MX) + L * (TPML + 1);
-  const T D = p.CH * (FDP_F(U, I + 1, L) - FDP_F(U, I, L));
+  const T D = p.CH * (FDP_R(U, I + 1, L) - FDP_R(U, I, L));
   const T m = MH[mi];
   const T e = p.ODA_XH[xi] * (p.ODD_XH[xi] * D + m);
   MH[mi] = p.ODB_XH[xi] * m + p.ODC_XH[xi] * D;
@@ -106,8 +140,8 @@ __device__ __forceinline__ T strain_xx(const Params<T>& p, const T* U, T* ML, T*
 // strain_uw_zz.F90:41-51 / strain_q_zz.F90:41-52 (interior and non-imaging row 1)
 template <class T>
 __device__ __forceinline__ T strain_zz(const Params<T>& p, const T* W, int I, int L) {
-  T e = (p.CH * (FDP_F(W, I, L + 1) - FDP_F(W, I, L)));
-  if (I >= 2 && I <= p.MX1) e = p.AH * (FDP_F(W, I, L + 2) - FDP_F(W, I, L - 1)) + p.BC * e;
+  T e = (p.CH * (FDP_R(W, I, L + 1) - FDP_R(W, I, L)));
+  if (I >= 2 && I <= p.MX1) e = p.AH * (FDP_R(W, I, L + 2) - FDP_R(W, I, L - 1)) + p.BC * e;
   return e;
 }
 
@@ -115,7 +149,7 @@ __device__ __forceinline__ T strain_zz(const Params<T>& p, const T* W, int I, in
 template <class T>
 __device__ __forceinline__ T strain_zz_pml(const Params<T>& p, const T* W, T* M, int I, int L, int LL) {
   const int zi = (I - p.PMLL) + LL * p.NX;
-  const T D = p.CH * (FDP_F(W, I, L + 1) - FDP_F(W, I, L));
+  const T D = p.CH * (FDP_R(W, I, L + 1) - FDP_R(W, I, L));
   const T m = M[zi];
   const T e = p.ODA_ZH[zi] * (p.ODD_ZH[zi] * D + m);
   M[zi] = p.ODB_ZH[zi] * m + p.ODC_ZH[zi] * D;
@@ -126,9 +160,11 @@ __device__ __forceinline__ T strain_zz_pml(const Params<T>& p, const T* W, T* M,
 // Stress update of one cell (I, L): the row routines of hplane_ic_stress,
 // hplane_lin_stress, hplane_0/1_stress (non-imaging), hplane_mz1_stress,
 // hplane_pml_stress and hplane_pmlzh0_stress restricted to that cell.
-template <class T, bool SI>
+template <class T, bool SI, int MODE>
 __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, int it) {
   const int TPML = p.TPML, MX = p.MX, MX1 = p.MX1;
+  const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
+  const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
   const bool last = (L == p.PMLZH);
   const bool pml = (L >= p.MZ) && !last;
   const bool mz1 = (L == p.MZ - 1);
@@ -143,8 +179,8 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
     } else if (pml || last) {
       // strain_uw_xz_2nd_pml.F90:69-121
       const int LL = last ? TPML + 1 : L - p.MZ + 1;
-      const T DZXA = p.CH * (FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
-      const T DXZA = p.CH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1));
+      const T DZXA = p.CH * (FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
+      const T DXZA = p.CH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1));
       const int zi = (I - p.PMLL) + LL * p.NX;
       const T mz = p.PXZH[zi];
       const T zpart = p.ODA2_ZH[zi] * (p.ODD2_ZH[zi] * DXZA + mz);
@@ -166,33 +202,32 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
       p.PXZH[zi] = p.ODB2_ZH[zi] * mz + p.ODC2_ZH[zi] * DXZA;
     } else if (I <= 2) {
       // strain_uw_xz.F90:181-196 (and strain_uw_xz_1.F90:62-76)
-      const T DZXA = p.CH * (FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
+      const T DZXA = p.CH * (FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
       const int xi = (3 - I) + L * (TPML + 2);
       const int mi = (I - p.PMLL) + L * (TPML + 2);
       const T mx = p.PZXL[mi];
-      exz = p.CH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1)) + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
+      exz = p.CH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1)) + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
       p.PZXL[mi] = p.ODB2_XL[xi] * mx + p.ODC2_XL[xi] * DZXA;
     } else if (I <= MX1) {
       if (r1) {
         // strain_uw_xz_1.F90:79-97 (AFDA_XZ undefined)
-        exz = p.AH * (FDP_F(p.WM, I + 1, 1) - FDP_F(p.WM, I - 2, 1)) + p.BH * (FDP_F(p.WM, I, 1) - FDP_F(p.WM, I - 1, 1))
-            + p.CH * (FDP_F(p.UM, I, 1) - FDP_F(p.UM, I, 0));
+        exz = p.AH * (FDP_R(p.WM, I + 1, 1) - FDP_R(p.WM, I - 2, 1)) + p.BH * (FDP_R(p.WM, I, 1) - FDP_R(p.WM, I - 1, 1))
+            + p.CH * (FDP_R(p.UM, I, 1) - FDP_R(p.UM, I, 0));
       } else {
         // strain_uw_xz.F90:198-206
-        exz = p.AH * (FDP_F(p.UM, I, L + 1) - FDP_F(p.UM, I, L - 2) + FDP_F(p.WM, I + 1, L) - FDP_F(p.WM, I - 2, L))
-            + p.BH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1) + FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
+        exz = p.AH * (FDP_R(p.UM, I, L + 1) - FDP_R(p.UM, I, L - 2) + FDP_R(p.WM, I + 1, L) - FDP_R(p.WM, I - 2, L))
+            + p.BH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1) + FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
       }
     } else {
       // strain_uw_xz.F90:209-223
-      const T DZXA = p.CH * (FDP_F(p.WM, I, L) - FDP_F(p.WM, I - 1, L));
+      const T DZXA = p.CH * (FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
       const int xi = (I - MX1) + L * (TPML + 2);
       const int mi = (I - MX) + L * (TPML + 1);
       const T mx = p.PZXH[mi];
-      exz = p.CH * (FDP_F(p.UM, I, L) - FDP_F(p.UM, I, L - 1)) + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
+      exz = p.CH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1)) + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
       p.PZXH[mi] = p.ODB2_XH[xi] * mx + p.ODC2_XH[xi] * DZXA;
     }
-    const int J = FDP_F(p.JM, I, L);
-    const T TXZv = FDP_C(C_MU, J) * exz;
+    const T TXZv = FDP_C(C_MU) * exz;
     FDP_F(p.TXZ, I, L) = FDP_F(p.TXZ, I, L) + p.DTE * TXZv;
   }
   if (last) return;  // hplane_pmlzh0_stress.F90 updates TXZ only
@@ -201,8 +236,8 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
   if (I < 2 - TPML || I > MX1 + TPML) return;
   T ezz, qzz;
   if (r0) {
-    ezz = (p.CH * (FDP_F(p.WM, I, 1) - FDP_F(p.WM, I, 0)));  // strain_uw_zz_0.F90:45-49
-    qzz = (p.CH * (FDP_F(p.QZ, I, 1) - FDP_F(p.QZ, I, 0)));  // strain_q_zz_0.F90:40-44
+    ezz = (p.CH * (FDP_R(p.WM, I, 1) - FDP_R(p.WM, I, 0)));  // strain_uw_zz_0.F90:45-49
+    qzz = (p.CH * (FDP_R(p.QZ, I, 1) - FDP_R(p.QZ, I, 0)));  // strain_q_zz_0.F90:40-44
   } else if (pml || mz1) {
     const int LL = mz1 ? 0 : L - p.MZ + 1;
     ezz = strain_zz_pml(p, p.WM, p.PZZH, I, L, LL);
@@ -213,10 +248,9 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
   }
   const T exx = strain_xx(p, p.UM, p.PXXL, p.PXXH, I, L);
   const T qxx = strain_xx(p, p.QX, p.OXXL, p.OXXH, I, L);
-  const int J = FDP_F(p.JM, I, L);
-  const T s1 = FDP_C(C_SXX1, J), s2 = FDP_C(C_SXX2, J), s3 = FDP_C(C_SXX3, J);
-  const T z1 = FDP_C(C_SZZ1, J), z2 = FDP_C(C_SZZ2, J), z3 = FDP_C(C_SZZ3, J);
-  const T q1 = FDP_C(C_P1, J), q2 = FDP_C(C_P2, J), q3 = FDP_C(C_P3, J);
+  const T s1 = FDP_C(C_SXX1), s2 = FDP_C(C_SXX2), s3 = FDP_C(C_SXX3);
+  const T z1 = FDP_C(C_SZZ1), z2 = FDP_C(C_SZZ2), z3 = FDP_C(C_SZZ3);
+  const T q1 = FDP_C(C_P1), q2 = FDP_C(C_P2), q3 = FDP_C(C_P3);
   const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
   const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
   const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
@@ -235,25 +269,29 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
   }
 }
 
-// One thread per column I, marching down the rows of one z-tile.
-template <class T, bool SI>
-__global__ void __launch_bounds__(128) k_stress(const __grid_constant__ Params<T> p, int it_off) {
-  const int I = p.PMLL + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (I > p.PMLXH) return;
-  const int t = blockIdx.y;
-  const int L0 = t * p.tz;
-  const int L1 = (t == p.ntz - 1) ? p.NZ : L0 + p.tz;
-  const int it = *p.it_base + it_off;
-  for (int L = (SI ? max(L0, 2) : L0); L < L1; ++L) stress_cell<T, SI>(p, I, L, it);
-  if (SI && t == 0) {
-    // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53, after rows 2..4
-    FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
-    FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
-    FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
-    FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
-    FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
-    FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
-    FDP_F(p.TXZ, I, 2) = T(0);
+// One thread per cell; blocks tile the grid from row 0 down, so the block
+// row holding rows 0..7 also holds rows 2..4 that the stress-imaging mirror
+// rows 0 and 1 copy.
+template <class T, bool SI, int MODE>
+__global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Params<T> p, int it_off) {
+  const int I = p.PMLL + (int)(blockIdx.x * kBX + threadIdx.x);
+  const int L = (int)(blockIdx.y * kBZ + threadIdx.y);
+  if (I <= p.PMLXH && L <= p.PMLZH && (!SI || L >= 2)) {
+    const int it = *p.it_base + it_off;
+    stress_cell<T, SI, MODE>(p, I, L, it);
+  }
+  if (SI && blockIdx.y == 0) {
+    __syncthreads();  // rows 2..4 of this block are final
+    if (I <= p.PMLXH && threadIdx.y == 0) {
+      // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53
+      FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
+      FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
+      FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
+      FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
+      FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
+      FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
+      FDP_F(p.TXZ, I, 2) = T(0);
+    }
   }
 }
 
@@ -264,17 +302,18 @@ __global__ void __launch_bounds__(128) k_stress(const __grid_constant__ Params<T
 // after its update over exactly the columns and rows where u and w read the
 // copy (sto_qxp.F90:24, sto_qzp.F90:24), so QXP(I,L) always equals the q of
 // the previous level at that cell.
-template <class T, bool SI>
+template <class T, bool SI, int MODE>
 __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) {
   const int TPML = p.TPML, MX = p.MX, MX1 = p.MX1;
+  const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
+  const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
   const bool pml = (L >= p.MZ - 1);
   const T A = p.A, B = p.B;
 
   // ---------------- qx and u: I = 3-TPML .. MX-1+TPML
   if (I >= 3 - TPML && I <= MX1 + TPML) {
-    const int J = FDP_F(p.JM, I, L);
-    const T E = FDP_C(C_EQX, J), Cu = FDP_C(C_CU, J);
-    const T R1 = FDP_C(C_R1QX, J), R2 = FDP_C(C_R2QX, J), R1u = FDP_C(C_R1U, J), R3u = FDP_C(C_R3U, J);
+    const T E = FDP_C(C_EQX), Cu = FDP_C(C_CU);
+    const T R1 = FDP_C(C_R1QX), R2 = FDP_C(C_R2QX), R1u = FDP_C(C_R1U), R3u = FDP_C(C_R3U);
     const T qx0 = FDP_F(p.QX, I, L);
     const T u0 = FDP_F(p.UM, I, L);
     T qx, u;
@@ -282,9 +321,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
       // inh_qx_int_2nd_pml.F90 / inh_v_u_int_2nd_pml.F90
       const int LL = L - p.MZ + 1;
       const int zi = (I - p.PMLL) + LL * p.NX;
-      const T DXXXA = FDP_F(p.TXX, I, L) - FDP_F(p.TXX, I - 1, L);
-      const T DXZZA = FDP_F(p.TXZ, I, L + 1) - FDP_F(p.TXZ, I, L);
-      const T PXXXA = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L);
+      const T DXXXA = FDP_R(p.TXX, I, L) - FDP_R(p.TXX, I - 1, L);
+      const T DXZZA = FDP_R(p.TXZ, I, L + 1) - FDP_R(p.TXZ, I, L);
+      const T PXXXA = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L);
       const T za = p.ODA_ZH[zi], zd = p.ODD_ZH[zi], zb = p.ODB_ZH[zi], zc = p.ODC_ZH[zi];
       const T gz = p.GXZH[zi], rz = p.RXZH[zi];
       if (I <= 3 || I >= MX1) {
@@ -309,7 +348,7 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         R[mi] = xb * r + xc * DXXXA;
         S[mi] = xb * s + xc * PXXXA;
       } else {
-        qx = E * qx0 - R1 * (za * (zd * DXZZA + gz) + DXXXA) - R2 * (FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L));
+        qx = E * qx0 - R1 * (za * (zd * DXZZA + gz) + DXXXA) - R2 * (FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L));
         u = u0 + Cu * qx0 + R1u * (DXXXA + za * (zd * DXZZA + rz)) + R3u * PXXXA;
       }
       p.GXZH[zi] = zb * gz + zc * DXZZA;
@@ -330,9 +369,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
           xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
           G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
         }
-        const T DXXXA = FDP_F(p.TXX, I, L) - FDP_F(p.TXX, I - 1, L);
-        const T PXXXA = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L);
-        const T txz1 = FDP_F(p.TXZ, I, L + 1), txz0 = FDP_F(p.TXZ, I, L);
+        const T DXXXA = FDP_R(p.TXX, I, L) - FDP_R(p.TXX, I - 1, L);
+        const T PXXXA = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L);
+        const T txz1 = FDP_R(p.TXZ, I, L + 1), txz0 = FDP_R(p.TXZ, I, L);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
         const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
         qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1 - txz0) - R2 * (xa * (xd * PXXXA + h));
@@ -343,9 +382,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         S[mi] = xb * s + xc * PXXXA;
       } else {
         // inh_qx_int.F90:40-54 / inh_v_uv_int.F90:41-56
-        const T X = A * (FDP_F(p.TXX, I + 1, L) - FDP_F(p.TXX, I - 2, L) + FDP_F(p.TXZ, I, L + 2) - FDP_F(p.TXZ, I, L - 1))
-                  + B * (FDP_F(p.TXX, I, L) - FDP_F(p.TXX, I - 1, L) + FDP_F(p.TXZ, I, L + 1) - FDP_F(p.TXZ, I, L));
-        const T P = A * (FDP_F(p.PRES, I + 1, L) - FDP_F(p.PRES, I - 2, L)) + B * (FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I - 1, L));
+        const T X = A * (FDP_R(p.TXX, I + 1, L) - FDP_R(p.TXX, I - 2, L) + FDP_R(p.TXZ, I, L + 2) - FDP_R(p.TXZ, I, L - 1))
+                  + B * (FDP_R(p.TXX, I, L) - FDP_R(p.TXX, I - 1, L) + FDP_R(p.TXZ, I, L + 1) - FDP_R(p.TXZ, I, L));
+        const T P = A * (FDP_R(p.PRES, I + 1, L) - FDP_R(p.PRES, I - 2, L)) + B * (FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L));
         qx = E * qx0 - R1 * X - R2 * P;
         u = u0 + Cu * qx0 + R1u * X + R3u * P;
       }
@@ -365,9 +404,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
           xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
           G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
         }
-        const T DXXXA = FDP_F(p.TXX, I, 0) - FDP_F(p.TXX, I - 1, 0);
-        const T PXXXA = FDP_F(p.PRES, I, 0) - FDP_F(p.PRES, I - 1, 0);
-        const T txz1 = FDP_F(p.TXZ, I, 1);
+        const T DXXXA = FDP_R(p.TXX, I, 0) - FDP_R(p.TXX, I - 1, 0);
+        const T PXXXA = FDP_R(p.PRES, I, 0) - FDP_R(p.PRES, I - 1, 0);
+        const T txz1 = FDP_R(p.TXZ, I, 1);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
         const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
         qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1) - R2 * (xa * (xd * PXXXA + h));
@@ -377,10 +416,10 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         R[mi] = xb * r + xc * DXXXA;
         S[mi] = xb * s + xc * PXXXA;
       } else {
-        const T X = A * (FDP_F(p.TXX, I + 1, 0) - FDP_F(p.TXX, I - 2, 0)) + B * (FDP_F(p.TXX, I, 0) - FDP_F(p.TXX, I - 1, 0))
-                  + T(17) / T(24) * FDP_F(p.TXZ, I, 1) + T(3) / T(8) * FDP_F(p.TXZ, I, 2)
-                  - T(5) / T(24) * FDP_F(p.TXZ, I, 3) + T(1) / T(24) * FDP_F(p.TXZ, I, 4);
-        const T P = A * (FDP_F(p.PRES, I + 1, 0) - FDP_F(p.PRES, I - 2, 0)) + B * (FDP_F(p.PRES, I, 0) - FDP_F(p.PRES, I - 1, 0));
+        const T X = A * (FDP_R(p.TXX, I + 1, 0) - FDP_R(p.TXX, I - 2, 0)) + B * (FDP_R(p.TXX, I, 0) - FDP_R(p.TXX, I - 1, 0))
+                  + T(17) / T(24) * FDP_R(p.TXZ, I, 1) + T(3) / T(8) * FDP_R(p.TXZ, I, 2)
+                  - T(5) / T(24) * FDP_R(p.TXZ, I, 3) + T(1) / T(24) * FDP_R(p.TXZ, I, 4);
+        const T P = A * (FDP_R(p.PRES, I + 1, 0) - FDP_R(p.PRES, I - 2, 0)) + B * (FDP_R(p.PRES, I, 0) - FDP_R(p.PRES, I - 1, 0));
         qx = E * qx0 - R1 * X - R2 * P;
         u = u0 + Cu * qx0 + R1u * X + R3u * P;
       }
@@ -391,9 +430,8 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
 
   // ---------------- qz and w: I = 2-TPML .. MX-1+TPML
   if (I >= 2 - TPML && I <= MX1 + TPML) {
-    const int J = FDP_F(p.JM, I, L);
-    const T E = FDP_C(C_EQZ, J), Cw = FDP_C(C_CW, J);
-    const T R1 = FDP_C(C_R1QZ, J), R2 = FDP_C(C_R2QZ, J), R1w = FDP_C(C_R1W, J), R3w = FDP_C(C_R3W, J);
+    const T E = FDP_C(C_EQZ), Cw = FDP_C(C_CW);
+    const T R1 = FDP_C(C_R1QZ), R2 = FDP_C(C_R2QZ), R1w = FDP_C(C_R1W), R3w = FDP_C(C_R3W);
     const T qz0 = FDP_F(p.QZ, I, L);
     const T w0 = FDP_F(p.WM, I, L);
     T qz, w;
@@ -401,9 +439,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
       // inh_qz_int_2nd_pml.F90 / inh_v_w_int_2nd_pml.F90
       const int LL = L - p.MZ + 1;
       const int zi = (I - p.PMLL) + LL * p.NX;
-      const T DXZXA = FDP_F(p.TXZ, I + 1, L) - FDP_F(p.TXZ, I, L);
-      const T DZZZA = FDP_F(p.TZZ, I, L) - FDP_F(p.TZZ, I, L - 1);
-      const T PZZZA = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I, L - 1);
+      const T DXZXA = FDP_R(p.TXZ, I + 1, L) - FDP_R(p.TXZ, I, L);
+      const T DZZZA = FDP_R(p.TZZ, I, L) - FDP_R(p.TZZ, I, L - 1);
+      const T PZZZA = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I, L - 1);
       const T za = p.ODA2_ZH[zi], zd = p.ODD2_ZH[zi], zb = p.ODB2_ZH[zi], zc = p.ODC2_ZH[zi];
       const T gz = p.GZZH[zi], hz = p.HZZH[zi], rz = p.RZZH[zi], sz = p.SZZH[zi];
       if (I <= 2 || I >= MX1) {
@@ -444,9 +482,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
           xi = (I - MX1) + L * (TPML + 1); mi = (I - (MX - 1)) + L * (TPML + 2);
           xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; R = p.RZXH;
         }
-        const T DXZXA = FDP_F(p.TXZ, I + 1, L) - FDP_F(p.TXZ, I, L);
-        const T dzz = FDP_F(p.TZZ, I, L) - FDP_F(p.TZZ, I, L - 1);
-        const T dp = FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I, L - 1);
+        const T DXZXA = FDP_R(p.TXZ, I + 1, L) - FDP_R(p.TXZ, I, L);
+        const T dzz = FDP_R(p.TZZ, I, L) - FDP_R(p.TZZ, I, L - 1);
+        const T dp = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I, L - 1);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
         const T g = G[mi], r = R[mi];
         qz = E * qz0 - R1 * (dzz + xa * (xd * DXZXA + g)) - R2 * dp;
@@ -455,18 +493,18 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         R[mi] = xb * r + xc * DXZXA;
       } else if (SI || L >= 2) {
         // inh_qz_int.F90:41-55 / inh_v_w_int.F90:43-58
-        const T X = A * (FDP_F(p.TZZ, I, L + 1) - FDP_F(p.TZZ, I, L - 2) + FDP_F(p.TXZ, I + 2, L) - FDP_F(p.TXZ, I - 1, L))
-                  + B * (FDP_F(p.TZZ, I, L) - FDP_F(p.TZZ, I, L - 1) + FDP_F(p.TXZ, I + 1, L) - FDP_F(p.TXZ, I, L));
-        const T P = A * (FDP_F(p.PRES, I, L + 1) - FDP_F(p.PRES, I, L - 2)) + B * (FDP_F(p.PRES, I, L) - FDP_F(p.PRES, I, L - 1));
+        const T X = A * (FDP_R(p.TZZ, I, L + 1) - FDP_R(p.TZZ, I, L - 2) + FDP_R(p.TXZ, I + 2, L) - FDP_R(p.TXZ, I - 1, L))
+                  + B * (FDP_R(p.TZZ, I, L) - FDP_R(p.TZZ, I, L - 1) + FDP_R(p.TXZ, I + 1, L) - FDP_R(p.TXZ, I, L));
+        const T P = A * (FDP_R(p.PRES, I, L + 1) - FDP_R(p.PRES, I, L - 2)) + B * (FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I, L - 1));
         qz = E * qz0 - R1 * X - R2 * P;
         w = w0 + Cw * qz0 + R1w * X + R3w * P;
       } else {
         // row 1 without stress imaging: inh_v_qz_int_1.F90 / inh_v_w_int_1.F90
-        const T X = A * (FDP_F(p.TXZ, I + 2, 1) - FDP_F(p.TXZ, I - 1, 1)) + B * (FDP_F(p.TXZ, I + 1, 1) - FDP_F(p.TXZ, I, 1))
-                  - T(31) / T(24) * FDP_F(p.TZZ, I, 0) + T(29) / T(24) * FDP_F(p.TZZ, I, 1)
-                  - T(3) / T(40) * FDP_F(p.TZZ, I, 2) + T(1) / T(168) * FDP_F(p.TZZ, I, 3);
-        const T P = -T(31) / T(24) * FDP_F(p.PRES, I, 0) + T(29) / T(24) * FDP_F(p.PRES, I, 1)
-                  - T(3) / T(40) * FDP_F(p.PRES, I, 2) + T(1) / T(168) * FDP_F(p.PRES, I, 3);
+        const T X = A * (FDP_R(p.TXZ, I + 2, 1) - FDP_R(p.TXZ, I - 1, 1)) + B * (FDP_R(p.TXZ, I + 1, 1) - FDP_R(p.TXZ, I, 1))
+                  - T(31) / T(24) * FDP_R(p.TZZ, I, 0) + T(29) / T(24) * FDP_R(p.TZZ, I, 1)
+                  - T(3) / T(40) * FDP_R(p.TZZ, I, 2) + T(1) / T(168) * FDP_R(p.TZZ, I, 3);
+        const T P = -T(31) / T(24) * FDP_R(p.PRES, I, 0) + T(29) / T(24) * FDP_R(p.PRES, I, 1)
+                  - T(3) / T(40) * FDP_R(p.PRES, I, 2) + T(1) / T(168) * FDP_R(p.PRES, I, 3);
         qz = E * qz0 - R1 * X - R2 * P;
         w = w0 + Cw * qz0 + R1w * X + R3w * P;
       }
@@ -475,13 +513,13 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
       // inh_qz_2nd_0.F90, inh_v_w_2nd_0.F90
       T X, P;
       if (I <= 2 || I >= MX1) {
-        X = T(3) * FDP_F(p.TZZ, I, 0) - T(1) / T(3) * FDP_F(p.TZZ, I, 1);
-        P = T(3) * FDP_F(p.PRES, I, 0) - T(1) / T(3) * FDP_F(p.PRES, I, 1);
+        X = T(3) * FDP_R(p.TZZ, I, 0) - T(1) / T(3) * FDP_R(p.TZZ, I, 1);
+        P = T(3) * FDP_R(p.PRES, I, 0) - T(1) / T(3) * FDP_R(p.PRES, I, 1);
       } else {
-        X = T(35) / T(8) * FDP_F(p.TZZ, I, 0) - T(35) / T(24) * FDP_F(p.TZZ, I, 1)
-          + T(21) / T(40) * FDP_F(p.TZZ, I, 2) - T(5) / T(56) * FDP_F(p.TZZ, I, 3);
-        P = T(35) / T(8) * FDP_F(p.PRES, I, 0) - T(35) / T(24) * FDP_F(p.PRES, I, 1)
-          + T(21) / T(40) * FDP_F(p.PRES, I, 2) - T(5) / T(56) * FDP_F(p.PRES, I, 3);
+        X = T(35) / T(8) * FDP_R(p.TZZ, I, 0) - T(35) / T(24) * FDP_R(p.TZZ, I, 1)
+          + T(21) / T(40) * FDP_R(p.TZZ, I, 2) - T(5) / T(56) * FDP_R(p.TZZ, I, 3);
+        P = T(35) / T(8) * FDP_R(p.PRES, I, 0) - T(35) / T(24) * FDP_R(p.PRES, I, 1)
+          + T(21) / T(40) * FDP_R(p.PRES, I, 2) - T(5) / T(56) * FDP_R(p.PRES, I, 3);
       }
       qz = E * qz0 - R1 * X - R2 * P;
       w = w0 + Cw * qz0 + R1w * X + R3w * P;
@@ -491,48 +529,53 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
   }
 }
 
-// One thread per column I, marching down the rows of one z-tile.  The last
-// tile holds at least the rows PMLZH-2..PMLZH, so the bottom row's inputs
-// (the new rows PMLZH-1 and PMLZH-2, and their values before this phase)
-// are all produced by the same thread.
-template <class T, bool SI>
-__global__ void __launch_bounds__(128) k_velocity(const __grid_constant__ Params<T> p, int it_off) {
+// One thread per cell; blocks tile the grid from row PMLZH up, so the block
+// row holding the bottom row also holds rows PMLZH-1 and PMLZH-2, whose new
+// values and pre-phase values (the history SZ of time_loop.F90:133-155) the
+// bottom row needs.
+template <class T, bool SI, int MODE>
+__global__ void __launch_bounds__(kBX * kBZ) k_velocity(const __grid_constant__ Params<T> p, int it_off) {
   (void)it_off;
-  const int I = p.PMLL + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  if (I > p.PMLXH) return;
-  const int t = blockIdx.y;
-  const int L0 = t * p.tz;
-  const bool lastTile = (t == p.ntz - 1);
-  const int L1 = lastTile ? p.NZ : L0 + p.tz;
-  const int Lstop = lastTile ? p.PMLZH : L1;
-  T h[3][4];  // old rows PMLZH (k=0), PMLZH-1 (k=1), PMLZH-2 (k=2) for u, w, qx, qz
-  for (int L = (SI ? max(L0, 2) : L0); L < Lstop; ++L) {
-    if (lastTile && L >= p.PMLZH - 2) {
-      const int k = p.PMLZH - L;
-      h[k][0] = FDP_F(p.UM, I, L); h[k][1] = FDP_F(p.WM, I, L);
-      h[k][2] = FDP_F(p.QX, I, L); h[k][3] = FDP_F(p.QZ, I, L);
-    }
-    velocity_cell<T, SI>(p, I, L);
+  __shared__ T old[3][4][kBX];  // pre-phase values of rows PMLZH-k, k = 0..2
+  const int I = p.PMLL + (int)(blockIdx.x * kBX + threadIdx.x);
+  const int L = p.PMLZH - (int)(blockIdx.y * kBZ + (kBZ - 1 - threadIdx.y));
+  const bool inx = I <= p.PMLXH;
+  const bool bottom = (blockIdx.y == 0);
+  const int tx = threadIdx.x;
+  if (bottom && inx && L >= p.PMLZH - 2) {
+    const int k = p.PMLZH - L;
+    old[k][0][tx] = FDP_F(p.UM, I, L); old[k][1][tx] = FDP_F(p.WM, I, L);
+    old[k][2][tx] = FDP_F(p.QX, I, L); old[k][3][tx] = FDP_F(p.QZ, I, L);
   }
-  if (lastTile) {
-    // time_loop.F90:133-155 and hplane_pmlzh0_velocity.F90:34-63
-    const int LST = p.PMLZH;
-    h[0][0] = FDP_F(p.UM, I, LST); h[0][1] = FDP_F(p.WM, I, LST);
-    h[0][2] = FDP_F(p.QX, I, LST); h[0][3] = FDP_F(p.QZ, I, LST);
-    T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+  if (inx && L >= (SI ? 2 : 0) && L < p.PMLZH) velocity_cell<T, SI, MODE>(p, I, L);
+  if (bottom) {
+    const bool me = inx && L == p.PMLZH;
     const int x = I - p.PMLL;
+    T sp[4][3];
+    if (me) {
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
-      T* hist = p.HIST + (long long)c * 3 * p.NX;
-      const T sp0 = hist[x], sp1 = hist[p.NX + x], sp2 = hist[2 * p.NX + x];
-      const T v = ab[0] * FDP_F(f[c], I, LST - 1) + ab[1] * FDP_F(f[c], I, LST - 2)
-                + ab[2] * h[0][c] + ab[3] * h[1][c] + ab[4] * h[2][c]
-                + ab[5] * sp0 + ab[6] * sp1 + ab[7] * sp2;
-      FDP_F(f[c], I, LST) = v;
-      hist[x] = h[0][c];
-      hist[p.NX + x] = h[1][c];
-      hist[2 * p.NX + x] = h[2][c];
+      for (int c = 0; c < 4; ++c) {
+        const T* hist = p.HIST + (long long)c * 3 * p.NX;
+        sp[c][0] = hist[x]; sp[c][1] = hist[p.NX + x]; sp[c][2] = hist[2 * p.NX + x];
+      }
+    }
+    __syncthreads();  // rows PMLZH-1, PMLZH-2 of this block are final
+    if (me) {
+      // hplane_pmlzh0_velocity.F90:34-63
+      const int LST = p.PMLZH;
+      T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
+        T* hist = p.HIST + (long long)c * 3 * p.NX;
+        const T v = ab[0] * FDP_F(f[c], I, LST - 1) + ab[1] * FDP_F(f[c], I, LST - 2)
+                  + ab[2] * old[0][c][tx] + ab[3] * old[1][c][tx] + ab[4] * old[2][c][tx]
+                  + ab[5] * sp[c][0] + ab[6] * sp[c][1] + ab[7] * sp[c][2];
+        FDP_F(f[c], I, LST) = v;
+        hist[x] = old[0][c][tx];
+        hist[p.NX + x] = old[1][c][tx];
+        hist[2 * p.NX + x] = old[2][c][tx];
+      }
     }
   }
 }
@@ -549,10 +592,10 @@ __device__ __forceinline__ T si_row1(const Params<T>& p, int c, int I) {
   if (c == 0) return (I >= 3 - TPML && I <= MX - 1 + TPML) ? u1(I) : FDP_F(p.UM, I, 1);
   if (c == 2) return (I >= 3 - TPML && I <= MX - 1 + TPML) ? q1(I) : FDP_F(p.QX, I, 1);
   if (I < 3 - TPML || I > MX - 2 + TPML) return c == 1 ? FDP_F(p.WM, I, 1) : FDP_F(p.QZ, I, 1);
-  const int J = FDP_F(p.JM, I, 0);
   const T du = u1(I + 1) - u1(I) + FDP_F(p.UM, I + 1, 2) - FDP_F(p.UM, I, 2);
-  if (c == 1) return FDP_F(p.WM, I, 3) + FDP_C(C_AUXW, J) * du;
-  return FDP_F(p.QZ, I, 3) + FDP_C(C_AUXQZ, J) * du + (q1(I + 1) - q1(I) + FDP_F(p.QX, I + 1, 2) - FDP_F(p.QX, I, 2));
+  const int x = I - p.PMLL;  // AUX holds AUXIL_W/AUXIL_QZ of material JM(I,0)
+  if (c == 1) return FDP_F(p.WM, I, 3) + p.AUX[x] * du;
+  return FDP_F(p.QZ, I, 3) + p.AUX[p.NX + x] * du + (q1(I + 1) - q1(I) + FDP_F(p.QX, I + 1, 2) - FDP_F(p.QX, I, 2));
 }
 
 template <class T, bool SI>
@@ -600,6 +643,7 @@ __global__ void k_set_base(int* base, int v) { *base = v; }
 __global__ void k_add_base(int* base, int v) { *base += v; }
 
 #undef FDP_F
+#undef FDP_R
 #undef FDP_C
 
 }  // namespace fdp

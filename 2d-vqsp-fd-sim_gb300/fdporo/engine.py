@@ -124,6 +124,19 @@ class Engine:
     def kernel_launches(self) -> int:
         return int(self.lib.fdp_kernel_launches(self._ctx))
 
+    def stream(self) -> int:
+        """The engine's cudaStream_t as an integer handle."""
+        s = C.c_void_p()
+        self._check(self.lib.fdp_get_stream(self._ctx, C.byref(s)))
+        return int(s.value or 0)
+
+    def profile(self, it_begin: int, it_end: int) -> dict:
+        """Per-kernel device time (ms) and launch counts over levels it_begin..it_end."""
+        ms = (C.c_double * 3)()
+        n = (C.c_int64 * 3)()
+        self._check(self.lib.fdp_profile_run(self._ctx, it_begin, it_end, ms, n))
+        return {k: (ms[i], n[i]) for i, k in enumerate(("stress", "velocity", "edge"))}
+
     # -- state ----------------------------------------------------------------
     def bounds(self, name: str) -> tuple[int, int, int, int]:
         b = np.zeros(4, dtype=np.int32)

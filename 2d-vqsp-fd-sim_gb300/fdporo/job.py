@@ -160,7 +160,7 @@ def prepare(cfg: JobConfig, medium: Medium, precision: str = "f32") -> Inputs:
     if rc:
         raise FdpError(rc, "fdp_prep_expand_jm")
     # READ_MODEL_PAR: the .MO values are read in precision PP, then scaled
-    table = np.ascontiguousarray(medium.table, dtype=dt_)
+    table = np.array(medium.table, dtype=dt_, order="C", copy=True)  # scaled in place below
     rc = lib.fdp_prep_scale_table(prec, table.shape[0], dt, h, table.ctypes.data_as(C.c_void_p))
     if rc:
         raise FdpError(rc, "fdp_prep_scale_table")

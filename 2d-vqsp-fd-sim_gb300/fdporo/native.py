@@ -71,6 +71,8 @@ SIGNATURES = {
     "fdp_set_field": (C.c_int, [_VP, _I32, _VP]),
     "fdp_synchronize": (C.c_int, [_VP]),
     "fdp_kernel_launches": (C.c_int64, [_VP]),
+    "fdp_get_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "fdp_profile_run": (C.c_int, [_VP, _I32, _I32, _PD, C.POINTER(C.c_int64)]),
     "fdp_last_error": (C.c_char_p, [_VP]),
     "fdp_destroy": (None, [_VP]),
     "fdp_prep_velocities": (C.c_int, [_I32, _D, _D, _D, _D, _D, _D, _D, _PD, _PD, _PD]),

@@ -1,0 +1,330 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 time-stepping engine on the layered 2048x2048 case.
+
+Workload ("layered-grf-2048"): MX = MZ = 2048 with a 20-cell PML
+(2088 x 2071 = 4,324,248 cells counting the PML), dx = 1 m, dt = 1e-4 s,
+a sandstone half-space over a tight layer at 1024 m, both perturbed by a
+10 % Gaussian random field (correlation 20 m), one material per cell,
+free surface by stress imaging, 20 Hz Ricker explosive source at 10 m,
+512 receivers on row 2; FP32.  Seeded synthetic inputs stand in for the
+reference's own model files, which its repository does not contain.
+
+A "step" is one time level of the whole grid (both half-steps, all
+boundary rows, receiver sampling).  The metric is cell-updates per second
+counting the PML cells.  The fields and per-cell media (~0.6 GB) are larger
+than L2, so no flush is needed between timed levels.
+
+Arms:
+  default            the CUDA engine (value, e2e through the C ABI, roofline
+                     of the dominant kernel, CPU baseline on a sample)
+  --impl reference   the CPU restatement of the reference's time loop
+                     (OpenMP over rows, all host threads), same workload
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "2d-vqsp-fd-sim_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = dict(mx=2048, mz=2048, tpml=20, h=1.0, dt=1e-4, mt2=4000, f0=20.0, n_rec=512, seed=20250)
+METRIC = "Gcell-updates/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier_max(value: float, ws: int) -> float:
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(ws: int) -> None:
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def prepare_inputs(precision: str, mt2: int):
+    from fdporo import job
+    w = WORKLOAD
+    cfg, med = job.layered(mx=w["mx"], mz=w["mz"], nsteps=mt2, tpml=w["tpml"], f0=w["f0"], dt=w["dt"], h=w["h"],
+                           n_rec=w["n_rec"], seed=w["seed"], layer_depth=1024.0)
+    return job.prepare(cfg, med, precision)
+
+
+def algorithmic_bytes(inp, s: int) -> dict:
+    """Compulsory DRAM bytes per launch of each kernel for this workload:
+    every wavefield value the kernel reads or read-modify-writes, the JM
+    index and the material coefficients of each cell, and every PML memory
+    variable it updates (read + write).  Damping profiles are one-dimensional
+    and cache-resident and are not counted."""
+    nx, nz, tp = inp.nx, inp.nz, inp.tpml
+    cells = nx * nz
+    # element counts of the memory variables (ppml.F90:85-112)
+    side = lambda w: w * nz
+    bottom = lambda h: nx * h
+    stress_mem = (side(tp + 2) + side(tp + 1) + 2 * side(tp + 1) + 2 * side(tp + 1)
+                  + bottom(tp + 2) + 2 * bottom(tp + 1))
+    vel_mem = (4 * side(tp + 3) + 4 * side(tp + 2) + 2 * side(tp + 2) + 2 * side(tp + 2) + 6 * bottom(tp + 1))
+    stress = cells * (4 * s + 8 * s + 4 + 10 * s) + 2 * s * stress_mem
+    velocity = cells * (4 * s + 8 * s + 4 + 12 * s) + 2 * s * vel_mem + 2 * s * 12 * nx
+    return {"stress": stress, "velocity": velocity, "per_cell_stress": stress / cells,
+            "per_cell_velocity": velocity / cells}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if parts[4 + k].lower().startswith("active"):
+                    reasons.add(n)
+        busy = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_gbs() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str) -> float | None:
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return float(d[kernel]["dram_bytes_per_launch_full_size"])
+    except Exception:
+        return None
+
+
+def cpu_time_levels(inp, levels: int, warmup: int, threads: int) -> float:
+    """Seconds for ``levels`` time levels of the oracle (after ``warmup``)."""
+    from oracle.oracle import make_oracle
+    o = make_oracle(inp, threads=threads)
+    if warmup:
+        o.time_loop(1, warmup)
+    t = time.perf_counter()
+    o.time_loop(warmup + 1, warmup + levels)
+    el = time.perf_counter() - t
+    o.close()
+    return el
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    inp = prepare_inputs(args.precision, max(WORKLOAD["mt2"], args.warmup + args.steps))
+    el = cpu_time_levels(inp, args.steps, args.warmup, threads)
+    value = inp.cells * args.steps / el / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "f32" else "f64",
+        "data": "synthetic (seeded layered medium with Gaussian random field)",
+        "config": {"workload": "layered-grf-2048", "cells": inp.cells, "mx": WORKLOAD["mx"], "mz": WORKLOAD["mz"],
+                   "tpml": WORKLOAD["tpml"], "levels_per_shot": WORKLOAD["mt2"], "media": "per-cell"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full-grid time levels after {args.warmup} warm-up levels "
+                                   "(C++ restatement of the reference time loop, OpenMP over rows)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local if torch.cuda.is_available() else 0
+    torch.cuda.set_device(dev)
+    from fdporo import job
+
+    prof_levels = 50
+    mt2 = max(WORKLOAD["mt2"], args.warmup + args.steps + prof_levels)
+    inp = prepare_inputs(args.precision, mt2)
+    s = 8 if args.precision == "f64" else 4
+    eng = job.make_engine(inp, device=dev)
+    ext = torch.cuda.ExternalStream(eng.stream(), device=dev)
+
+    # ---- warm-up
+    eng.time_loop(1, args.warmup)
+    eng.synchronize()
+    # ---- timed region
+    n0 = eng.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        _barrier(ws)
+        torch.cuda.synchronize()
+        e0.record(ext)
+        eng.time_loop(args.warmup + 1, args.warmup + args.steps)
+        e1.record(ext)
+        e1.synchronize()
+        torch.cuda.synchronize()
+    launches = eng.kernel_launches() - n0
+    ms = e0.elapsed_time(e1)
+    ms_max = _barrier_max(ms, ws)
+    value = inp.cells * args.steps * ws / (ms_max / 1e3) / 1e9
+
+    # ---- per-kernel device time (separate launches between events)
+    lo = args.warmup + args.steps + 1
+    prof = eng.profile(lo, lo + prof_levels - 1)
+    alg = algorithmic_bytes(inp, s)
+    kern = max(("stress", "velocity"), key=lambda k: prof[k][0])
+    avg_ms = prof[kern][0] / prof[kern][1]
+    peak, peak_kind = measured_peak_gbs()
+    achieved = alg[kern] / (avg_ms / 1e3) / 1e9
+    shares = {k: prof[k][0] / sum(v[0] for v in prof.values()) for k in prof}
+    eng.close()
+
+    # ---- end to end through the C ABI: one whole shot (create, upload, run, download)
+    e2e = None
+    if not args.no_e2e:
+        from fdporo.engine import Engine
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e = Engine(inp.mx, inp.mz, inp.tpml, inp.lin_x, inp.lin_z, inp.h, inp.dt, precision=args.precision,
+                   stress_imaging=inp.stress_imaging, device=dev)
+        job.load_inputs(e, inp)
+        e.time_loop(1, WORKLOAD["mt2"])
+        rec = e.receivers(1, WORKLOAD["mt2"])
+        el = time.perf_counter() - t
+        e.close()
+        h2d = (inp.jm.nbytes + inp.table.nbytes + sum(p.nbytes for p in inp.profiles) + inp.ab.nbytes
+               + inp.sourtf[: WORKLOAD["mt2"]].nbytes + 16 * len(inp.irecx))
+        e2e = {"value": inp.cells * WORKLOAD["mt2"] * ws / _barrier_max(el, ws) / 1e9, "unit": METRIC,
+               "h2d_bytes_per_step": h2d // WORKLOAD["mt2"], "d2h_bytes_per_step": rec.nbytes // WORKLOAD["mt2"],
+               "shot_seconds": el, "shots_per_hour": 3600.0 / el,
+               "scope": f"one whole shot of {WORKLOAD['mt2']} levels: fdp_create, fdp_set_* from host buffers, "
+                        "fdp_run, fdp_get_receivers"}
+
+    # ---- CPU baseline on a bounded sample (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        t1 = cpu_time_levels(inp, 2, 0, threads)
+        lv = int(max(2, min(200, args.cpu_seconds / max(t1 / 2, 1e-6))))
+        el = cpu_time_levels(inp, lv, 0, threads)
+        cpu = {"value": inp.cells * lv / el / 1e9, "unit": METRIC, "cores": threads, "kind": "port",
+               "sample": f"{lv} full-grid time levels from rest ({el:.1f} s; C++ restatement of the reference "
+                         "time loop, OpenMP over rows)"}
+
+    if rank != 0:
+        return
+    step_s = ms_max / 1e3 / args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if args.precision == "f32" else "f64",
+        "data": "synthetic (seeded layered medium with Gaussian random field)",
+        "config": {"workload": "layered-grf-2048", "cells": inp.cells, "mx": WORKLOAD["mx"], "mz": WORKLOAD["mz"],
+                   "tpml": WORKLOAD["tpml"], "media": "per-cell", "levels_per_shot": WORKLOAD["mt2"],
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"shot replicas x{ws}",
+                   "shots_per_hour_device": 3600.0 / (step_s * WORKLOAD["mt2"])},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": ncu_traffic(kern),
+                     "alg_bytes_per_launch": alg[kern], "avg_launch_ms": avg_ms,
+                     "kernel_share": shares},
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

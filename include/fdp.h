@@ -156,6 +156,17 @@ int fdp_set_field(fdp_ctx* ctx, int32_t id, const void* host);
 /* Waits for all work of the context. */
 int fdp_synchronize(fdp_ctx* ctx);
 
+/* The context's CUDA stream (a cudaStream_t), so a caller can order its own
+ * work, or record its own events, after the engine's. */
+int fdp_get_stream(fdp_ctx* ctx, void** stream);
+
+/* Diagnostics: advances levels it_begin..it_end like fdp_run but launches
+ * each kernel separately between CUDA events, waits, and returns the summed
+ * device time in milliseconds of each kernel kind in ms_out[0..2] =
+ * {stress, velocity, edge} and the number of launches of each in
+ * launches_out[0..2]. */
+int fdp_profile_run(fdp_ctx* ctx, int32_t it_begin, int32_t it_end, double* ms_out, int64_t* launches_out);
+
 /* Number of CUDA kernel launches this context has enqueued since creation
  * (graph-launched kernels counted individually). */
 int64_t fdp_kernel_launches(fdp_ctx* ctx);

@@ -1,0 +1,98 @@
+"""Checks of the CPU oracle itself (no GPU): it runs the reference's time
+loop with bounds checking on every array index, and its results obey the
+physics and the algebra the scheme must satisfy."""
+import numpy as np
+import pytest
+
+from fdporo import job, media
+from fdporo.native import HISTORY, MEMORY_VARS, WAVEFIELD
+from oracle.oracle import make_oracle
+
+from helpers import small_job
+
+
+def _run(cfg, med, prec, n):
+    inp = job.prepare(cfg, med, prec)
+    o = make_oracle(inp)
+    o.time_loop(1, n)
+    return inp, o
+
+
+@pytest.mark.parametrize("si", [True, False])
+def test_zero_source_gives_zero_fields(si):
+    cfg, med = small_job(si=si, nsteps=30)
+    cfg.stf_value = np.zeros_like(cfg.stf_value)
+    _, o = _run(cfg, med, "f64", 30)
+    for n in WAVEFIELD + MEMORY_VARS + HISTORY:
+        assert not np.any(o.field(n)), n
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("si", [True, False])
+def test_linearity_is_exact_under_power_of_two_scaling(prec, si):
+    # every operation of the scheme is linear in the wavefield, and scaling
+    # by 4 commutes with IEEE rounding, so the fields scale bit for bit --
+    # except where the unscaled run underflowed into subnormal numbers
+    cfg, med = small_job(si=si, nsteps=40, seed=4)
+    _, a = _run(cfg, med, prec, 40)
+    cfg.stf_value = cfg.stf_value * 4.0
+    _, b = _run(cfg, med, prec, 40)
+    # values built from subnormal intermediates stay within a few ulps of tiny
+    tiny = 2.0 ** 24 * np.finfo(np.float32 if prec == "f32" else np.float64).tiny
+    for n in WAVEFIELD + MEMORY_VARS:
+        x, y = a.field(n), b.field(n)
+        normal = np.abs(x) > tiny
+        np.testing.assert_array_equal(y[normal], 4 * x[normal], err_msg=n)
+        np.testing.assert_allclose(y, 4 * x, rtol=0, atol=8 * tiny, err_msg=n)
+    np.testing.assert_allclose(b.receivers(1, 40), 4 * a.receivers(1, 40), rtol=0, atol=8 * tiny)
+
+
+def test_single_precision_tracks_double():
+    cfg, med = job.small_homogeneous(mx=80, mz=60, nsteps=300, tpml=10, f0=150.0, n_rec=11)
+    _, a = _run(cfg, med, "f64", 300)
+    _, b = _run(cfg, med, "f32", 300)
+    ra, rb = a.receivers(1, 300)[..., [0, 1, 8]], b.receivers(1, 300)[..., [0, 1, 8]].astype(np.float64)
+    rel = np.linalg.norm(rb - ra) / np.linalg.norm(ra)
+    assert rel < 1e-4, rel
+
+
+def test_fast_p_arrival_time():
+    # pressure at a receiver 40 m from the source first moves near t = 40 m / vpf
+    cfg, med = job.small_homogeneous(mx=120, mz=120, nsteps=420, tpml=10, f0=200.0, n_rec=1)
+    x0 = cfg.x_source
+    cfg.irecx = np.array([int(x0) + 40]); cfg.irecz = cfg.irecx.copy()
+    cfg.lrecx = np.array([int(cfg.z_source) + 2]); cfg.lrecz = cfg.lrecx.copy()
+    cfg.stf_value = job.ricker(cfg.stf_time, 200.0, t0=0.0)   # zero-phase, centred on t = 0
+    inp, o = _run(cfg, med, "f64", 420)
+    p = o.receivers(1, 420)[:, 0, 8]
+    t = np.arange(1, 421) * cfg.dt
+    t_peak = t[np.argmax(np.abs(p))]
+    from oracle.setup_ref import COL, calcul_velocity
+    r = media.rock_table(media.SANDSTONE)
+    vpf = calcul_velocity(r[COL["SXX1"]], -r[COL["P1"]], -r[COL["P3"]], r[COL["MU"]], r[COL["R1U"]], r[COL["R2QX"]],
+                          r[COL["R3U"]], np.float64)[0]
+    assert abs(t_peak - 40.0 / vpf) < 1.5e-3, (t_peak, 40.0 / vpf)
+
+
+def test_pml_absorbs_the_outgoing_wave():
+    cfg, med = job.small_homogeneous(mx=80, mz=80, nsteps=1200, tpml=20, f0=300.0, n_rec=1)
+    inp = job.prepare(cfg, med, "f64")
+    o = make_oracle(inp)
+    energy = []
+    for k in range(0, 1200, 100):
+        o.time_loop(k + 1, k + 100)
+        u, w = o.field("UM"), o.field("WM")
+        energy.append(float(np.sum(u * u + w * w)))
+    peak = max(energy)
+    assert energy[-1] < 0.05 * peak, (energy[-1] / peak)
+
+
+def test_bounds_checked_build_catches_bad_jm():
+    cfg, med = small_job(nsteps=5)
+    inp = job.prepare(cfg, med, "f32")
+    bad = inp.jm.copy()
+    bad[3, 3] = inp.table.shape[0] + 1
+    from oracle.oracle import Oracle
+    o = Oracle(inp.mx, inp.mz, inp.tpml, inp.lin_x, inp.lin_z, inp.h, inp.dt)
+    with pytest.raises(RuntimeError):
+        o.set_medium(bad, inp.table)
