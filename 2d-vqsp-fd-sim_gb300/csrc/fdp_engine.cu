@@ -5,9 +5,12 @@
 // history, the source time function and the receiver samples.  fdp_run
 // enqueues three kernels per time level on the context's stream; runs of
 // kChunk levels are captured once into a CUDA graph and replayed.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 #include <cmath>
 #include <cstdarg>
@@ -17,7 +20,7 @@
 #include <vector>
 
 #include "fdp.h"
-#include "fdp_kernels.cuh"
+#include "fdp_stencil.cuh"
 
 using fdp::Params;
 using fdp::kPadX;
@@ -51,7 +54,12 @@ struct fdp_ctx {
   std::string err;
   // device memory
   DevArr fields[8];
-  DevArr jm, coef, planes, aux, prof[24], mem[27], ab, hist, stf, rec, raw, itbase;
+  DevArr jm, coef, planes, aux, prof[24], mem[27], ab, hist, stf, rec, raw, itbase, errbuf;
+  // TMA descriptors of the input fields of each phase; use_tma selects the
+  // TMA-staged kernels (FDP_KERNEL_VARIANT=tma; the global-load kernels are
+  // the default)
+  fdp::TmaMaps tma_vel{}, tma_str{};
+  bool use_tma = false;
   int jmnum = 0;
   int mt2 = 0;
   int mr = 0, rec_flags = 0;
@@ -139,6 +147,41 @@ int copy2d_sync(fdp_ctx* c, void* dst, size_t dpitch, const void* src, size_t sp
 
 size_t count_of(const int b[4]) { return (size_t)(b[1] - b[0] + 1) * (size_t)(b[3] - b[2] + 1); }
 
+// TMA descriptor of one padded field (whole allocation, kSX x kSZ boxes).
+// cuTensorMapEncodeTiled is reached through the runtime's driver entry
+// point, so the library does not link libcuda itself.
+int make_field_map(fdp_ctx* c, CUtensorMap* map, void* base) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+      return fail(c, FDP_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)c->pitch, (cuuint64_t)c->rows_alloc};
+  const cuuint64_t strides[1] = {(cuuint64_t)c->pitch * (cuuint64_t)c->prec};
+  const cuuint32_t box[2] = {(cuuint32_t)fdp::kSX, (cuuint32_t)fdp::kSZ};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(map, c->prec == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                            base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(c, FDP_ERR_CUDA, "cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+  return FDP_OK;
+}
+
+// Waits for the context's work and reports a kernel whose bounded wait
+// expired (the status word the kernels set instead of hanging).
+int device_status(fdp_ctx* c) {
+  CK(c, cudaStreamSynchronize(c->stream));
+  int v = 0;
+  CK(c, cudaMemcpyAsync(&v, c->errbuf.p, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (v) return fail(c, FDP_ERR_DEVICE, "a kernel gave up waiting for its tile copy (status %d)", v);
+  return FDP_OK;
+}
+
 template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   std::memset(&p, 0, sizeof p);
   p.MX = c->MX; p.MZ = c->MZ; p.TPML = c->TPML; p.PMLL = c->PMLL; p.PMLXH = c->PMLXH; p.PMLZH = c->PMLZH;
@@ -183,6 +226,7 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   p.MR = c->mr;
   p.REC = (const int*)c->rec.p;
   p.RAW = (T*)c->raw.p;
+  p.err = (int*)c->errbuf.p;
 }
 
 dim3 cell_grid(const fdp_ctx* c) {
@@ -192,9 +236,16 @@ dim3 cell_grid(const fdp_ctx* c) {
 int edge_threads(const fdp_ctx* c) { return std::max(c->g.stress_imaging ? c->NX : 0, c->mr); }
 
 // kind 0 = stress phase, 1 = velocity phase, 2 = edge (imaging row 1 and receivers)
+dim3 tile_grid(const fdp_ctx* c) {
+  return dim3((c->NX + fdp::kTX - 1) / fdp::kTX, (c->NZ + fdp::kTZ - 1) / fdp::kTZ, 1);
+}
+
 template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
   const dim3 blk(fdp::kBX, fdp::kBZ, 1);
-  if (kind == 0) fdp::k_stress<T, SI, MODE><<<cell_grid(c), blk, 0, c->stream>>>(p, it_off);
+  const dim3 tblk(fdp::kTX, 4, 1);
+  if (kind == 0 && c->use_tma) fdp::k_stress_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_vel, it_off);
+  else if (kind == 1 && c->use_tma) fdp::k_velocity_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_str, it_off);
+  else if (kind == 0) fdp::k_stress<T, SI, MODE><<<cell_grid(c), blk, 0, c->stream>>>(p, it_off);
   else if (kind == 1) fdp::k_velocity<T, SI, MODE><<<cell_grid(c), blk, 0, c->stream>>>(p, it_off);
   else fdp::k_edge<T, SI><<<(edge_threads(c) + kBlockX - 1) / kBlockX, kBlockX, 0, c->stream>>>(p, it_off);
   c->launches += 1;
@@ -429,6 +480,15 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   if ((rc = dev_alloc(c, c->ab, 16 * es)) != FDP_OK) return bail(rc);
   if ((rc = dev_alloc(c, c->hist, (size_t)12 * c->NX * es)) != FDP_OK) return bail(rc);
   if ((rc = dev_alloc(c, c->itbase, sizeof(int))) != FDP_OK) return bail(rc);
+  if ((rc = dev_alloc(c, c->errbuf, sizeof(int))) != FDP_OK) return bail(rc);
+  const char* variant = std::getenv("FDP_KERNEL_VARIANT");
+  c->use_tma = variant && std::strcmp(variant, "tma") == 0;
+  if (c->use_tma) {
+    for (int k = 0; k < 4; ++k) {
+      if ((rc = make_field_map(c, &c->tma_vel.m[k], c->fields[k].p)) != FDP_OK) return bail(rc);
+      if ((rc = make_field_map(c, &c->tma_str.m[k], c->fields[4 + k].p)) != FDP_OK) return bail(rc);
+    }
+  }
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) { c->err = std::string("init: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
   *out = c;
@@ -542,7 +602,7 @@ int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host
   if (!c || (!host && n_levels > 0)) return fail(c, FDP_ERR_ARG, "null argument");
   if (n_levels <= 0 || c->mr == 0) return FDP_OK;
   if (it_first < 1 || it_first + n_levels - 1 > c->mt2) return fail(c, FDP_ERR_ARG, "levels outside 1..MT2");
-  CK(c, cudaStreamSynchronize(c->stream));
+  if (int rc = device_status(c)) return rc;
   const int mr = c->mr;
   const int lo = it_first - 1;  // also fetch the previous level for the time derivative
   const int first_fetch = std::max(lo, 1);
@@ -596,7 +656,7 @@ static int field_copy(fdp_ctx* c, int32_t id, void* host, bool set) {
   int b[4];
   if (!bounds_of(c, id, b)) return fail(c, FDP_ERR_ARG, "unknown field id %d", id);
   if (id == FDP_QXP || id == FDP_QZP) return fail(c, FDP_ERR_UNSUPPORTED, "QXP/QZP are not stored by this engine");
-  CK(c, cudaStreamSynchronize(c->stream));
+  if (int rc = device_status(c)) return rc;
   const size_t es = (size_t)c->prec;
   if (id <= FDP_PRES) {
     char* dev = (char*)c->fields[id].p + ((size_t)kPadZ * c->pitch + kPadX) * es;
@@ -633,11 +693,26 @@ int fdp_get_snapshot(fdp_ctx* c, int32_t mask, void* host) {
 
 int fdp_synchronize(fdp_ctx* c) {
   if (!c) return fail(c, FDP_ERR_ARG, "null context");
-  CK(c, cudaStreamSynchronize(c->stream));
-  return FDP_OK;
+  return device_status(c);
 }
 
 int64_t fdp_kernel_launches(fdp_ctx* c) { return c ? c->launches : 0; }
+
+int fdp_medium_info(fdp_ctx* c, int32_t* mode, int32_t* planes_stress, int32_t* planes_velocity) {
+  if (!c || !mode || !planes_stress || !planes_velocity) return fail(c, FDP_ERR_ARG, "null argument");
+  if (!c->have_medium) return fail(c, FDP_ERR_STATE, "no medium set");
+  auto count = [&](int k0, int k1) {
+    bool seen[fdp::C_NCOEF] = {};
+    int n = 0;
+    for (int k = k0; k <= k1; ++k)
+      if (c->src[k] >= 0 && !seen[c->src[k]]) { seen[c->src[k]] = true; ++n; }
+    return n;
+  };
+  *mode = c->medium_mode;
+  *planes_stress = c->medium_mode == fdp::M_PLANES ? count(fdp::C_MU, fdp::C_P3) : 0;
+  *planes_velocity = c->medium_mode == fdp::M_PLANES ? count(fdp::C_EQX, fdp::C_R3W) : 0;
+  return FDP_OK;
+}
 
 int fdp_get_stream(fdp_ctx* c, void** stream) {
   if (!c || !stream) return fail(c, FDP_ERR_ARG, "null argument");
@@ -695,7 +770,7 @@ void fdp_destroy(fdp_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase};
+  DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase, &c->errbuf};
   for (auto* a : all) if (a->p) cudaFree(a->p);
   for (auto& a : c->fields) if (a.p) cudaFree(a.p);
   for (auto& a : c->prof) if (a.p) cudaFree(a.p);

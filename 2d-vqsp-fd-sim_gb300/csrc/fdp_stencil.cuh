@@ -27,6 +27,7 @@
 //            stored transposed [J][I-PMLL] so a warp reads them coalesced
 //   memory variables in the reference's own bounds (ppml.F90:85-112)
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -90,6 +91,8 @@ template <class T> struct Params {
   int MR;
   const int* REC;
   T* RAW;
+  // device status word: bit 0 set when a bounded wait gave up
+  int* err;
 };
 
 #define FDP_F(ptr, I, L) (ptr)[(long long)(L) * p.pitch + ((I) - p.PMLL)]
@@ -111,26 +114,39 @@ __device__ __forceinline__ T coef(const Params<T>& p, int k, long long cell, int
 #define FDP_C(k) coef<T, MODE>(p, (k), cell_, J_)
 
 // ---------------------------------------------------------------------------
+// Stencil neighbours are read through a reader: rd(f, I, L) returns input
+// field f of the phase (velocities u w qx qz in the stress phase; stresses
+// txx tzz txz p in the velocity phase) at cell (I, L).
+template <class T> struct GlobalRd {
+  const T* f[4];
+  long long pitch;
+  int PMLL;
+  __device__ __forceinline__ T operator()(int k, int I, int L) const {
+    return __ldg(f[k] + (long long)L * pitch + (I - PMLL));
+  }
+};
+
+// ---------------------------------------------------------------------------
 // strain_uw_xx.F90:51-94 / strain_q_xx.F90:50-91 for one cell
-template <class T>
-__device__ __forceinline__ T strain_xx(const Params<T>& p, const T* U, T* ML, T* MH, int I, int L) {
+template <class T, class R>
+__device__ __forceinline__ T strain_xx(const Params<T>& p, const R& rd, int f, T* ML, T* MH, int I, int L) {
   const int TPML = p.TPML;
   if (I <= 1) {
     const int xi = (2 - I) + L * (TPML + 1);
     const int mi = (I - p.PMLL) + L * (TPML + 1);
-    const T D = p.CH * (FDP_R(U, I + 1, L) - FDP_R(U, I, L));
+    const T D = p.CH * (rd(f, I + 1, L) - rd(f, I, L));
     const T m = ML[mi];
     const T e = p.ODA_XL[xi] * (p.ODD_XL[xi] * D + m);
     ML[mi] = p.ODB_XL[xi] * m + p.ODC_XL[xi] * D;
     return e;
   }
-  if (I == 2) return p.CH * (FDP_R(U, 3, L) - FDP_R(U, 2, L));
+  if (I == 2) return p.CH * (rd(f, 3, L) - rd(f, 2, L));
   if (I <= p.MX - 2)
-    return p.AH * (FDP_R(U, I + 2, L) - FDP_R(U, I - 1, L)) + p.BH * (FDP_R(U, I + 1, L) - FDP_R(U, I, L));
-  if (I == p.MX1) return p.CH * (FDP_R(U, p.MX1 + 1, L) - FDP_R(U, p.MX1, L));
+    return p.AH * (rd(f, I + 2, L) - rd(f, I - 1, L)) + p.BH * (rd(f, I + 1, L) - rd(f, I, L));
+  if (I == p.MX1) return p.CH * (rd(f, p.MX1 + 1, L) - rd(f, p.MX1, L));
   const int xi = (I - p.MX1) + L * (TPML + 1);
   const int mi = (I - p.MX) + L * (TPML + 1);
-  const T D = p.CH * (FDP_R(U, I + 1, L) - FDP_R(U, I, L));
+  const T D = p.CH * (rd(f, I + 1, L) - rd(f, I, L));
   const T m = MH[mi];
   const T e = p.ODA_XH[xi] * (p.ODD_XH[xi] * D + m);
   MH[mi] = p.ODB_XH[xi] * m + p.ODC_XH[xi] * D;
@@ -138,18 +154,18 @@ __device__ __forceinline__ T strain_xx(const Params<T>& p, const T* U, T* ML, T*
 }
 
 // strain_uw_zz.F90:41-51 / strain_q_zz.F90:41-52 (interior and non-imaging row 1)
-template <class T>
-__device__ __forceinline__ T strain_zz(const Params<T>& p, const T* W, int I, int L) {
-  T e = (p.CH * (FDP_R(W, I, L + 1) - FDP_R(W, I, L)));
-  if (I >= 2 && I <= p.MX1) e = p.AH * (FDP_R(W, I, L + 2) - FDP_R(W, I, L - 1)) + p.BC * e;
+template <class T, class R>
+__device__ __forceinline__ T strain_zz(const Params<T>& p, const R& rd, int f, int I, int L) {
+  T e = (p.CH * (rd(f, I, L + 1) - rd(f, I, L)));
+  if (I >= 2 && I <= p.MX1) e = p.AH * (rd(f, I, L + 2) - rd(f, I, L - 1)) + p.BC * e;
   return e;
 }
 
 // strain_uw_zz_2nd_pml.F90:55-65 / strain_q_zz_2nd_pml.F90:51-64
-template <class T>
-__device__ __forceinline__ T strain_zz_pml(const Params<T>& p, const T* W, T* M, int I, int L, int LL) {
+template <class T, class R>
+__device__ __forceinline__ T strain_zz_pml(const Params<T>& p, const R& rd, int f, T* M, int I, int L, int LL) {
   const int zi = (I - p.PMLL) + LL * p.NX;
-  const T D = p.CH * (FDP_R(W, I, L + 1) - FDP_R(W, I, L));
+  const T D = p.CH * (rd(f, I, L + 1) - rd(f, I, L));
   const T m = M[zi];
   const T e = p.ODA_ZH[zi] * (p.ODD_ZH[zi] * D + m);
   M[zi] = p.ODB_ZH[zi] * m + p.ODC_ZH[zi] * D;
@@ -160,8 +176,8 @@ __device__ __forceinline__ T strain_zz_pml(const Params<T>& p, const T* W, T* M,
 // Stress update of one cell (I, L): the row routines of hplane_ic_stress,
 // hplane_lin_stress, hplane_0/1_stress (non-imaging), hplane_mz1_stress,
 // hplane_pml_stress and hplane_pmlzh0_stress restricted to that cell.
-template <class T, bool SI, int MODE>
-__device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, int it) {
+template <class T, bool SI, int MODE, class R>
+__device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int I, int L, int it) {
   const int TPML = p.TPML, MX = p.MX, MX1 = p.MX1;
   const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
   const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
@@ -179,8 +195,8 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
     } else if (pml || last) {
       // strain_uw_xz_2nd_pml.F90:69-121
       const int LL = last ? TPML + 1 : L - p.MZ + 1;
-      const T DZXA = p.CH * (FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
-      const T DXZA = p.CH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1));
+      const T DZXA = p.CH * (rd(1, I, L) - rd(1, I - 1, L));
+      const T DXZA = p.CH * (rd(0, I, L) - rd(0, I, L - 1));
       const int zi = (I - p.PMLL) + LL * p.NX;
       const T mz = p.PXZH[zi];
       const T zpart = p.ODA2_ZH[zi] * (p.ODD2_ZH[zi] * DXZA + mz);
@@ -202,29 +218,29 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
       p.PXZH[zi] = p.ODB2_ZH[zi] * mz + p.ODC2_ZH[zi] * DXZA;
     } else if (I <= 2) {
       // strain_uw_xz.F90:181-196 (and strain_uw_xz_1.F90:62-76)
-      const T DZXA = p.CH * (FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
+      const T DZXA = p.CH * (rd(1, I, L) - rd(1, I - 1, L));
       const int xi = (3 - I) + L * (TPML + 2);
       const int mi = (I - p.PMLL) + L * (TPML + 2);
       const T mx = p.PZXL[mi];
-      exz = p.CH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1)) + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
+      exz = p.CH * (rd(0, I, L) - rd(0, I, L - 1)) + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
       p.PZXL[mi] = p.ODB2_XL[xi] * mx + p.ODC2_XL[xi] * DZXA;
     } else if (I <= MX1) {
       if (r1) {
         // strain_uw_xz_1.F90:79-97 (AFDA_XZ undefined)
-        exz = p.AH * (FDP_R(p.WM, I + 1, 1) - FDP_R(p.WM, I - 2, 1)) + p.BH * (FDP_R(p.WM, I, 1) - FDP_R(p.WM, I - 1, 1))
-            + p.CH * (FDP_R(p.UM, I, 1) - FDP_R(p.UM, I, 0));
+        exz = p.AH * (rd(1, I + 1, 1) - rd(1, I - 2, 1)) + p.BH * (rd(1, I, 1) - rd(1, I - 1, 1))
+            + p.CH * (rd(0, I, 1) - rd(0, I, 0));
       } else {
         // strain_uw_xz.F90:198-206
-        exz = p.AH * (FDP_R(p.UM, I, L + 1) - FDP_R(p.UM, I, L - 2) + FDP_R(p.WM, I + 1, L) - FDP_R(p.WM, I - 2, L))
-            + p.BH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1) + FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
+        exz = p.AH * (rd(0, I, L + 1) - rd(0, I, L - 2) + rd(1, I + 1, L) - rd(1, I - 2, L))
+            + p.BH * (rd(0, I, L) - rd(0, I, L - 1) + rd(1, I, L) - rd(1, I - 1, L));
       }
     } else {
       // strain_uw_xz.F90:209-223
-      const T DZXA = p.CH * (FDP_R(p.WM, I, L) - FDP_R(p.WM, I - 1, L));
+      const T DZXA = p.CH * (rd(1, I, L) - rd(1, I - 1, L));
       const int xi = (I - MX1) + L * (TPML + 2);
       const int mi = (I - MX) + L * (TPML + 1);
       const T mx = p.PZXH[mi];
-      exz = p.CH * (FDP_R(p.UM, I, L) - FDP_R(p.UM, I, L - 1)) + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
+      exz = p.CH * (rd(0, I, L) - rd(0, I, L - 1)) + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
       p.PZXH[mi] = p.ODB2_XH[xi] * mx + p.ODC2_XH[xi] * DZXA;
     }
     const T TXZv = FDP_C(C_MU) * exz;
@@ -236,18 +252,18 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, int I, int L, in
   if (I < 2 - TPML || I > MX1 + TPML) return;
   T ezz, qzz;
   if (r0) {
-    ezz = (p.CH * (FDP_R(p.WM, I, 1) - FDP_R(p.WM, I, 0)));  // strain_uw_zz_0.F90:45-49
-    qzz = (p.CH * (FDP_R(p.QZ, I, 1) - FDP_R(p.QZ, I, 0)));  // strain_q_zz_0.F90:40-44
+    ezz = (p.CH * (rd(1, I, 1) - rd(1, I, 0)));  // strain_uw_zz_0.F90:45-49
+    qzz = (p.CH * (rd(3, I, 1) - rd(3, I, 0)));  // strain_q_zz_0.F90:40-44
   } else if (pml || mz1) {
     const int LL = mz1 ? 0 : L - p.MZ + 1;
-    ezz = strain_zz_pml(p, p.WM, p.PZZH, I, L, LL);
-    qzz = strain_zz_pml(p, p.QZ, p.OZZH, I, L, LL);
+    ezz = strain_zz_pml(p, rd, 1, p.PZZH, I, L, LL);
+    qzz = strain_zz_pml(p, rd, 3, p.OZZH, I, L, LL);
   } else {
-    ezz = strain_zz(p, p.WM, I, L);
-    qzz = strain_zz(p, p.QZ, I, L);
+    ezz = strain_zz(p, rd, 1, I, L);
+    qzz = strain_zz(p, rd, 3, I, L);
   }
-  const T exx = strain_xx(p, p.UM, p.PXXL, p.PXXH, I, L);
-  const T qxx = strain_xx(p, p.QX, p.OXXL, p.OXXH, I, L);
+  const T exx = strain_xx(p, rd, 0, p.PXXL, p.PXXH, I, L);
+  const T qxx = strain_xx(p, rd, 2, p.OXXL, p.OXXH, I, L);
   const T s1 = FDP_C(C_SXX1), s2 = FDP_C(C_SXX2), s3 = FDP_C(C_SXX3);
   const T z1 = FDP_C(C_SZZ1), z2 = FDP_C(C_SZZ2), z3 = FDP_C(C_SZZ3);
   const T q1 = FDP_C(C_P1), q2 = FDP_C(C_P2), q3 = FDP_C(C_P3);
@@ -278,7 +294,8 @@ __global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Pa
   const int L = (int)(blockIdx.y * kBZ + threadIdx.y);
   if (I <= p.PMLXH && L <= p.PMLZH && (!SI || L >= 2)) {
     const int it = *p.it_base + it_off;
-    stress_cell<T, SI, MODE>(p, I, L, it);
+    const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
+    stress_cell<T, SI, MODE>(p, rd, I, L, it);
   }
   if (SI && blockIdx.y == 0) {
     __syncthreads();  // rows 2..4 of this block are final
@@ -302,8 +319,8 @@ __global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Pa
 // after its update over exactly the columns and rows where u and w read the
 // copy (sto_qxp.F90:24, sto_qzp.F90:24), so QXP(I,L) always equals the q of
 // the previous level at that cell.
-template <class T, bool SI, int MODE>
-__device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) {
+template <class T, bool SI, int MODE, class R>
+__device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, int I, int L) {
   const int TPML = p.TPML, MX = p.MX, MX1 = p.MX1;
   const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
   const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
@@ -321,9 +338,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
       // inh_qx_int_2nd_pml.F90 / inh_v_u_int_2nd_pml.F90
       const int LL = L - p.MZ + 1;
       const int zi = (I - p.PMLL) + LL * p.NX;
-      const T DXXXA = FDP_R(p.TXX, I, L) - FDP_R(p.TXX, I - 1, L);
-      const T DXZZA = FDP_R(p.TXZ, I, L + 1) - FDP_R(p.TXZ, I, L);
-      const T PXXXA = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L);
+      const T DXXXA = rd(0, I, L) - rd(0, I - 1, L);
+      const T DXZZA = rd(2, I, L + 1) - rd(2, I, L);
+      const T PXXXA = rd(3, I, L) - rd(3, I - 1, L);
       const T za = p.ODA_ZH[zi], zd = p.ODD_ZH[zi], zb = p.ODB_ZH[zi], zc = p.ODC_ZH[zi];
       const T gz = p.GXZH[zi], rz = p.RXZH[zi];
       if (I <= 3 || I >= MX1) {
@@ -348,7 +365,7 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         R[mi] = xb * r + xc * DXXXA;
         S[mi] = xb * s + xc * PXXXA;
       } else {
-        qx = E * qx0 - R1 * (za * (zd * DXZZA + gz) + DXXXA) - R2 * (FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L));
+        qx = E * qx0 - R1 * (za * (zd * DXZZA + gz) + DXXXA) - R2 * (rd(3, I, L) - rd(3, I - 1, L));
         u = u0 + Cu * qx0 + R1u * (DXXXA + za * (zd * DXZZA + rz)) + R3u * PXXXA;
       }
       p.GXZH[zi] = zb * gz + zc * DXZZA;
@@ -369,9 +386,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
           xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
           G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
         }
-        const T DXXXA = FDP_R(p.TXX, I, L) - FDP_R(p.TXX, I - 1, L);
-        const T PXXXA = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L);
-        const T txz1 = FDP_R(p.TXZ, I, L + 1), txz0 = FDP_R(p.TXZ, I, L);
+        const T DXXXA = rd(0, I, L) - rd(0, I - 1, L);
+        const T PXXXA = rd(3, I, L) - rd(3, I - 1, L);
+        const T txz1 = rd(2, I, L + 1), txz0 = rd(2, I, L);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
         const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
         qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1 - txz0) - R2 * (xa * (xd * PXXXA + h));
@@ -382,9 +399,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         S[mi] = xb * s + xc * PXXXA;
       } else {
         // inh_qx_int.F90:40-54 / inh_v_uv_int.F90:41-56
-        const T X = A * (FDP_R(p.TXX, I + 1, L) - FDP_R(p.TXX, I - 2, L) + FDP_R(p.TXZ, I, L + 2) - FDP_R(p.TXZ, I, L - 1))
-                  + B * (FDP_R(p.TXX, I, L) - FDP_R(p.TXX, I - 1, L) + FDP_R(p.TXZ, I, L + 1) - FDP_R(p.TXZ, I, L));
-        const T P = A * (FDP_R(p.PRES, I + 1, L) - FDP_R(p.PRES, I - 2, L)) + B * (FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I - 1, L));
+        const T X = A * (rd(0, I + 1, L) - rd(0, I - 2, L) + rd(2, I, L + 2) - rd(2, I, L - 1))
+                  + B * (rd(0, I, L) - rd(0, I - 1, L) + rd(2, I, L + 1) - rd(2, I, L));
+        const T P = A * (rd(3, I + 1, L) - rd(3, I - 2, L)) + B * (rd(3, I, L) - rd(3, I - 1, L));
         qx = E * qx0 - R1 * X - R2 * P;
         u = u0 + Cu * qx0 + R1u * X + R3u * P;
       }
@@ -404,9 +421,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
           xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
           G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
         }
-        const T DXXXA = FDP_R(p.TXX, I, 0) - FDP_R(p.TXX, I - 1, 0);
-        const T PXXXA = FDP_R(p.PRES, I, 0) - FDP_R(p.PRES, I - 1, 0);
-        const T txz1 = FDP_R(p.TXZ, I, 1);
+        const T DXXXA = rd(0, I, 0) - rd(0, I - 1, 0);
+        const T PXXXA = rd(3, I, 0) - rd(3, I - 1, 0);
+        const T txz1 = rd(2, I, 1);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
         const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
         qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1) - R2 * (xa * (xd * PXXXA + h));
@@ -416,10 +433,10 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         R[mi] = xb * r + xc * DXXXA;
         S[mi] = xb * s + xc * PXXXA;
       } else {
-        const T X = A * (FDP_R(p.TXX, I + 1, 0) - FDP_R(p.TXX, I - 2, 0)) + B * (FDP_R(p.TXX, I, 0) - FDP_R(p.TXX, I - 1, 0))
-                  + T(17) / T(24) * FDP_R(p.TXZ, I, 1) + T(3) / T(8) * FDP_R(p.TXZ, I, 2)
-                  - T(5) / T(24) * FDP_R(p.TXZ, I, 3) + T(1) / T(24) * FDP_R(p.TXZ, I, 4);
-        const T P = A * (FDP_R(p.PRES, I + 1, 0) - FDP_R(p.PRES, I - 2, 0)) + B * (FDP_R(p.PRES, I, 0) - FDP_R(p.PRES, I - 1, 0));
+        const T X = A * (rd(0, I + 1, 0) - rd(0, I - 2, 0)) + B * (rd(0, I, 0) - rd(0, I - 1, 0))
+                  + T(17) / T(24) * rd(2, I, 1) + T(3) / T(8) * rd(2, I, 2)
+                  - T(5) / T(24) * rd(2, I, 3) + T(1) / T(24) * rd(2, I, 4);
+        const T P = A * (rd(3, I + 1, 0) - rd(3, I - 2, 0)) + B * (rd(3, I, 0) - rd(3, I - 1, 0));
         qx = E * qx0 - R1 * X - R2 * P;
         u = u0 + Cu * qx0 + R1u * X + R3u * P;
       }
@@ -439,9 +456,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
       // inh_qz_int_2nd_pml.F90 / inh_v_w_int_2nd_pml.F90
       const int LL = L - p.MZ + 1;
       const int zi = (I - p.PMLL) + LL * p.NX;
-      const T DXZXA = FDP_R(p.TXZ, I + 1, L) - FDP_R(p.TXZ, I, L);
-      const T DZZZA = FDP_R(p.TZZ, I, L) - FDP_R(p.TZZ, I, L - 1);
-      const T PZZZA = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I, L - 1);
+      const T DXZXA = rd(2, I + 1, L) - rd(2, I, L);
+      const T DZZZA = rd(1, I, L) - rd(1, I, L - 1);
+      const T PZZZA = rd(3, I, L) - rd(3, I, L - 1);
       const T za = p.ODA2_ZH[zi], zd = p.ODD2_ZH[zi], zb = p.ODB2_ZH[zi], zc = p.ODC2_ZH[zi];
       const T gz = p.GZZH[zi], hz = p.HZZH[zi], rz = p.RZZH[zi], sz = p.SZZH[zi];
       if (I <= 2 || I >= MX1) {
@@ -482,9 +499,9 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
           xi = (I - MX1) + L * (TPML + 1); mi = (I - (MX - 1)) + L * (TPML + 2);
           xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; R = p.RZXH;
         }
-        const T DXZXA = FDP_R(p.TXZ, I + 1, L) - FDP_R(p.TXZ, I, L);
-        const T dzz = FDP_R(p.TZZ, I, L) - FDP_R(p.TZZ, I, L - 1);
-        const T dp = FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I, L - 1);
+        const T DXZXA = rd(2, I + 1, L) - rd(2, I, L);
+        const T dzz = rd(1, I, L) - rd(1, I, L - 1);
+        const T dp = rd(3, I, L) - rd(3, I, L - 1);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
         const T g = G[mi], r = R[mi];
         qz = E * qz0 - R1 * (dzz + xa * (xd * DXZXA + g)) - R2 * dp;
@@ -493,18 +510,18 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
         R[mi] = xb * r + xc * DXZXA;
       } else if (SI || L >= 2) {
         // inh_qz_int.F90:41-55 / inh_v_w_int.F90:43-58
-        const T X = A * (FDP_R(p.TZZ, I, L + 1) - FDP_R(p.TZZ, I, L - 2) + FDP_R(p.TXZ, I + 2, L) - FDP_R(p.TXZ, I - 1, L))
-                  + B * (FDP_R(p.TZZ, I, L) - FDP_R(p.TZZ, I, L - 1) + FDP_R(p.TXZ, I + 1, L) - FDP_R(p.TXZ, I, L));
-        const T P = A * (FDP_R(p.PRES, I, L + 1) - FDP_R(p.PRES, I, L - 2)) + B * (FDP_R(p.PRES, I, L) - FDP_R(p.PRES, I, L - 1));
+        const T X = A * (rd(1, I, L + 1) - rd(1, I, L - 2) + rd(2, I + 2, L) - rd(2, I - 1, L))
+                  + B * (rd(1, I, L) - rd(1, I, L - 1) + rd(2, I + 1, L) - rd(2, I, L));
+        const T P = A * (rd(3, I, L + 1) - rd(3, I, L - 2)) + B * (rd(3, I, L) - rd(3, I, L - 1));
         qz = E * qz0 - R1 * X - R2 * P;
         w = w0 + Cw * qz0 + R1w * X + R3w * P;
       } else {
         // row 1 without stress imaging: inh_v_qz_int_1.F90 / inh_v_w_int_1.F90
-        const T X = A * (FDP_R(p.TXZ, I + 2, 1) - FDP_R(p.TXZ, I - 1, 1)) + B * (FDP_R(p.TXZ, I + 1, 1) - FDP_R(p.TXZ, I, 1))
-                  - T(31) / T(24) * FDP_R(p.TZZ, I, 0) + T(29) / T(24) * FDP_R(p.TZZ, I, 1)
-                  - T(3) / T(40) * FDP_R(p.TZZ, I, 2) + T(1) / T(168) * FDP_R(p.TZZ, I, 3);
-        const T P = -T(31) / T(24) * FDP_R(p.PRES, I, 0) + T(29) / T(24) * FDP_R(p.PRES, I, 1)
-                  - T(3) / T(40) * FDP_R(p.PRES, I, 2) + T(1) / T(168) * FDP_R(p.PRES, I, 3);
+        const T X = A * (rd(2, I + 2, 1) - rd(2, I - 1, 1)) + B * (rd(2, I + 1, 1) - rd(2, I, 1))
+                  - T(31) / T(24) * rd(1, I, 0) + T(29) / T(24) * rd(1, I, 1)
+                  - T(3) / T(40) * rd(1, I, 2) + T(1) / T(168) * rd(1, I, 3);
+        const T P = -T(31) / T(24) * rd(3, I, 0) + T(29) / T(24) * rd(3, I, 1)
+                  - T(3) / T(40) * rd(3, I, 2) + T(1) / T(168) * rd(3, I, 3);
         qz = E * qz0 - R1 * X - R2 * P;
         w = w0 + Cw * qz0 + R1w * X + R3w * P;
       }
@@ -513,13 +530,13 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, int I, int L) 
       // inh_qz_2nd_0.F90, inh_v_w_2nd_0.F90
       T X, P;
       if (I <= 2 || I >= MX1) {
-        X = T(3) * FDP_R(p.TZZ, I, 0) - T(1) / T(3) * FDP_R(p.TZZ, I, 1);
-        P = T(3) * FDP_R(p.PRES, I, 0) - T(1) / T(3) * FDP_R(p.PRES, I, 1);
+        X = T(3) * rd(1, I, 0) - T(1) / T(3) * rd(1, I, 1);
+        P = T(3) * rd(3, I, 0) - T(1) / T(3) * rd(3, I, 1);
       } else {
-        X = T(35) / T(8) * FDP_R(p.TZZ, I, 0) - T(35) / T(24) * FDP_R(p.TZZ, I, 1)
-          + T(21) / T(40) * FDP_R(p.TZZ, I, 2) - T(5) / T(56) * FDP_R(p.TZZ, I, 3);
-        P = T(35) / T(8) * FDP_R(p.PRES, I, 0) - T(35) / T(24) * FDP_R(p.PRES, I, 1)
-          + T(21) / T(40) * FDP_R(p.PRES, I, 2) - T(5) / T(56) * FDP_R(p.PRES, I, 3);
+        X = T(35) / T(8) * rd(1, I, 0) - T(35) / T(24) * rd(1, I, 1)
+          + T(21) / T(40) * rd(1, I, 2) - T(5) / T(56) * rd(1, I, 3);
+        P = T(35) / T(8) * rd(3, I, 0) - T(35) / T(24) * rd(3, I, 1)
+          + T(21) / T(40) * rd(3, I, 2) - T(5) / T(56) * rd(3, I, 3);
       }
       qz = E * qz0 - R1 * X - R2 * P;
       w = w0 + Cw * qz0 + R1w * X + R3w * P;
@@ -547,7 +564,10 @@ __global__ void __launch_bounds__(kBX * kBZ) k_velocity(const __grid_constant__ 
     old[k][0][tx] = FDP_F(p.UM, I, L); old[k][1][tx] = FDP_F(p.WM, I, L);
     old[k][2][tx] = FDP_F(p.QX, I, L); old[k][3][tx] = FDP_F(p.QZ, I, L);
   }
-  if (inx && L >= (SI ? 2 : 0) && L < p.PMLZH) velocity_cell<T, SI, MODE>(p, I, L);
+  if (inx && L >= (SI ? 2 : 0) && L < p.PMLZH) {
+    const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
+    velocity_cell<T, SI, MODE>(p, rd, I, L);
+  }
   if (bottom) {
     const bool me = inx && L == p.PMLZH;
     const int x = I - p.PMLL;
@@ -637,6 +657,212 @@ __global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> 
 #pragma unroll
     for (int k = 0; k < 6; ++k) out[k] = s[k];
   }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged variants of the two phases.
+//
+// A CTA of 64 x 4 threads owns a tile of kTX x kTZ cells.  One thread issues
+// a 2-D bulk tensor copy (cp.async.bulk.tensor) of each of the phase's four
+// input fields -- the tile plus kHX columns and kHZ rows of halo -- into
+// shared memory, completing on one mbarrier; meanwhile every thread
+// prefetches the cells it read-modify-writes and their medium planes into
+// L1.  Each thread then updates kRows cells of one column with every stencil
+// neighbour read from shared memory.  The cell arithmetic is the same
+// stress_cell / velocity_cell code as the global-load kernels.
+constexpr int kTX = 64, kTZ = 16, kHX = 4, kHZ = 2;
+constexpr int kSX = kTX + 2 * kHX, kSZ = kTZ + 2 * kHZ;
+constexpr int kRows = kTZ / 4;
+static_assert(kHX == kPadX, "the halo of a tile must start on the 16-byte-aligned padding column");
+
+struct TmaMaps {
+  CUtensorMap m[4];  // the phase's input fields, boxes of kSX x kSZ elements
+};
+
+template <class T> struct SmemRd {
+  const T* s;  // [4][kSZ][kSX]
+  int I0, L0;  // cell of tile element (kHX, kHZ)
+  __device__ __forceinline__ T operator()(int k, int I, int L) const {
+    return s[(k * kSZ + (L - L0 + kHZ)) * kSX + (I - I0 + kHX)];
+  }
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* ptr) { return (uint32_t)__cvta_generic_to_shared(ptr); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for the tile's copies with an iteration limit (far above any real
+// latency); false means the copies did not complete in time.
+constexpr unsigned kWaitLimit = 1u << 22;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (unsigned i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_l1(const void* ptr) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(ptr));
+}
+
+// Issues the tile copy (thread 0), prefetches the thread's own cells, and
+// waits.  x, y: element coordinates of the tile's first halo element.
+template <class T>
+__device__ __forceinline__ bool stage_tile(T* s, uint64_t* bar, const TmaMaps& maps, int x, int y) {
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  if (tid == 0) mbar_init(bar, 1);
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, 4u * kSZ * kSX * (uint32_t)sizeof(T));
+#pragma unroll
+    for (int f = 0; f < 4; ++f) tma_load_2d(s + f * kSZ * kSX, &maps.m[f], x, y, bar);
+  }
+  return true;
+}
+
+template <class T, bool SI, int MODE>
+__global__ void __launch_bounds__(kTX * 4) k_stress_tma(const __grid_constant__ Params<T> p,
+                                                        const __grid_constant__ TmaMaps maps, int it_off) {
+  __shared__ alignas(128) T s[4 * kSZ * kSX];
+  __shared__ alignas(8) uint64_t bar;
+  const int I0 = p.PMLL + (int)blockIdx.x * kTX, L0 = (int)blockIdx.y * kTZ;
+  const int I = I0 + (int)threadIdx.x;
+  const int Lt = L0 + (int)threadIdx.y * kRows;
+  stage_tile(s, &bar, maps, (int)blockIdx.x * kTX + kPadX - kHX, L0 + kPadZ - kHZ);
+  if (I <= p.PMLXH) {
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      if (Lt + r > p.PMLZH) break;
+      const long long c = (long long)(Lt + r) * p.pitch + (I - p.PMLL);
+      prefetch_l1(p.TXX + c); prefetch_l1(p.TZZ + c); prefetch_l1(p.TXZ + c); prefetch_l1(p.PRES + c);
+      if (MODE == M_PLANES)
+        for (int k = 0; k < C_NCOEF; ++k)
+          if (k <= C_P3 && p.src[k] >= 0) prefetch_l1(p.planes + (long long)p.src[k] * p.pstride + c);
+    }
+  }
+  const int it = *p.it_base + it_off;
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (!ok && threadIdx.x == 0 && threadIdx.y == 0) atomicOr(p.err, 1);
+  if (ok && I <= p.PMLXH) {
+    const SmemRd<T> rd{s, I0, L0};
+    for (int r = 0; r < kRows; ++r) {
+      const int L = Lt + r;
+      if (L <= p.PMLZH && (!SI || L >= 2)) stress_cell<T, SI, MODE>(p, rd, I, L, it);
+    }
+  }
+  if (SI && blockIdx.y == 0) {
+    __syncthreads();  // rows 2..4 of this tile are final
+    if (ok && I <= p.PMLXH && threadIdx.y == 0) {
+      // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53
+      FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
+      FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
+      FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
+      FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
+      FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
+      FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
+      FDP_F(p.TXZ, I, 2) = T(0);
+    }
+  }
+  if (!ok) mbar_wait_bounded(&bar, 0);  // let copies still in flight land before the CTA exits
+}
+
+// Tiles run from the bottom row up, so the thread that owns the bottom row
+// of a column also owns rows PMLZH-1 and PMLZH-2 (kRows >= 3) and keeps their
+// pre-phase values (the history of time_loop.F90:133-155) in registers.
+template <class T, bool SI, int MODE>
+__global__ void __launch_bounds__(kTX * 4) k_velocity_tma(const __grid_constant__ Params<T> p,
+                                                          const __grid_constant__ TmaMaps maps, int it_off) {
+  static_assert(kRows >= 3, "the bottom row needs two rows above it in the same thread");
+  (void)it_off;
+  __shared__ alignas(128) T s[4 * kSZ * kSX];
+  __shared__ alignas(8) uint64_t bar;
+  const int I0 = p.PMLL + (int)blockIdx.x * kTX;
+  const int L0 = p.PMLZH + 1 - ((int)blockIdx.y + 1) * kTZ;
+  const int I = I0 + (int)threadIdx.x;
+  const int Lt = L0 + (int)threadIdx.y * kRows;
+  const int Lmin = SI ? 2 : 0;
+  stage_tile(s, &bar, maps, (int)blockIdx.x * kTX + kPadX - kHX, L0 + kPadZ - kHZ);
+  if (I <= p.PMLXH) {
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      if (Lt + r < Lmin) continue;
+      const long long c = (long long)(Lt + r) * p.pitch + (I - p.PMLL);
+      prefetch_l1(p.UM + c); prefetch_l1(p.WM + c); prefetch_l1(p.QX + c); prefetch_l1(p.QZ + c);
+      if (MODE == M_PLANES)
+        for (int k = C_EQX; k <= C_R3W; ++k)
+          if (p.src[k] >= 0) prefetch_l1(p.planes + (long long)p.src[k] * p.pstride + c);
+    }
+  }
+  const bool ok = mbar_wait_bounded(&bar, 0);
+  if (!ok && threadIdx.x == 0 && threadIdx.y == 0) atomicOr(p.err, 1);
+  if (ok && I <= p.PMLXH) {
+    const SmemRd<T> rd{s, I0, L0};
+    const bool owns_bottom = (Lt + kRows - 1 == p.PMLZH);
+    T old[3][4];  // pre-phase rows PMLZH (k=0), PMLZH-1 (1), PMLZH-2 (2) of u w qx qz
+#pragma unroll
+    for (int r = 0; r < kRows; ++r) {
+      const int L = Lt + r;
+      if (owns_bottom && r >= kRows - 3) {
+        const int k = kRows - 1 - r;
+        old[k][0] = FDP_F(p.UM, I, L); old[k][1] = FDP_F(p.WM, I, L);
+        old[k][2] = FDP_F(p.QX, I, L); old[k][3] = FDP_F(p.QZ, I, L);
+      }
+      if (L >= Lmin && L < p.PMLZH) {
+        if (!SI && L <= 1) {
+          // rows 0 and 1 without stress imaging reach rows up to 4
+          // (inh_qx_int_0.F90), beyond the tile's halo when the tile starts
+          // above row -13
+          const GlobalRd<T> grd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
+          velocity_cell<T, SI, MODE>(p, grd, I, L);
+        } else {
+          velocity_cell<T, SI, MODE>(p, rd, I, L);
+        }
+      }
+    }
+    if (owns_bottom) {
+      // hplane_pmlzh0_velocity.F90:34-63
+      const int LST = p.PMLZH, x = I - p.PMLL;
+      T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
+        T* hist = p.HIST + (long long)c * 3 * p.NX;
+        const T sp0 = hist[x], sp1 = hist[p.NX + x], sp2 = hist[2 * p.NX + x];
+        const T v = ab[0] * FDP_F(f[c], I, LST - 1) + ab[1] * FDP_F(f[c], I, LST - 2)
+                  + ab[2] * old[0][c] + ab[3] * old[1][c] + ab[4] * old[2][c]
+                  + ab[5] * sp0 + ab[6] * sp1 + ab[7] * sp2;
+        FDP_F(f[c], I, LST) = v;
+        hist[x] = old[0][c];
+        hist[p.NX + x] = old[1][c];
+        hist[2 * p.NX + x] = old[2][c];
+      }
+    }
+  }
+  if (!ok) mbar_wait_bounded(&bar, 0);
 }
 
 __global__ void k_set_base(int* base, int v) { *base = v; }

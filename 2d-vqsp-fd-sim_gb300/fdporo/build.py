@@ -31,7 +31,8 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "--fmad=false", "-std=c++17",
                      "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-SOURCES = ["fdp_engine.cu", "fdp_prep.cpp"]
+SOURCES = ["fdp_engine.cu", "fdp_prep.cpp", "fdp_io.cpp"]
+HOST_EXE = LIB_DIR / "fdp_host"
 
 
 def _nvcc() -> str:
@@ -42,7 +43,7 @@ def _nvcc() -> str:
 
 
 def _inputs() -> list[Path]:
-    files = [CSRC / s for s in SOURCES]
+    files = [CSRC / s for s in SOURCES] + [CSRC / "fdp_host.cpp"]
     files += sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
     return files
 
@@ -87,6 +88,16 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB_PATH)
+    # the drop-in host executable, linked against the library next to it
+    exe_tmp = HOST_EXE.with_suffix(".tmp")
+    cmd = ["g++", *CXX_FLAGS, f"-I{INCLUDE}", str(CSRC / "fdp_host.cpp"), "-o", str(exe_tmp),
+           f"-L{LIB_DIR}", "-lfdp", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(exe_tmp, HOST_EXE)
     return LIB_PATH
 
 

@@ -130,6 +130,14 @@ class Engine:
         self._check(self.lib.fdp_get_stream(self._ctx, C.byref(s)))
         return int(s.value or 0)
 
+    def medium_info(self) -> dict:
+        """Device representation of the medium: mode ("table" or "planes")
+        and the per-cell coefficient planes each phase reads."""
+        v = [C.c_int32() for _ in range(3)]
+        self._check(self.lib.fdp_medium_info(self._ctx, *[C.byref(x) for x in v]))
+        return {"mode": "planes" if v[0].value == 1 else "table", "planes_stress": v[1].value,
+                "planes_velocity": v[2].value}
+
     def profile(self, it_begin: int, it_end: int) -> dict:
         """Per-kernel device time (ms) and launch counts over levels it_begin..it_end."""
         ms = (C.c_double * 3)()

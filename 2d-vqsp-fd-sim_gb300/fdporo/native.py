@@ -72,6 +72,7 @@ SIGNATURES = {
     "fdp_synchronize": (C.c_int, [_VP]),
     "fdp_kernel_launches": (C.c_int64, [_VP]),
     "fdp_get_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "fdp_medium_info": (C.c_int, [_VP, _PI32, _PI32, _PI32]),
     "fdp_profile_run": (C.c_int, [_VP, _I32, _I32, _PD, C.POINTER(C.c_int64)]),
     "fdp_last_error": (C.c_char_p, [_VP]),
     "fdp_destroy": (None, [_VP]),
@@ -82,6 +83,10 @@ SIGNATURES = {
                                C.POINTER(_VP)]),
     "fdp_prep_bottom_nr": (C.c_int, [_I32, _I32, _I32, _I32, _I32, _D, _D, _D, _D, _D, _D, _PI32, _I32, _VP, _VP]),
     "fdp_prep_source": (C.c_int, [_I32, _I32, _VP, _VP, _I32, _D, _D, _I32, _D, _VP]),
+    "fdp_io_format_e": (C.c_int, [_D, _I32, _I32, C.c_char_p]),
+    "fdp_io_namelist_get": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t]),
+    "fdp_io_read_record": (C.c_int, [C.c_char_p, C.c_int64, _VP, C.c_int64, C.POINTER(C.c_int64)]),
+    "fdp_io_append_record": (C.c_int, [C.c_char_p, _VP, C.c_int64]),
 }
 
 _lib: C.CDLL | None = None

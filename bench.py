@@ -74,22 +74,27 @@ def prepare_inputs(precision: str, mt2: int):
     return job.prepare(cfg, med, precision)
 
 
-def algorithmic_bytes(inp, s: int) -> dict:
+def algorithmic_bytes(inp, s: int, medium: dict) -> dict:
     """Compulsory DRAM bytes per launch of each kernel for this workload:
-    every wavefield value the kernel reads or read-modify-writes, the JM
-    index and the material coefficients of each cell, and every PML memory
-    variable it updates (read + write).  Damping profiles are one-dimensional
-    and cache-resident and are not counted."""
+    every wavefield value the kernel reads or read-modify-writes, the
+    material coefficients of each cell as the engine holds them (one value
+    per distinct coefficient plane, or the JM index in table mode), and
+    every PML memory variable it updates (read + write).  Damping profiles
+    and a material table are small and cache-resident and are not counted."""
     nx, nz, tp = inp.nx, inp.nz, inp.tpml
     cells = nx * nz
+    if medium["mode"] == "table":
+        med_s = med_v = 4
+    else:
+        med_s, med_v = medium["planes_stress"] * s, medium["planes_velocity"] * s
     # element counts of the memory variables (ppml.F90:85-112)
     side = lambda w: w * nz
     bottom = lambda h: nx * h
     stress_mem = (side(tp + 2) + side(tp + 1) + 2 * side(tp + 1) + 2 * side(tp + 1)
                   + bottom(tp + 2) + 2 * bottom(tp + 1))
     vel_mem = (4 * side(tp + 3) + 4 * side(tp + 2) + 2 * side(tp + 2) + 2 * side(tp + 2) + 6 * bottom(tp + 1))
-    stress = cells * (4 * s + 8 * s + 4 + 10 * s) + 2 * s * stress_mem
-    velocity = cells * (4 * s + 8 * s + 4 + 12 * s) + 2 * s * vel_mem + 2 * s * 12 * nx
+    stress = cells * (4 * s + 8 * s + med_s) + 2 * s * stress_mem
+    velocity = cells * (4 * s + 8 * s + med_v) + 2 * s * vel_mem + 2 * s * 12 * nx
     return {"stress": stress, "velocity": velocity, "per_cell_stress": stress / cells,
             "per_cell_velocity": velocity / cells}
 
@@ -243,7 +248,8 @@ def run_gpu(args) -> None:
     # ---- per-kernel device time (separate launches between events)
     lo = args.warmup + args.steps + 1
     prof = eng.profile(lo, lo + prof_levels - 1)
-    alg = algorithmic_bytes(inp, s)
+    medium = eng.medium_info()
+    alg = algorithmic_bytes(inp, s, medium)
     kern = max(("stress", "velocity"), key=lambda k: prof[k][0])
     avg_ms = prof[kern][0] / prof[kern][1]
     peak, peak_kind = measured_peak_gbs()
@@ -300,7 +306,9 @@ def run_gpu(args) -> None:
         "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": ncu_traffic(kern),
                      "alg_bytes_per_launch": alg[kern], "avg_launch_ms": avg_ms,
-                     "kernel_share": shares},
+                     "alg_bytes_per_cell": {"stress": alg["per_cell_stress"], "velocity": alg["per_cell_velocity"]},
+                     "kernel_ms": {k: prof[k][0] / max(prof[k][1], 1) for k in prof},
+                     "medium": medium, "kernel_share": shares},
         "e2e": e2e,
         "cpu_baseline": cpu,
     }

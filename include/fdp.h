@@ -38,6 +38,7 @@ extern "C" {
 #define FDP_ERR_ALLOC (-3)       /* device or host allocation failed           */
 #define FDP_ERR_STATE (-4)       /* call out of order (e.g. run before set_*)  */
 #define FDP_ERR_UNSUPPORTED (-5) /* field not held by this engine              */
+#define FDP_ERR_DEVICE (-6)      /* a kernel reported that a bounded wait expired */
 
 #define FDP_F32 4
 #define FDP_F64 8
@@ -171,9 +172,17 @@ int fdp_profile_run(fdp_ctx* ctx, int32_t it_begin, int32_t it_end, double* ms_o
  * (graph-launched kernels counted individually). */
 int64_t fdp_kernel_launches(fdp_ctx* ctx);
 
+/* How the medium is held on the device after fdp_set_medium: *mode is 0
+ * when the kernels index the material table through JM, 1 when each
+ * distinct coefficient column is a per-cell plane (columns equal up to sign
+ * share a plane, constant columns need none); *planes_stress and
+ * *planes_velocity count the planes each phase reads per cell. */
+int fdp_medium_info(fdp_ctx* ctx, int32_t* mode, int32_t* planes_stress, int32_t* planes_velocity);
+
 /* Last error message of the context (or of the last failed fdp_create when
  * ctx is NULL). */
 const char* fdp_last_error(const fdp_ctx* ctx);
+
 
 /* Frees the context and all its device memory (the DEALLOCATEs the
  * reference leaves to program exit). */

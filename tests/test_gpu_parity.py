@@ -14,6 +14,14 @@ from helpers import compare_state, randomize_state, small_job
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True, params=["tma", "global"])
+def kernel_variant(request, monkeypatch):
+    """Runs every test with the TMA-staged kernels and with the global-load
+    kernels (fdp_create reads FDP_KERNEL_VARIANT)."""
+    monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
+    return request.param
+
+
 def _pair(cfg, med, prec):
     from fdporo import job
     from oracle.oracle import make_oracle
