@@ -40,6 +40,11 @@ struct DevArr {
 
 }  // namespace
 
+namespace fdp {
+// Error message of calls that have no context (fdp_create, fdp_receivers_noalloc).
+void set_global_error(const char* msg) { g_create_error = msg; }
+}  // namespace fdp
+
 struct fdp_ctx {
   fdp_grid g{};
   int prec = 4;

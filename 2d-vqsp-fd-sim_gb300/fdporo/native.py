@@ -75,6 +75,8 @@ SIGNATURES = {
     "fdp_medium_info": (C.c_int, [_VP, _PI32, _PI32, _PI32]),
     "fdp_profile_run": (C.c_int, [_VP, _I32, _I32, _PD, C.POINTER(C.c_int64)]),
     "fdp_last_error": (C.c_char_p, [_VP]),
+    "fdp_receivers_noalloc": (C.c_int, [_I32, _VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _I32, _I32, _VP, _I32,
+                                        _I32, _D, _I32, _VP, _VP]),
     "fdp_destroy": (None, [_VP]),
     "fdp_prep_velocities": (C.c_int, [_I32, _D, _D, _D, _D, _D, _D, _D, _PD, _PD, _PD]),
     "fdp_prep_scale_table": (C.c_int, [_I32, _I32, _D, _D, _VP]),

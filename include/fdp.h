@@ -179,10 +179,39 @@ int64_t fdp_kernel_launches(fdp_ctx* ctx);
  * *planes_velocity count the planes each phase reads per cell. */
 int fdp_medium_info(fdp_ctx* ctx, int32_t* mode, int32_t* planes_stress, int32_t* planes_velocity);
 
-/* Last error message of the context (or of the last failed fdp_create when
- * ctx is NULL). */
+/* Last error message of the context (or of the last failed call that has
+ * no context -- fdp_create, fdp_receivers_noalloc -- when ctx is NULL). */
 const char* fdp_last_error(const fdp_ctx* ctx);
 
+/* Receiver capacity of fdp_receivers_noalloc. */
+#define FDP_NOALLOC_MAX_RECEIVERS 16384
+
+/* Receiver sampling that allocates no device memory.  It has no
+ * counterpart in the reference.  It serves callers that cannot call
+ * cudaMalloc -- a host whose device arrays come from its own memory pool,
+ * work recorded inside a CUDA stream capture, or a runtime that forbids
+ * allocation once running.  All inputs and outputs are the caller's device
+ * memory:
+ *   um wm qx qz pres txx  the wavefield after a completed level, each
+ *                         (pmll:pmll+nx-1, 0:nz-1) column-major with leading
+ *                         dimension ld elements, in precision `precision`;
+ *   rec                   4*mr int32 (IRECX LRECX IRECZ LRECZ per receiver);
+ *   out                   mr*FDP_REC_VALUES values, written exactly as one
+ *                         level of fdp_get_receivers (flags as there).
+ * The previous sample of each receiver, which the time derivative needs
+ * (store_seismograms.F90:65-66), is kept between calls in one static device
+ * array of FDP_NOALLOC_MAX_RECEIVERS entries that every GPU loading the
+ * library holds until exit; larger mr is rejected with FDP_ERR_ARG.  A call
+ * with level == 1 clears that state (the reference starts it at zero);
+ * later levels must follow in order, one call per level.  All calls share
+ * the array, so calls that overlap on the GPU race.  The first call on a
+ * device looks up the array's device address; make it before any stream
+ * capture.  The kernel is enqueued on `stream` (a cudaStream_t, may be 0);
+ * errors are returned and described by fdp_last_error(NULL). */
+int fdp_receivers_noalloc(int32_t precision, const void* um, const void* wm, const void* qx, const void* qz,
+                          const void* pres, const void* txx, int32_t nx, int32_t nz, int32_t ld, int32_t pmll,
+                          const int32_t* rec, int32_t mr, int32_t flags, double dt, int32_t level, void* out,
+                          void* stream);
 
 /* Frees the context and all its device memory (the DEALLOCATEs the
  * reference leaves to program exit). */
