@@ -214,6 +214,8 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
     p.cval[k] = sizeof(T) == 8 ? (T)c->cval_d[k] : (T)c->cval_f[k];
   }
   p.AUX = (const T*)c->aux.p;
+  for (int k = 0; k < fdp::C_NCOEF; ++k)
+    p.cptr[k] = (p.planes && c->src[k] >= 0) ? p.planes + (long long)c->src[k] * p.pstride : nullptr;
   const T** pr[24] = {&p.ODA_XL, &p.ODB_XL, &p.ODC_XL, &p.ODD_XL, &p.ODA_XH, &p.ODB_XH, &p.ODC_XH, &p.ODD_XH,
                       &p.ODA_ZH, &p.ODB_ZH, &p.ODC_ZH, &p.ODD_ZH,
                       &p.ODA2_XL, &p.ODB2_XL, &p.ODC2_XL, &p.ODD2_XL, &p.ODA2_XH, &p.ODB2_XH, &p.ODC2_XH, &p.ODD2_XH,

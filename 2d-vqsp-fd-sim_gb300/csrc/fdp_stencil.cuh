@@ -67,6 +67,7 @@ template <class T> struct Params {
   // src[k] (negated when neg[k]) at the cell's field offset
   const T* planes;
   long long pstride;
+  const T* cptr[C_NCOEF];  // plane of coefficient k at (PMLL, 0), or null when constant
   int src[C_NCOEF];
   int neg[C_NCOEF];
   T cval[C_NCOEF];
@@ -106,12 +107,103 @@ template <class T> struct Params {
 template <class T, int MODE>
 __device__ __forceinline__ T coef(const Params<T>& p, int k, long long cell, int J) {
   if (MODE == M_TABLE) return __ldg(p.coef + (long long)k * p.cld + J);
-  const int s = p.src[k];
-  if (s < 0) return p.cval[k];
-  const T v = __ldg(p.planes + (long long)s * p.pstride + cell);
+  const T* c = p.cptr[k];
+  if (!c) return p.cval[k];
+  const T v = __ldg(c + cell);
   return p.neg[k] ? -v : v;
 }
 #define FDP_C(k) coef<T, MODE>(p, (k), cell_, J_)
+
+// ---------------------------------------------------------------------------
+// Interior fast paths.  A warp is 32 consecutive cells of one row; when the
+// row is an interior row (2..MZ-2, not the source row) and all 32 columns
+// lie where every stencil of the phase is the 4th-order one, the warp runs
+// these straight-line versions of the interior branches of stress_cell /
+// velocity_cell (same expressions, same order) without region tests.
+
+// stress: EXX needs 3 <= I <= MX-2 (strain_uw_xx.F90:69); EXZ, EZZ, the
+// stresses cover that range
+template <class T>
+__device__ __forceinline__ bool stress_fast_warp(const Params<T>& p, int I, int L) {
+  const int I0 = I - (int)(threadIdx.x & 31);
+  return L >= 2 && L <= p.MZ - 2 && L != p.LIN_Z && I0 >= 3 && I0 + 31 <= p.MX - 2;
+}
+
+template <class T, int MODE>
+__device__ __forceinline__ void stress_interior(const Params<T>& p, int I, int L) {
+  const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
+  const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+  const long long P = p.pitch;
+  const T* U = p.UM + cell_;
+  const T* W = p.WM + cell_;
+  const T* X = p.QX + cell_;
+  const T* Z = p.QZ + cell_;
+  // strain_uw_xz.F90:201-204
+  const T exz = p.AH * (__ldg(U + P) - __ldg(U - 2 * P) + __ldg(W + 1) - __ldg(W - 2))
+              + p.BH * (__ldg(U) - __ldg(U - P) + __ldg(W) - __ldg(W - 1));
+  // strain_uw_zz.F90:43,49 and strain_q_zz.F90:43,49
+  T ezz = (p.CH * (__ldg(W + P) - __ldg(W)));
+  ezz = p.AH * (__ldg(W + 2 * P) - __ldg(W - P)) + p.BC * ezz;
+  T qzz = (p.CH * (__ldg(Z + P) - __ldg(Z)));
+  qzz = p.AH * (__ldg(Z + 2 * P) - __ldg(Z - P)) + p.BC * qzz;
+  // strain_uw_xx.F90:71-72 and strain_q_xx.F90:70-71
+  const T exx = p.AH * (__ldg(U + 2) - __ldg(U - 1)) + p.BH * (__ldg(U + 1) - __ldg(U));
+  const T qxx = p.AH * (__ldg(X + 2) - __ldg(X - 1)) + p.BH * (__ldg(X + 1) - __ldg(X));
+  // stress_xz.F90:44-46 and stress_nn.F90:53-59
+  const T TXZv = FDP_C(C_MU) * exz;
+  p.TXZ[cell_] = p.TXZ[cell_] + p.DTE * TXZv;
+  const T s1 = FDP_C(C_SXX1), s2 = FDP_C(C_SXX2), s3 = FDP_C(C_SXX3);
+  const T z1 = FDP_C(C_SZZ1), z2 = FDP_C(C_SZZ2), z3 = FDP_C(C_SZZ3);
+  const T q1 = FDP_C(C_P1), q2 = FDP_C(C_P2), q3 = FDP_C(C_P3);
+  const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
+  const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
+  const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
+  p.TXX[cell_] = p.TXX[cell_] + p.DTE * TXXv;
+  p.TZZ[cell_] = p.TZZ[cell_] + p.DTE * TZZv;
+  p.PRES[cell_] = p.PRES[cell_] + p.DTE * PRv;
+}
+
+// velocity: qx and u need 4 <= I <= MX-2 (inh_qx_int.F90:40); qz and w
+// (3..MX-2) cover that range
+template <class T>
+__device__ __forceinline__ bool velocity_fast_warp(const Params<T>& p, int I, int L) {
+  const int I0 = I - (int)(threadIdx.x & 31);
+  return L >= 2 && L <= p.MZ - 2 && I0 >= 4 && I0 + 31 <= p.MX - 2;
+}
+
+template <class T, int MODE>
+__device__ __forceinline__ void velocity_interior(const Params<T>& p, int I, int L) {
+  const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
+  const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+  const long long P = p.pitch;
+  const T A = p.A, B = p.B;
+  const T* XX = p.TXX + cell_;
+  const T* ZZ = p.TZZ + cell_;
+  const T* XZ = p.TXZ + cell_;
+  const T* PR = p.PRES + cell_;
+  {
+    // inh_qx_int.F90:44-52 and inh_v_uv_int.F90:45-54
+    const T E = FDP_C(C_EQX), Cu = FDP_C(C_CU);
+    const T R1 = FDP_C(C_R1QX), R2 = FDP_C(C_R2QX), R1u = FDP_C(C_R1U), R3u = FDP_C(C_R3U);
+    const T qx0 = p.QX[cell_], u0 = p.UM[cell_];
+    const T X = A * (__ldg(XX + 1) - __ldg(XX - 2) + __ldg(XZ + 2 * P) - __ldg(XZ - P))
+              + B * (__ldg(XX) - __ldg(XX - 1) + __ldg(XZ + P) - __ldg(XZ));
+    const T Pp = A * (__ldg(PR + 1) - __ldg(PR - 2)) + B * (__ldg(PR) - __ldg(PR - 1));
+    p.QX[cell_] = E * qx0 - R1 * X - R2 * Pp;
+    p.UM[cell_] = u0 + Cu * qx0 + R1u * X + R3u * Pp;
+  }
+  {
+    // inh_qz_int.F90:45-53 and inh_v_w_int.F90:47-56
+    const T E = FDP_C(C_EQZ), Cw = FDP_C(C_CW);
+    const T R1 = FDP_C(C_R1QZ), R2 = FDP_C(C_R2QZ), R1w = FDP_C(C_R1W), R3w = FDP_C(C_R3W);
+    const T qz0 = p.QZ[cell_], w0 = p.WM[cell_];
+    const T X = A * (__ldg(ZZ + P) - __ldg(ZZ - 2 * P) + __ldg(XZ + 2) - __ldg(XZ - 1))
+              + B * (__ldg(ZZ) - __ldg(ZZ - P) + __ldg(XZ + 1) - __ldg(XZ));
+    const T Pp = A * (__ldg(PR + P) - __ldg(PR - 2 * P)) + B * (__ldg(PR) - __ldg(PR - P));
+    p.QZ[cell_] = E * qz0 - R1 * X - R2 * Pp;
+    p.WM[cell_] = w0 + Cw * qz0 + R1w * X + R3w * Pp;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Stencil neighbours are read through a reader: rd(f, I, L) returns input
@@ -293,9 +385,13 @@ __global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Pa
   const int I = p.PMLL + (int)(blockIdx.x * kBX + threadIdx.x);
   const int L = (int)(blockIdx.y * kBZ + threadIdx.y);
   if (I <= p.PMLXH && L <= p.PMLZH && (!SI || L >= 2)) {
-    const int it = *p.it_base + it_off;
-    const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
-    stress_cell<T, SI, MODE>(p, rd, I, L, it);
+    if (stress_fast_warp(p, I, L)) {
+      stress_interior<T, MODE>(p, I, L);
+    } else {
+      const int it = *p.it_base + it_off;
+      const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
+      stress_cell<T, SI, MODE>(p, rd, I, L, it);
+    }
   }
   if (SI && blockIdx.y == 0) {
     __syncthreads();  // rows 2..4 of this block are final
@@ -565,8 +661,12 @@ __global__ void __launch_bounds__(kBX * kBZ) k_velocity(const __grid_constant__ 
     old[k][2][tx] = FDP_F(p.QX, I, L); old[k][3][tx] = FDP_F(p.QZ, I, L);
   }
   if (inx && L >= (SI ? 2 : 0) && L < p.PMLZH) {
-    const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
-    velocity_cell<T, SI, MODE>(p, rd, I, L);
+    if (velocity_fast_warp(p, I, L)) {
+      velocity_interior<T, MODE>(p, I, L);
+    } else {
+      const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
+      velocity_cell<T, SI, MODE>(p, rd, I, L);
+    }
   }
   if (bottom) {
     const bool me = inx && L == p.PMLZH;
