@@ -216,6 +216,8 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   p.AUX = (const T*)c->aux.p;
   for (int k = 0; k < fdp::C_NCOEF; ++k)
     p.cptr[k] = (p.planes && c->src[k] >= 0) ? p.planes + (long long)c->src[k] * p.pstride : nullptr;
+  for (int s = 0; s < 10; ++s)
+    p.bplane[s] = (c->medium_mode == fdp::M_BIOT) ? p.planes + (long long)s * p.pstride : nullptr;
   const T** pr[24] = {&p.ODA_XL, &p.ODB_XL, &p.ODC_XL, &p.ODD_XL, &p.ODA_XH, &p.ODB_XH, &p.ODC_XH, &p.ODD_XH,
                       &p.ODA_ZH, &p.ODB_ZH, &p.ODC_ZH, &p.ODD_ZH,
                       &p.ODA2_XL, &p.ODB2_XL, &p.ODC2_XL, &p.ODD2_XL, &p.ODA2_XH, &p.ODB2_XH, &p.ODC2_XH, &p.ODD2_XH,
@@ -236,8 +238,9 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   p.err = (int*)c->errbuf.p;
 }
 
-dim3 cell_grid(const fdp_ctx* c) {
-  return dim3((c->NX + fdp::kBX - 1) / fdp::kBX, (c->NZ + fdp::kBZ - 1) / fdp::kBZ, 1);
+dim3 cell_grid(const fdp_ctx* c, int kind) {
+  const int rows = fdp::kBZ * (kind == 0 ? fdp::kRZS : fdp::kRZV);  // rows per block
+  return dim3((c->NX + fdp::kBX - 1) / fdp::kBX, (c->NZ + rows - 1) / rows, 1);
 }
 
 int edge_threads(const fdp_ctx* c) { return std::max(c->g.stress_imaging ? c->NX : 0, c->mr); }
@@ -252,16 +255,24 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
   const dim3 tblk(fdp::kTX, 4, 1);
   if (kind == 0 && c->use_tma) fdp::k_stress_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_vel, it_off);
   else if (kind == 1 && c->use_tma) fdp::k_velocity_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_str, it_off);
-  else if (kind == 0) fdp::k_stress<T, SI, MODE><<<cell_grid(c), blk, 0, c->stream>>>(p, it_off);
-  else if (kind == 1) fdp::k_velocity<T, SI, MODE><<<cell_grid(c), blk, 0, c->stream>>>(p, it_off);
+  else if (kind == 0) fdp::k_stress<T, SI, MODE><<<cell_grid(c, 0), blk, 0, c->stream>>>(p, it_off);
+  else if (kind == 1) fdp::k_velocity<T, SI, MODE><<<cell_grid(c, 1), blk, 0, c->stream>>>(p, it_off);
   else fdp::k_edge<T, SI><<<(edge_threads(c) + kBlockX - 1) / kBlockX, kBlockX, 0, c->stream>>>(p, it_off);
   c->launches += 1;
 }
 
 template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
-  const bool si = c->g.stress_imaging != 0, tab = c->medium_mode == fdp::M_TABLE;
-  if (si) tab ? launch_kind<T, true, fdp::M_TABLE>(c, p, kind, it_off) : launch_kind<T, true, fdp::M_PLANES>(c, p, kind, it_off);
-  else tab ? launch_kind<T, false, fdp::M_TABLE>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_PLANES>(c, p, kind, it_off);
+  const bool si = c->g.stress_imaging != 0;
+  switch (c->medium_mode) {
+    case fdp::M_TABLE:
+      si ? launch_kind<T, true, fdp::M_TABLE>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_TABLE>(c, p, kind, it_off);
+      break;
+    case fdp::M_BIOT:
+      si ? launch_kind<T, true, fdp::M_BIOT>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_BIOT>(c, p, kind, it_off);
+      break;
+    default:
+      si ? launch_kind<T, true, fdp::M_PLANES>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_PLANES>(c, p, kind, it_off);
+  }
 }
 
 template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_off) {
@@ -398,7 +409,12 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
   }
   c->nplanes = (int)plane_col.size();
   const bool table_mode = c->nplanes > 0 && jmnum <= kMaxTableMaterials;
-  c->medium_mode = table_mode ? fdp::M_TABLE : fdp::M_PLANES;
+  // Biot relations: ten distinct planes, in first-occurrence order equal to
+  // the slot order, and every column on its slot with its sign
+  bool biot = !table_mode && c->nplanes == 10;
+  for (int k = 0; k < fdp::C_AUXW && biot; ++k)
+    biot = c->src[k] == fdp::biot_slot(k) && (c->neg[k] != 0) == fdp::biot_neg(k);
+  c->medium_mode = table_mode ? fdp::M_TABLE : biot ? fdp::M_BIOT : fdp::M_PLANES;
   const size_t cells = (size_t)c->rows_alloc * c->pitch;
   if (table_mode) {
     // JM into the padded field layout (padding holds material 1) and the table
@@ -716,8 +732,9 @@ int fdp_medium_info(fdp_ctx* c, int32_t* mode, int32_t* planes_stress, int32_t* 
     return n;
   };
   *mode = c->medium_mode;
-  *planes_stress = c->medium_mode == fdp::M_PLANES ? count(fdp::C_MU, fdp::C_P3) : 0;
-  *planes_velocity = c->medium_mode == fdp::M_PLANES ? count(fdp::C_EQX, fdp::C_R3W) : 0;
+  const bool planes = c->medium_mode != fdp::M_TABLE;
+  *planes_stress = planes ? count(fdp::C_MU, fdp::C_P3) : 0;
+  *planes_velocity = planes ? count(fdp::C_EQX, fdp::C_R3W) : 0;
   return FDP_OK;
 }
 
@@ -784,6 +801,370 @@ void fdp_destroy(fdp_ctx* c) {
   for (auto& a : c->mem) if (a.p) cudaFree(a.p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched shots (fdp_batch_*): many prepared contexts advanced together.
+// Shots are grouped by free-surface mode and medium representation (the
+// template parameters of the kernels); each level is one launch per phase
+// per group, and runs of kChunk levels are replayed from a CUDA graph.
+
+struct BatchGroup {
+  bool si = false;
+  int mode = 0;
+  int first_shot = 0, n = 0;  // shots [first_shot, first_shot + n) of the sorted order
+  int items[3] = {0, 0, 0};   // stress, velocity, edge items at the current m
+  int resident[3] = {0, 0, 0};  // CTAs of each kernel one SM holds
+};
+
+struct fdp_batch {
+  std::vector<fdp_ctx*> shots;  // sorted by group
+  std::vector<BatchGroup> groups;
+  int prec = 4, device = 0;
+  cudaStream_t stream = nullptr;
+  DevArr params, first, itbase;  // Params[shots]; per group [3][n+1] first items
+  int m = 0, waves = 0;          // units per item; persistent CTAs per resident slot (0: one CTA per item)
+  bool tuned = false;            // shape fixed (by the caller or by tuning)
+  int sms = 0;
+  cudaGraphExec_t graph = nullptr;
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int bfail(fdp_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf; else g_create_error = buf;
+  return code;
+}
+
+#define BCK(b, call)                                                                        \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) return bfail((b), FDP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// first-item offsets of group g inside b->first
+size_t group_first_offset(const fdp_batch* b, size_t g) {
+  size_t off = 0;
+  for (size_t k = 0; k < g; ++k) off += (size_t)3 * (b->groups[k].n + 1);
+  return off;
+}
+
+// Items of each phase per shot at m units per item; uploads the queues.
+int batch_queue(fdp_batch* b) {
+  std::vector<int> first;
+  for (BatchGroup& G : b->groups) {
+    for (int ph = 0; ph < 3; ++ph) {
+      int acc = 0;
+      for (int s = 0; s < G.n; ++s) {
+        const fdp_ctx* c = b->shots[G.first_shot + s];
+        first.push_back(acc);
+        if (ph < 2) {
+          const int rows = fdp::kBZ * (ph == 0 ? fdp::kRZS : fdp::kRZV);
+          const int gx = (c->NX + fdp::kBX - 1) / fdp::kBX, gy = (c->NZ + rows - 1) / rows;
+          acc += gx * ((gy + b->m - 1) / b->m);
+        } else {
+          acc += (edge_threads(c) + fdp::kBX * fdp::kBZ - 1) / (fdp::kBX * fdp::kBZ);
+        }
+      }
+      first.push_back(acc);
+      G.items[ph] = acc;
+    }
+  }
+  cudaError_t e = cudaMemcpyAsync(b->first.p, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bfail(b, FDP_ERR_CUDA, "batch queue upload: %s", cudaGetErrorString(e));
+  return FDP_OK;
+}
+
+template <class T, bool SI, int MODE> int group_occupancy(fdp_batch* b, BatchGroup& G) {
+  const int threads = fdp::kBX * fdp::kBZ;
+  BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[0], fdp::k_stress_batch<T, SI, MODE>, threads, 0));
+  BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[1], fdp::k_velocity_batch<T, SI, MODE>, threads, 0));
+  BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[2], fdp::k_edge_batch<T, SI>, threads, 0));
+  return FDP_OK;
+}
+
+template <class T> int group_occupancy_any(fdp_batch* b, BatchGroup& G) {
+  switch (G.mode) {
+    case fdp::M_TABLE: return G.si ? group_occupancy<T, true, fdp::M_TABLE>(b, G) : group_occupancy<T, false, fdp::M_TABLE>(b, G);
+    case fdp::M_BIOT: return G.si ? group_occupancy<T, true, fdp::M_BIOT>(b, G) : group_occupancy<T, false, fdp::M_BIOT>(b, G);
+    default: return G.si ? group_occupancy<T, true, fdp::M_PLANES>(b, G) : group_occupancy<T, false, fdp::M_PLANES>(b, G);
+  }
+}
+
+int group_grid(const fdp_batch* b, const BatchGroup& G, int kind) {
+  const int items = G.items[kind];
+  if (b->waves <= 0) return std::max(items, 1);
+  return std::max(1, std::min(items, b->waves * G.resident[kind] * b->sms));
+}
+
+template <class T, bool SI, int MODE> void group_level(fdp_batch* b, size_t g, int it_off) {
+  const BatchGroup& G = b->groups[g];
+  const size_t psize = sizeof(Params<T>);
+  const fdp::BatchQueue q{(const char*)b->params.p + psize * G.first_shot,
+                          (const int*)b->first.p + group_first_offset(b, g), G.n, b->m};
+  const dim3 blk(fdp::kBX, fdp::kBZ, 1);
+  fdp::k_stress_batch<T, SI, MODE><<<group_grid(b, G, 0), blk, 0, b->stream>>>(q, G.items[0], it_off);
+  fdp::k_velocity_batch<T, SI, MODE><<<group_grid(b, G, 1), blk, 0, b->stream>>>(q, G.items[1], it_off);
+  b->launches += 2;
+  if (G.items[2] > 0) {
+    fdp::k_edge_batch<T, SI><<<group_grid(b, G, 2), blk, 0, b->stream>>>(q, G.items[2], it_off);
+    b->launches += 1;
+  }
+}
+
+template <class T> void batch_level(fdp_batch* b, int it_off) {
+  for (size_t g = 0; g < b->groups.size(); ++g) {
+    const BatchGroup& G = b->groups[g];
+    switch (G.mode) {
+      case fdp::M_TABLE: G.si ? group_level<T, true, fdp::M_TABLE>(b, g, it_off) : group_level<T, false, fdp::M_TABLE>(b, g, it_off); break;
+      case fdp::M_BIOT: G.si ? group_level<T, true, fdp::M_BIOT>(b, g, it_off) : group_level<T, false, fdp::M_BIOT>(b, g, it_off); break;
+      default: G.si ? group_level<T, true, fdp::M_PLANES>(b, g, it_off) : group_level<T, false, fdp::M_PLANES>(b, g, it_off);
+    }
+  }
+}
+
+int batch_launches_per_level(const fdp_batch* b) {
+  int n = 0;
+  for (const BatchGroup& G : b->groups) n += 2 + (G.items[2] > 0 ? 1 : 0);
+  return n;
+}
+
+// Runs levels [it, it + n) directly (no graph), starting the level counter at it.
+template <class T> int batch_direct(fdp_batch* b, int it, int n) {
+  fdp::k_set_base<<<1, 1, 0, b->stream>>>((int*)b->itbase.p, it);
+  b->launches += 1;
+  for (int k = 0; k < n; ++k) batch_level<T>(b, k);
+  BCK(b, cudaGetLastError());
+  return FDP_OK;
+}
+
+int batch_set_shape(fdp_batch* b, int m, int waves) {
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  b->m = m;
+  b->waves = waves;
+  return batch_queue(b);
+}
+
+// Shape tuning on real levels: every candidate computes the same values bit
+// for bit, so the levels spent timing candidates are levels of the run.
+// Sets *used to the number of levels run (0 when the run is too short).
+template <class T> int batch_tune(fdp_batch* b, int it_begin, int it_end, int* used) {
+  static const int kM[] = {1, 2, 4};
+  static const int kWaves[] = {0, 1, 2};
+  const int per = 2;  // levels per candidate
+  *used = 0;
+  const int ncand = (int)(sizeof kM / sizeof kM[0]) * (int)(sizeof kWaves / sizeof kWaves[0]);
+  if (it_end - it_begin + 1 < ncand * per) return FDP_OK;
+  cudaEvent_t e0, e1;
+  BCK(b, cudaEventCreate(&e0));
+  BCK(b, cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bm = b->m, bw = b->waves, it = it_begin, rc = FDP_OK;
+  for (int m : kM) {
+    for (int w : kWaves) {
+      if ((rc = batch_set_shape(b, m, w)) != FDP_OK) break;
+      cudaEventRecord(e0, b->stream);
+      if ((rc = batch_direct<T>(b, it, per)) != FDP_OK) break;
+      cudaEventRecord(e1, b->stream);
+      float ms = 0.f;
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) { rc = bfail(b, FDP_ERR_CUDA, "shape tuning: %s", cudaGetErrorString(e)); break; }
+      if (ms < best) { best = ms; bm = m; bw = w; }
+      it += per;
+    }
+    if (rc != FDP_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != FDP_OK) return rc;
+  *used = it - it_begin;
+  return batch_set_shape(b, bm, bw);
+}
+
+template <class T> int batch_run_t(fdp_batch* b, int it_begin, int it_end) {
+  int it = it_begin;
+  if (!b->tuned) {
+    int used = 0, rc = batch_tune<T>(b, it_begin, it_end, &used);
+    if (rc != FDP_OK) return rc;
+    it += used;
+    b->tuned = used > 0;
+  }
+  if (it > it_end) return FDP_OK;
+  fdp::k_set_base<<<1, 1, 0, b->stream>>>((int*)b->itbase.p, it);
+  b->launches += 1;
+  if (it_end - it + 1 >= kChunk && !b->graph) {
+    cudaGraph_t gr = nullptr;
+    BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = b->launches;
+    for (int k = 0; k < kChunk; ++k) batch_level<T>(b, k);
+    fdp::k_add_base<<<1, 1, 0, b->stream>>>((int*)b->itbase.p, kChunk);
+    b->launches = before;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &gr);
+    if (e != cudaSuccess) return bfail(b, FDP_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) { b->graph = nullptr; return bfail(b, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+  }
+  while (it_end - it + 1 >= kChunk && b->graph) {
+    BCK(b, cudaGraphLaunch(b->graph, b->stream));
+    b->launches += (long long)kChunk * batch_launches_per_level(b) + 1;
+    it += kChunk;
+  }
+  int k = 0;
+  for (; it <= it_end; ++it, ++k) batch_level<T>(b, k);
+  BCK(b, cudaGetLastError());
+  return FDP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
+  if (!shots || !out || n < 1) return bfail(nullptr, FDP_ERR_ARG, "need at least one shot and an output pointer");
+  *out = nullptr;
+  for (int s = 0; s < n; ++s) {
+    const fdp_ctx* c = shots[s];
+    if (!c) return bfail(nullptr, FDP_ERR_ARG, "shot %d is null", s);
+    if (!c->have_medium || !c->have_pml || !c->have_nr || !c->have_source)
+      return bfail(nullptr, FDP_ERR_STATE, "shot %d: set medium, PML profiles, bottom coefficients and source first", s);
+    if (c->mr > 0 && !c->raw.p) return bfail(nullptr, FDP_ERR_STATE, "shot %d: receiver buffer missing", s);
+    for (int t = 0; t < s; ++t)
+      if (shots[t] == c) return bfail(nullptr, FDP_ERR_ARG, "shot %d appears twice", s);
+    if (c->prec != shots[0]->prec || c->g.device != shots[0]->g.device)
+      return bfail(nullptr, FDP_ERR_UNSUPPORTED, "shot %d differs from shot 0 in precision or device", s);
+  }
+  fdp_batch* b = new fdp_batch();
+  b->prec = shots[0]->prec;
+  b->device = shots[0]->g.device;
+  // group by (free-surface mode, medium representation), keeping the order within a group
+  for (int si = 0; si < 2; ++si)
+    for (int mode : {fdp::M_TABLE, fdp::M_PLANES, fdp::M_BIOT}) {
+      BatchGroup G;
+      G.si = si != 0;
+      G.mode = mode;
+      G.first_shot = (int)b->shots.size();
+      for (int s = 0; s < n; ++s)
+        if ((shots[s]->g.stress_imaging != 0) == G.si && shots[s]->medium_mode == mode) b->shots.push_back(shots[s]);
+      G.n = (int)b->shots.size() - G.first_shot;
+      if (G.n > 0) b->groups.push_back(G);
+    }
+  auto bail = [&](int rc) {
+    if (!b->err.empty()) g_create_error = b->err;
+    fdp_batch_destroy(b);
+    return rc;
+  };
+  int rc;
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+  if (e != cudaSuccess) return bail(bfail(b, FDP_ERR_CUDA, "batch stream: %s", cudaGetErrorString(e)));
+  for (fdp_ctx* c : b->shots) cudaStreamSynchronize(c->stream);
+  const size_t psize = b->prec == 8 ? sizeof(Params<double>) : sizeof(Params<float>);
+  auto alloc = [&](DevArr& a, size_t bytes) -> int {
+    cudaError_t err = cudaMalloc(&a.p, bytes);
+    if (err != cudaSuccess) return bfail(b, FDP_ERR_ALLOC, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(err));
+    a.bytes = bytes;
+    return FDP_OK;
+  };
+  if ((rc = alloc(b->params, psize * n)) || (rc = alloc(b->first, sizeof(int) * 3 * (n + b->groups.size()))) ||
+      (rc = alloc(b->itbase, sizeof(int))))
+    return bail(rc);
+  std::vector<unsigned char> host(psize * n);
+  for (int s = 0; s < n; ++s) {
+    if (b->prec == 8) {
+      Params<double> p;
+      fill_params<double>(b->shots[s], p);
+      p.it_base = (const int*)b->itbase.p;
+      std::memcpy(&host[psize * s], &p, psize);
+    } else {
+      Params<float> p;
+      fill_params<float>(b->shots[s], p);
+      p.it_base = (const int*)b->itbase.p;
+      std::memcpy(&host[psize * s], &p, psize);
+    }
+  }
+  e = cudaMemcpyAsync(b->params.p, host.data(), host.size(), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bail(bfail(b, FDP_ERR_CUDA, "batch parameters: %s", cudaGetErrorString(e)));
+  for (BatchGroup& G : b->groups)
+    if ((rc = (b->prec == 8 ? group_occupancy_any<double>(b, G) : group_occupancy_any<float>(b, G))) != FDP_OK)
+      return bail(rc);
+  if ((rc = batch_set_shape(b, 2, 1)) != FDP_OK) return bail(rc);
+  *out = b;
+  return FDP_OK;
+}
+
+int fdp_batch_set_shape(fdp_batch* b, int32_t units_per_item, int32_t waves) {
+  if (!b) return bfail(b, FDP_ERR_ARG, "null batch");
+  if (units_per_item == 0) {  // tune again on the next run
+    b->tuned = false;
+    return FDP_OK;
+  }
+  if (units_per_item < 1 || units_per_item > 64 || waves < 0 || waves > 64)
+    return bfail(b, FDP_ERR_ARG, "units per item must be 1..64 and waves 0..64");
+  BCK(b, cudaSetDevice(b->device));
+  BCK(b, cudaStreamSynchronize(b->stream));
+  b->tuned = true;
+  return batch_set_shape(b, units_per_item, waves);
+}
+
+int fdp_batch_get_shape(fdp_batch* b, int32_t* units_per_item, int32_t* waves) {
+  if (!b || !units_per_item || !waves) return bfail(b, FDP_ERR_ARG, "null argument");
+  *units_per_item = b->m;
+  *waves = b->waves;
+  return FDP_OK;
+}
+
+int fdp_batch_run(fdp_batch* b, int32_t it_begin, int32_t it_end) {
+  if (!b) return bfail(b, FDP_ERR_ARG, "null batch");
+  if (it_end < it_begin) return FDP_OK;
+  for (size_t s = 0; s < b->shots.size(); ++s)
+    if (it_begin < 1 || it_end > b->shots[s]->mt2)
+      return bfail(b, FDP_ERR_ARG, "levels %d..%d outside 1..MT2=%d of a shot", it_begin, it_end, b->shots[s]->mt2);
+  BCK(b, cudaSetDevice(b->device));
+  const int rc = b->prec == 8 ? batch_run_t<double>(b, it_begin, it_end) : batch_run_t<float>(b, it_begin, it_end);
+  if (rc == FDP_OK)
+    for (fdp_ctx* c : b->shots) c->last_it = std::max(c->last_it, (int)it_end);
+  return rc;
+}
+
+int fdp_batch_synchronize(fdp_batch* b) {
+  if (!b) return bfail(b, FDP_ERR_ARG, "null batch");
+  BCK(b, cudaStreamSynchronize(b->stream));
+  for (fdp_ctx* c : b->shots)
+    if (int rc = device_status(c)) return bfail(b, rc, "%s", c->err.c_str());
+  return FDP_OK;
+}
+
+int64_t fdp_batch_kernel_launches(fdp_batch* b) { return b ? b->launches : 0; }
+
+int fdp_batch_get_stream(fdp_batch* b, void** stream) {
+  if (!b || !stream) return bfail(b, FDP_ERR_ARG, "null argument");
+  *stream = (void*)b->stream;
+  return FDP_OK;
+}
+
+const char* fdp_batch_last_error(const fdp_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+void fdp_batch_destroy(fdp_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (DevArr* a : {&b->params, &b->first, &b->itbase}) if (a->p) cudaFree(a->p);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
 }
 
 }  // extern "C"

@@ -50,9 +50,48 @@ enum Coef {
 constexpr int kPadX = 4;
 constexpr int kPadZ = 2;
 constexpr int kBX = 32;  // block width (cells along x)
-constexpr int kBZ = 8;   // block height (rows)
+// Launch shape of k_stress / k_velocity, fixed at build time: threads per
+// block kBX x kBZ and rows per thread kRZS (stress) and kRZV (velocity).
+// Measured on the layered 2048^2 workload (FP32, per-cell Biot planes):
+// one row per thread suits the stress phase (40 registers, 75 % occupancy),
+// four rows with a register window suit the velocity phase, with its
+// registers capped at three FP32 blocks (two FP64 blocks) per SM.
+#ifndef FDP_KBZ
+#define FDP_KBZ 8
+#endif
+#ifndef FDP_KRZS
+#define FDP_KRZS 1
+#endif
+#ifndef FDP_KRZV
+#define FDP_KRZV 4
+#endif
+#ifndef FDP_MIN_BLOCKS_F32
+#define FDP_MIN_BLOCKS_F32 3
+#endif
+#ifndef FDP_MIN_BLOCKS_F64
+#define FDP_MIN_BLOCKS_F64 2
+#endif
+constexpr int kBZ = FDP_KBZ;  // block height (threads along z)
+constexpr int kRZS = FDP_KRZS;
+constexpr int kRZV = FDP_KRZV;
+#define FDP_VELOCITY_BOUNDS(T) __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? FDP_MIN_BLOCKS_F32 : FDP_MIN_BLOCKS_F64)
+static_assert(kBZ * kRZS >= 5, "the first block row of k_stress must hold rows 0..4");
 
-enum MediumMode { M_TABLE = 0, M_PLANES = 1 };
+enum MediumMode { M_TABLE = 0, M_PLANES = 1, M_BIOT = 2 };
+
+// Plane mode whose columns follow Biot's relations (M_BIOT): five planes per
+// phase, with the aliases resolved at compile time.  Slots 0..4 are the
+// stress planes MU, SIG_XX_1 (= SIG_ZZ_2), SIG_XX_2 (= SIG_ZZ_1),
+// SIG_XX_3 (= SIG_ZZ_3 = -PRES_1 = -PRES_2), PRES_3; slots 5..9 the velocity
+// planes EXP(-REL3_Q), the drag factor, REL1_Q (= REL3_U), REL2_Q, REL1_U.
+// The host selects this mode only after checking, column by column, that
+// the medium's derived coefficients have exactly these equalities.
+__host__ __device__ constexpr int biot_slot(int k) {
+  return k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 2 : k == 3 ? 3 : k == 4 ? 2 : k == 5 ? 1 : k == 6 ? 3 : k == 7 ? 3
+       : k == 8 ? 3 : k == 9 ? 4 : k == 10 ? 5 : k == 11 ? 6 : k == 12 ? 7 : k == 13 ? 8 : k == 14 ? 9
+       : k == 15 ? 7 : k == 16 ? 5 : k == 17 ? 6 : k == 18 ? 7 : k == 19 ? 8 : k == 20 ? 9 : k == 21 ? 7 : -1;
+}
+__host__ __device__ constexpr bool biot_neg(int k) { return k == 7 || k == 8; }
 
 template <class T> struct Params {
   int MX, MZ, TPML, PMLL, PMLXH, PMLZH, NX, NZ, MX1, LIN_X, LIN_Z;
@@ -68,6 +107,7 @@ template <class T> struct Params {
   const T* planes;
   long long pstride;
   const T* cptr[C_NCOEF];  // plane of coefficient k at (PMLL, 0), or null when constant
+  const T* bplane[10];     // M_BIOT: the plane of each slot at (PMLL, 0)
   int src[C_NCOEF];
   int neg[C_NCOEF];
   T cval[C_NCOEF];
@@ -107,6 +147,10 @@ template <class T> struct Params {
 template <class T, int MODE>
 __device__ __forceinline__ T coef(const Params<T>& p, int k, long long cell, int J) {
   if (MODE == M_TABLE) return __ldg(p.coef + (long long)k * p.cld + J);
+  if (MODE == M_BIOT) {
+    const T v = __ldg(p.bplane[biot_slot(k)] + cell);
+    return biot_neg(k) ? -v : v;
+  }
   const T* c = p.cptr[k];
   if (!c) return p.cval[k];
   const T v = __ldg(c + cell);
@@ -115,93 +159,155 @@ __device__ __forceinline__ T coef(const Params<T>& p, int k, long long cell, int
 #define FDP_C(k) coef<T, MODE>(p, (k), cell_, J_)
 
 // ---------------------------------------------------------------------------
-// Interior fast paths.  A warp is 32 consecutive cells of one row; when the
-// row is an interior row (2..MZ-2, not the source row) and all 32 columns
-// lie where every stencil of the phase is the 4th-order one, the warp runs
-// these straight-line versions of the interior branches of stress_cell /
-// velocity_cell (same expressions, same order) without region tests.
+// Interior fast paths.  A thread of k_stress (k_velocity) updates kRZS
+// (kRZV) consecutive rows of one column, and a warp 32 consecutive columns
+// of those rows.  When every row is an interior row (2..MZ-2, not the source row) and
+// all 32 columns lie where every stencil of the phase is the 4th-order one,
+// the warp runs these straight-line versions of the interior branches of
+// stress_cell / velocity_cell (same expressions, same order) without region
+// tests.  The column's values that the z stencils of those rows share are
+// loaded once, into a window of kRZS + 3 (kRZV + 3) registers per field.
 
 // stress: EXX needs 3 <= I <= MX-2 (strain_uw_xx.F90:69); EXZ, EZZ, the
 // stresses cover that range
 template <class T>
-__device__ __forceinline__ bool stress_fast_warp(const Params<T>& p, int I, int L) {
+__device__ __forceinline__ bool stress_fast_rows(const Params<T>& p, int I, int L0) {
   const int I0 = I - (int)(threadIdx.x & 31);
-  return L >= 2 && L <= p.MZ - 2 && L != p.LIN_Z && I0 >= 3 && I0 + 31 <= p.MX - 2;
+  const int L1 = L0 + kRZS - 1;
+  return L0 >= 2 && L1 <= p.MZ - 2 && (p.LIN_Z < L0 || p.LIN_Z > L1) && I0 >= 3 && I0 + 31 <= p.MX - 2;
 }
 
 template <class T, int MODE>
-__device__ __forceinline__ void stress_interior(const Params<T>& p, int I, int L) {
-  const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
-  const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+__device__ __forceinline__ void stress_interior_rows(const Params<T>& p, int I, int L0) {
   const long long P = p.pitch;
-  const T* U = p.UM + cell_;
-  const T* W = p.WM + cell_;
-  const T* X = p.QX + cell_;
-  const T* Z = p.QZ + cell_;
-  // strain_uw_xz.F90:201-204
-  const T exz = p.AH * (__ldg(U + P) - __ldg(U - 2 * P) + __ldg(W + 1) - __ldg(W - 2))
-              + p.BH * (__ldg(U) - __ldg(U - P) + __ldg(W) - __ldg(W - 1));
-  // strain_uw_zz.F90:43,49 and strain_q_zz.F90:43,49
-  T ezz = (p.CH * (__ldg(W + P) - __ldg(W)));
-  ezz = p.AH * (__ldg(W + 2 * P) - __ldg(W - P)) + p.BC * ezz;
-  T qzz = (p.CH * (__ldg(Z + P) - __ldg(Z)));
-  qzz = p.AH * (__ldg(Z + 2 * P) - __ldg(Z - P)) + p.BC * qzz;
-  // strain_uw_xx.F90:71-72 and strain_q_xx.F90:70-71
-  const T exx = p.AH * (__ldg(U + 2) - __ldg(U - 1)) + p.BH * (__ldg(U + 1) - __ldg(U));
-  const T qxx = p.AH * (__ldg(X + 2) - __ldg(X - 1)) + p.BH * (__ldg(X + 1) - __ldg(X));
-  // stress_xz.F90:44-46 and stress_nn.F90:53-59
-  const T TXZv = FDP_C(C_MU) * exz;
-  p.TXZ[cell_] = p.TXZ[cell_] + p.DTE * TXZv;
-  const T s1 = FDP_C(C_SXX1), s2 = FDP_C(C_SXX2), s3 = FDP_C(C_SXX3);
-  const T z1 = FDP_C(C_SZZ1), z2 = FDP_C(C_SZZ2), z3 = FDP_C(C_SZZ3);
-  const T q1 = FDP_C(C_P1), q2 = FDP_C(C_P2), q3 = FDP_C(C_P3);
-  const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
-  const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
-  const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
-  p.TXX[cell_] = p.TXX[cell_] + p.DTE * TXXv;
-  p.TZZ[cell_] = p.TZZ[cell_] + p.DTE * TZZv;
-  p.PRES[cell_] = p.PRES[cell_] + p.DTE * PRv;
+  const long long c0 = (long long)L0 * P + (I - p.PMLL);
+  const T* U = p.UM + c0;
+  const T* W = p.WM + c0;
+  const T* X = p.QX + c0;
+  const T* Z = p.QZ + c0;
+  // u[k] = U(I, L0-2+k); w[k], z[k] = W, QZ(I, L0-1+k)
+  T u[kRZS + 3], w[kRZS + 3], z[kRZS + 3];
+#pragma unroll
+  for (int k = 0; k < kRZS + 3; ++k) {
+    u[k] = __ldg(U + (k - 2) * P);
+    w[k] = __ldg(W + (k - 1) * P);
+    z[k] = __ldg(Z + (k - 1) * P);
+  }
+  // the stresses of all rows; they receive the new values
+  T oxz[kRZS], oxx[kRZS], ozz[kRZS], opr[kRZS];
+#pragma unroll
+  for (int r = 0; r < kRZS; ++r) {
+    oxz[r] = p.TXZ[c0 + r * P]; oxx[r] = p.TXX[c0 + r * P];
+    ozz[r] = p.TZZ[c0 + r * P]; opr[r] = p.PRES[c0 + r * P];
+  }
+#pragma unroll
+  for (int r = 0; r < kRZS; ++r) {
+    const long long cell_ = c0 + r * P;
+    const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+    const T* Ur = U + r * P;
+    const T* Wr = W + r * P;
+    const T* Xr = X + r * P;
+    // strain_uw_xz.F90:201-204
+    const T exz = p.AH * (u[r + 3] - u[r] + __ldg(Wr + 1) - __ldg(Wr - 2))
+                + p.BH * (u[r + 2] - u[r + 1] + w[r + 1] - __ldg(Wr - 1));
+    // strain_uw_zz.F90:43,49 and strain_q_zz.F90:43,49
+    T ezz = (p.CH * (w[r + 2] - w[r + 1]));
+    ezz = p.AH * (w[r + 3] - w[r]) + p.BC * ezz;
+    T qzz = (p.CH * (z[r + 2] - z[r + 1]));
+    qzz = p.AH * (z[r + 3] - z[r]) + p.BC * qzz;
+    // strain_uw_xx.F90:71-72 and strain_q_xx.F90:70-71
+    const T exx = p.AH * (__ldg(Ur + 2) - __ldg(Ur - 1)) + p.BH * (__ldg(Ur + 1) - u[r + 2]);
+    const T qxx = p.AH * (__ldg(Xr + 2) - __ldg(Xr - 1)) + p.BH * (__ldg(Xr + 1) - __ldg(Xr));
+    // stress_xz.F90:44-46 and stress_nn.F90:53-59
+    const T TXZv = FDP_C(C_MU) * exz;
+    oxz[r] = oxz[r] + p.DTE * TXZv;
+    const T s1 = FDP_C(C_SXX1), s2 = FDP_C(C_SXX2), s3 = FDP_C(C_SXX3);
+    const T z1 = FDP_C(C_SZZ1), z2 = FDP_C(C_SZZ2), z3 = FDP_C(C_SZZ3);
+    const T q1 = FDP_C(C_P1), q2 = FDP_C(C_P2), q3 = FDP_C(C_P3);
+    const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
+    const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
+    const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
+    oxx[r] = oxx[r] + p.DTE * TXXv;
+    ozz[r] = ozz[r] + p.DTE * TZZv;
+    opr[r] = opr[r] + p.DTE * PRv;
+  }
+  // every load above precedes every store (a load may not pass a store
+  // to memory it could alias, so interleaving would serialise the rows)
+#pragma unroll
+  for (int r = 0; r < kRZS; ++r) {
+    p.TXZ[c0 + r * P] = oxz[r]; p.TXX[c0 + r * P] = oxx[r];
+    p.TZZ[c0 + r * P] = ozz[r]; p.PRES[c0 + r * P] = opr[r];
+  }
 }
 
 // velocity: qx and u need 4 <= I <= MX-2 (inh_qx_int.F90:40); qz and w
 // (3..MX-2) cover that range
 template <class T>
-__device__ __forceinline__ bool velocity_fast_warp(const Params<T>& p, int I, int L) {
+__device__ __forceinline__ bool velocity_fast_rows(const Params<T>& p, int I, int L0) {
   const int I0 = I - (int)(threadIdx.x & 31);
-  return L >= 2 && L <= p.MZ - 2 && I0 >= 4 && I0 + 31 <= p.MX - 2;
+  return L0 >= 2 && L0 + kRZV - 1 <= p.MZ - 2 && I0 >= 4 && I0 + 31 <= p.MX - 2;
 }
 
 template <class T, int MODE>
-__device__ __forceinline__ void velocity_interior(const Params<T>& p, int I, int L) {
-  const long long cell_ = (long long)L * p.pitch + (I - p.PMLL);
-  const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+__device__ __forceinline__ void velocity_interior_rows(const Params<T>& p, int I, int L0) {
   const long long P = p.pitch;
+  const long long c0 = (long long)L0 * P + (I - p.PMLL);
   const T A = p.A, B = p.B;
-  const T* XX = p.TXX + cell_;
-  const T* ZZ = p.TZZ + cell_;
-  const T* XZ = p.TXZ + cell_;
-  const T* PR = p.PRES + cell_;
-  {
-    // inh_qx_int.F90:44-52 and inh_v_uv_int.F90:45-54
-    const T E = FDP_C(C_EQX), Cu = FDP_C(C_CU);
-    const T R1 = FDP_C(C_R1QX), R2 = FDP_C(C_R2QX), R1u = FDP_C(C_R1U), R3u = FDP_C(C_R3U);
-    const T qx0 = p.QX[cell_], u0 = p.UM[cell_];
-    const T X = A * (__ldg(XX + 1) - __ldg(XX - 2) + __ldg(XZ + 2 * P) - __ldg(XZ - P))
-              + B * (__ldg(XX) - __ldg(XX - 1) + __ldg(XZ + P) - __ldg(XZ));
-    const T Pp = A * (__ldg(PR + 1) - __ldg(PR - 2)) + B * (__ldg(PR) - __ldg(PR - 1));
-    p.QX[cell_] = E * qx0 - R1 * X - R2 * Pp;
-    p.UM[cell_] = u0 + Cu * qx0 + R1u * X + R3u * Pp;
+  const T* XX = p.TXX + c0;
+  const T* ZZ = p.TZZ + c0;
+  const T* XZ = p.TXZ + c0;
+  const T* PR = p.PRES + c0;
+  // xz[k] = TXZ(I, L0-1+k); zz[k], pr[k] = TZZ, PRES(I, L0-2+k)
+  T xz[kRZV + 3], zz[kRZV + 3], pr[kRZV + 3];
+#pragma unroll
+  for (int k = 0; k < kRZV + 3; ++k) {
+    xz[k] = __ldg(XZ + (k - 1) * P);
+    zz[k] = __ldg(ZZ + (k - 2) * P);
+    pr[k] = __ldg(PR + (k - 2) * P);
   }
-  {
-    // inh_qz_int.F90:45-53 and inh_v_w_int.F90:47-56
-    const T E = FDP_C(C_EQZ), Cw = FDP_C(C_CW);
-    const T R1 = FDP_C(C_R1QZ), R2 = FDP_C(C_R2QZ), R1w = FDP_C(C_R1W), R3w = FDP_C(C_R3W);
-    const T qz0 = p.QZ[cell_], w0 = p.WM[cell_];
-    const T X = A * (__ldg(ZZ + P) - __ldg(ZZ - 2 * P) + __ldg(XZ + 2) - __ldg(XZ - 1))
-              + B * (__ldg(ZZ) - __ldg(ZZ - P) + __ldg(XZ + 1) - __ldg(XZ));
-    const T Pp = A * (__ldg(PR + P) - __ldg(PR - 2 * P)) + B * (__ldg(PR) - __ldg(PR - P));
-    p.QZ[cell_] = E * qz0 - R1 * X - R2 * Pp;
-    p.WM[cell_] = w0 + Cw * qz0 + R1w * X + R3w * Pp;
+  // the velocities of all rows; they receive the new values
+  T oqx[kRZV], oum[kRZV], oqz[kRZV], owm[kRZV];
+#pragma unroll
+  for (int r = 0; r < kRZV; ++r) {
+    oqx[r] = p.QX[c0 + r * P]; oum[r] = p.UM[c0 + r * P];
+    oqz[r] = p.QZ[c0 + r * P]; owm[r] = p.WM[c0 + r * P];
+  }
+#pragma unroll
+  for (int r = 0; r < kRZV; ++r) {
+    const long long cell_ = c0 + r * P;
+    const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+    const T* XXr = XX + r * P;
+    const T* XZr = XZ + r * P;
+    const T* PRr = PR + r * P;
+    {
+      // inh_qx_int.F90:44-52 and inh_v_uv_int.F90:45-54
+      const T E = FDP_C(C_EQX), Cu = FDP_C(C_CU);
+      const T R1 = FDP_C(C_R1QX), R2 = FDP_C(C_R2QX), R1u = FDP_C(C_R1U), R3u = FDP_C(C_R3U);
+      const T qx0 = oqx[r], u0 = oum[r];
+      const T X = A * (__ldg(XXr + 1) - __ldg(XXr - 2) + xz[r + 3] - xz[r])
+                + B * (__ldg(XXr) - __ldg(XXr - 1) + xz[r + 2] - xz[r + 1]);
+      const T Pp = A * (__ldg(PRr + 1) - __ldg(PRr - 2)) + B * (pr[r + 2] - __ldg(PRr - 1));
+      oqx[r] = E * qx0 - R1 * X - R2 * Pp;
+      oum[r] = u0 + Cu * qx0 + R1u * X + R3u * Pp;
+    }
+    {
+      // inh_qz_int.F90:45-53 and inh_v_w_int.F90:47-56
+      const T E = FDP_C(C_EQZ), Cw = FDP_C(C_CW);
+      const T R1 = FDP_C(C_R1QZ), R2 = FDP_C(C_R2QZ), R1w = FDP_C(C_R1W), R3w = FDP_C(C_R3W);
+      const T qz0 = oqz[r], w0 = owm[r];
+      const T X = A * (zz[r + 3] - zz[r] + __ldg(XZr + 2) - __ldg(XZr - 1))
+                + B * (zz[r + 2] - zz[r + 1] + __ldg(XZr + 1) - xz[r + 1]);
+      const T Pp = A * (pr[r + 3] - pr[r]) + B * (pr[r + 2] - pr[r + 1]);
+      oqz[r] = E * qz0 - R1 * X - R2 * Pp;
+      owm[r] = w0 + Cw * qz0 + R1w * X + R3w * Pp;
+    }
+  }
+  // every load above precedes every store (a load may not pass a store
+  // to memory it could alias, so interleaving would serialise the rows)
+#pragma unroll
+  for (int r = 0; r < kRZV; ++r) {
+    p.QX[c0 + r * P] = oqx[r]; p.UM[c0 + r * P] = oum[r];
+    p.QZ[c0 + r * P] = oqz[r]; p.WM[c0 + r * P] = owm[r];
   }
 }
 
@@ -377,24 +483,26 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
   }
 }
 
-// One thread per cell; blocks tile the grid from row 0 down, so the block
-// row holding rows 0..7 also holds rows 2..4 that the stress-imaging mirror
-// rows 0 and 1 copy.
+// One thread per kRZS cells of a column; a unit of kBX x kBZ threads covers
+// kBX columns and kBZ*kRZS rows.  Units tile the grid from row 0 down, so
+// unit row 0 holds rows 2..4 that the stress-imaging mirror rows 0 and 1
+// copy.  (bx, by) is the unit's position; k_stress runs one unit per block,
+// the batched kernels several per block.
 template <class T, bool SI, int MODE>
-__global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Params<T> p, int it_off) {
-  const int I = p.PMLL + (int)(blockIdx.x * kBX + threadIdx.x);
-  const int L = (int)(blockIdx.y * kBZ + threadIdx.y);
-  if (I <= p.PMLXH && L <= p.PMLZH && (!SI || L >= 2)) {
-    if (stress_fast_warp(p, I, L)) {
-      stress_interior<T, MODE>(p, I, L);
-    } else {
-      const int it = *p.it_base + it_off;
-      const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
-      stress_cell<T, SI, MODE>(p, rd, I, L, it);
-    }
+__device__ __forceinline__ void stress_unit(const Params<T>& p, int bx, int by, int it_off) {
+  const int I = p.PMLL + (int)(bx * kBX + threadIdx.x);
+  const int L0 = (int)(by * kBZ + threadIdx.y) * kRZS;  // rows L0 .. L0+kRZS-1
+  if (stress_fast_rows(p, I, L0)) {
+    stress_interior_rows<T, MODE>(p, I, L0);
+  } else if (I <= p.PMLXH) {
+    const int it = *p.it_base + it_off;
+    const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
+#pragma unroll 1
+    for (int L = L0; L < L0 + kRZS; ++L)
+      if (L <= p.PMLZH && (!SI || L >= 2)) stress_cell<T, SI, MODE>(p, rd, I, L, it);
   }
-  if (SI && blockIdx.y == 0) {
-    __syncthreads();  // rows 2..4 of this block are final
+  if (SI && by == 0) {
+    __syncthreads();  // rows 2..4 of this unit are final
     if (I <= p.PMLXH && threadIdx.y == 0) {
       // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53
       FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
@@ -406,6 +514,11 @@ __global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Pa
       FDP_F(p.TXZ, I, 2) = T(0);
     }
   }
+}
+
+template <class T, bool SI, int MODE>
+__global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Params<T> p, int it_off) {
+  stress_unit<T, SI, MODE>(p, (int)blockIdx.x, (int)blockIdx.y, it_off);
 }
 
 // ---------------------------------------------------------------------------
@@ -642,62 +755,62 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
   }
 }
 
-// One thread per cell; blocks tile the grid from row PMLZH up, so the block
-// row holding the bottom row also holds rows PMLZH-1 and PMLZH-2, whose new
-// values and pre-phase values (the history SZ of time_loop.F90:133-155) the
-// bottom row needs.
+// One thread per kRZV cells of a column; units of kBX x kBZ threads tile
+// the grid from row PMLZH up, so the thread holding the bottom row also
+// holds rows PMLZH-1 and PMLZH-2, whose new values and pre-phase values (the
+// history SZ of time_loop.F90:133-155) the bottom row needs.  The pre-phase
+// values wait in the thread's own slots of shared memory while it updates
+// those rows.
 template <class T, bool SI, int MODE>
-__global__ void __launch_bounds__(kBX * kBZ) k_velocity(const __grid_constant__ Params<T> p, int it_off) {
-  (void)it_off;
+__device__ __forceinline__ void velocity_unit(const Params<T>& p, int bx, int by) {
+  static_assert(kRZV >= 3, "the bottom row needs two rows above it in the same thread");
   __shared__ T old[3][4][kBX];  // pre-phase values of rows PMLZH-k, k = 0..2
-  const int I = p.PMLL + (int)(blockIdx.x * kBX + threadIdx.x);
-  const int L = p.PMLZH - (int)(blockIdx.y * kBZ + (kBZ - 1 - threadIdx.y));
+  const int I = p.PMLL + (int)(bx * kBX + threadIdx.x);
+  const int L1 = p.PMLZH - (int)(by * kBZ + (kBZ - 1 - threadIdx.y)) * kRZV;  // last row
+  const int L0 = L1 - kRZV + 1;                                                         // first row
   const bool inx = I <= p.PMLXH;
-  const bool bottom = (blockIdx.y == 0);
+  const bool me = inx && L1 == p.PMLZH;  // this thread updates the bottom row
   const int tx = threadIdx.x;
-  if (bottom && inx && L >= p.PMLZH - 2) {
-    const int k = p.PMLZH - L;
-    old[k][0][tx] = FDP_F(p.UM, I, L); old[k][1][tx] = FDP_F(p.WM, I, L);
-    old[k][2][tx] = FDP_F(p.QX, I, L); old[k][3][tx] = FDP_F(p.QZ, I, L);
-  }
-  if (inx && L >= (SI ? 2 : 0) && L < p.PMLZH) {
-    if (velocity_fast_warp(p, I, L)) {
-      velocity_interior<T, MODE>(p, I, L);
-    } else {
-      const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
-      velocity_cell<T, SI, MODE>(p, rd, I, L);
+  if (me) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      old[k][0][tx] = FDP_F(p.UM, I, L1 - k); old[k][1][tx] = FDP_F(p.WM, I, L1 - k);
+      old[k][2][tx] = FDP_F(p.QX, I, L1 - k); old[k][3][tx] = FDP_F(p.QZ, I, L1 - k);
     }
   }
-  if (bottom) {
-    const bool me = inx && L == p.PMLZH;
+  if (velocity_fast_rows(p, I, L0)) {
+    velocity_interior_rows<T, MODE>(p, I, L0);
+  } else if (inx) {
+    const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
+#pragma unroll 1
+    for (int L = L0; L <= L1; ++L)
+      if (L >= (SI ? 2 : 0) && L < p.PMLZH) velocity_cell<T, SI, MODE>(p, rd, I, L);
+  }
+  if (me) {
+    // hplane_pmlzh0_velocity.F90:34-63
+    const int LST = p.PMLZH;
     const int x = I - p.PMLL;
-    T sp[4][3];
-    if (me) {
+    T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const T* hist = p.HIST + (long long)c * 3 * p.NX;
-        sp[c][0] = hist[x]; sp[c][1] = hist[p.NX + x]; sp[c][2] = hist[2 * p.NX + x];
-      }
-    }
-    __syncthreads();  // rows PMLZH-1, PMLZH-2 of this block are final
-    if (me) {
-      // hplane_pmlzh0_velocity.F90:34-63
-      const int LST = p.PMLZH;
-      T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
-        T* hist = p.HIST + (long long)c * 3 * p.NX;
-        const T v = ab[0] * FDP_F(f[c], I, LST - 1) + ab[1] * FDP_F(f[c], I, LST - 2)
-                  + ab[2] * old[0][c][tx] + ab[3] * old[1][c][tx] + ab[4] * old[2][c][tx]
-                  + ab[5] * sp[c][0] + ab[6] * sp[c][1] + ab[7] * sp[c][2];
-        FDP_F(f[c], I, LST) = v;
-        hist[x] = old[0][c][tx];
-        hist[p.NX + x] = old[1][c][tx];
-        hist[2 * p.NX + x] = old[2][c][tx];
-      }
+    for (int c = 0; c < 4; ++c) {
+      const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
+      T* hist = p.HIST + (long long)c * 3 * p.NX;
+      const T sp0 = hist[x], sp1 = hist[p.NX + x], sp2 = hist[2 * p.NX + x];
+      const T v = ab[0] * FDP_F(f[c], I, LST - 1) + ab[1] * FDP_F(f[c], I, LST - 2)
+                + ab[2] * old[0][c][tx] + ab[3] * old[1][c][tx] + ab[4] * old[2][c][tx]
+                + ab[5] * sp0 + ab[6] * sp1 + ab[7] * sp2;
+      FDP_F(f[c], I, LST) = v;
+      hist[x] = old[0][c][tx];
+      hist[p.NX + x] = old[1][c][tx];
+      hist[2 * p.NX + x] = old[2][c][tx];
     }
   }
+}
+
+template <class T, bool SI, int MODE>
+__global__ void FDP_VELOCITY_BOUNDS(T) k_velocity(const __grid_constant__ Params<T> p, int it_off) {
+  (void)it_off;
+  velocity_unit<T, SI, MODE>(p, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -728,9 +841,9 @@ __device__ __forceinline__ T final_value(const Params<T>& p, int c, int I, int L
 // Row 1 under stress imaging (threads 0..NX-1) and receiver sampling
 // (threads 0..MR-1).  Sampling recomputes row-1 values instead of reading
 // them, so it does not depend on the order in which threads write row 1.
+// g is the thread's index within the shot.
 template <class T, bool SI>
-__global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> p, int it_off) {
-  const int g = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+__device__ __forceinline__ void edge_thread(const Params<T>& p, int g, int it_off) {
   if (SI) {
     const int I = p.PMLL + g;
     if (I <= p.PMLXH && I >= 3 - p.TPML && I <= p.MX - 1 + p.TPML) {
@@ -756,6 +869,104 @@ __global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> 
     T* out = p.RAW + ((long long)(it - 1) * p.MR + g) * 6;
 #pragma unroll
     for (int k = 0; k < 6; ++k) out[k] = s[k];
+  }
+}
+
+template <class T, bool SI>
+__global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> p, int it_off) {
+  edge_thread<T, SI>(p, (int)(blockIdx.x * blockDim.x + threadIdx.x), it_off);
+}
+
+// ---------------------------------------------------------------------------
+// Batched shots.  Every shot of a batch advances one level per launch of
+// each phase.  A phase's work is a queue of items: an item of a cell phase
+// is `m` vertically adjacent units of one shot's grid, an edge item is
+// kBX * kBZ consecutive edge threads of one shot.  Persistent CTAs take the
+// items round-robin and hold the current shot's parameters in shared memory.
+// Shots may differ in grid size, medium, source and receivers, and share
+// precision, free-surface mode and medium representation.
+struct BatchQueue {
+  const void* params;  // Params<T>[n]
+  const int* first;    // [3][n+1]: first item of each shot for stress, velocity, edge
+  int n;               // shots
+  int m;               // units per cell item
+};
+
+// largest s with first[s] <= item (first[0] = 0, first[n] = items)
+__device__ __forceinline__ int batch_shot(const int* first, int n, int item) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(first + mid) <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class T>
+__device__ __forceinline__ void batch_load_params(Params<T>& dst, const BatchQueue& q, int s) {
+  static_assert(sizeof(Params<T>) % 4 == 0, "parameter block is copied as 32-bit words");
+  const int* src = (const int*)((const Params<T>*)q.params + s);
+  int* d = (int*)&dst;
+  const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x);
+  for (int k = tid; k < (int)(sizeof(Params<T>) / 4); k += (int)(blockDim.x * blockDim.y)) d[k] = __ldg(src + k);
+}
+
+// phase 0 stress, 1 velocity: units along x and y of a shot's grid
+template <class T>
+__device__ __forceinline__ int2 batch_units(const Params<T>& p, int phase) {
+  const int rows = kBZ * (phase == 0 ? kRZS : kRZV);
+  return make_int2((p.NX + kBX - 1) / kBX, (p.PMLZH + 1 + rows - 1) / rows);
+}
+
+template <class T, bool SI, int MODE, int PHASE>
+__device__ __forceinline__ void batch_cells(const BatchQueue& q, int items, int it_off) {
+  __shared__ Params<T> sp;
+  const int* first = q.first + PHASE * (q.n + 1);
+  int cur = -1;
+  for (int item = (int)blockIdx.x; item < items; item += (int)gridDim.x) {
+    const int s = batch_shot(first, q.n, item);
+    if (s != cur) {
+      __syncthreads();  // the previous shot's parameters are no longer read
+      batch_load_params<T>(sp, q, s);
+      __syncthreads();
+      cur = s;
+    }
+    const int2 g = batch_units(sp, PHASE);
+    const int j = item - __ldg(first + s);
+    const int bx = j % g.x, by0 = (j / g.x) * q.m;
+    const int by1 = min(by0 + q.m, g.y);
+    for (int by = by0; by < by1; ++by) {
+      if (PHASE == 0) stress_unit<T, SI, MODE>(sp, bx, by, it_off);
+      else velocity_unit<T, SI, MODE>(sp, bx, by);
+    }
+  }
+}
+
+template <class T, bool SI, int MODE>
+__global__ void __launch_bounds__(kBX * kBZ) k_stress_batch(const __grid_constant__ BatchQueue q, int items, int it_off) {
+  batch_cells<T, SI, MODE, 0>(q, items, it_off);
+}
+
+template <class T, bool SI, int MODE>
+__global__ void FDP_VELOCITY_BOUNDS(T) k_velocity_batch(const __grid_constant__ BatchQueue q, int items, int it_off) {
+  batch_cells<T, SI, MODE, 1>(q, items, it_off);
+}
+
+template <class T, bool SI>
+__global__ void __launch_bounds__(kBX * kBZ) k_edge_batch(const __grid_constant__ BatchQueue q, int items, int it_off) {
+  __shared__ Params<T> sp;
+  const int* first = q.first + 2 * (q.n + 1);
+  const int tid = (int)(threadIdx.y * blockDim.x + threadIdx.x);
+  int cur = -1;
+  for (int item = (int)blockIdx.x; item < items; item += (int)gridDim.x) {
+    const int s = batch_shot(first, q.n, item);
+    if (s != cur) {
+      __syncthreads();
+      batch_load_params<T>(sp, q, s);
+      __syncthreads();
+      cur = s;
+    }
+    edge_thread<T, SI>(sp, (item - __ldg(first + s)) * (kBX * kBZ) + tid, it_off);
   }
 }
 

@@ -131,11 +131,12 @@ class Engine:
         return int(s.value or 0)
 
     def medium_info(self) -> dict:
-        """Device representation of the medium: mode ("table" or "planes")
-        and the per-cell coefficient planes each phase reads."""
+        """Device representation of the medium: mode ("table", "planes", or
+        "biot" -- planes whose aliases follow Biot's relations) and the
+        per-cell coefficient planes each phase reads."""
         v = [C.c_int32() for _ in range(3)]
         self._check(self.lib.fdp_medium_info(self._ctx, *[C.byref(x) for x in v]))
-        return {"mode": "planes" if v[0].value == 1 else "table", "planes_stress": v[1].value,
+        return {"mode": {0: "table", 1: "planes", 2: "biot"}[v[0].value], "planes_stress": v[1].value,
                 "planes_velocity": v[2].value}
 
     def profile(self, it_begin: int, it_end: int) -> dict:
@@ -168,3 +169,68 @@ class Engine:
         out = np.zeros((n, self.nz, self.nx), dtype=self.dtype)
         self._check(self.lib.fdp_get_snapshot(self._ctx, mask, _ptr(out)))
         return out
+
+
+class Batch:
+    """Many prepared :class:`Engine` shots advanced together (``fdp_batch``).
+
+    The engines stay usable for reading results (:meth:`Engine.receivers`,
+    :meth:`Engine.field`, ...) after :meth:`synchronize`; while the batch
+    exists they are advanced only through it.  Every shot's values are
+    bit-identical to running it alone."""
+
+    def __init__(self, engines: list[Engine]):
+        if not engines:
+            raise ValueError("a batch needs at least one shot")
+        self.lib = native.load()
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(engines))(*[e._ctx.value for e in engines])
+        self._b = C.c_void_p()
+        rc = self.lib.fdp_batch_create(arr, len(engines), C.byref(self._b))
+        if rc != 0:
+            raise FdpError(rc, self.lib.fdp_batch_last_error(None).decode())
+
+    def close(self) -> None:
+        if self._b:
+            self.lib.fdp_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise FdpError(rc, self.lib.fdp_batch_last_error(self._b).decode())
+
+    def time_loop(self, it_begin: int, it_end: int) -> None:
+        """Advances every shot over levels it_begin..it_end (asynchronous)."""
+        self._check(self.lib.fdp_batch_run(self._b, it_begin, it_end))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.fdp_batch_synchronize(self._b))
+
+    def set_shape(self, units_per_item: int, waves: int) -> None:
+        """Fixes the tile shape (``units_per_item = 0``: tune on the next run)."""
+        self._check(self.lib.fdp_batch_set_shape(self._b, units_per_item, waves))
+
+    def shape(self) -> tuple[int, int]:
+        m, w = C.c_int32(), C.c_int32()
+        self._check(self.lib.fdp_batch_get_shape(self._b, C.byref(m), C.byref(w)))
+        return m.value, w.value
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.fdp_batch_kernel_launches(self._b))
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.fdp_batch_get_stream(self._b, C.byref(s)))
+        return int(s.value or 0)

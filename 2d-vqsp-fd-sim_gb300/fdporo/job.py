@@ -244,3 +244,30 @@ def layered(mx: int = 2048, mz: int = 2048, nsteps: int = 4000, tpml: int = 20, 
                     stf_time=t, stf_value=ricker(t, f0), irecx=ir, lrecx=lr, irecz=ir, lrecz=lr, key_tlp=key_tlp)
     depth = layer_depth if layer_depth is not None else mz * h / 2
     return cfg, layered_grf(mx, cfg.n_model_rows, h, seed, layer_depth=depth)
+
+
+def batch_shots(n_shots: int = 64, nsteps: int = 3000, seed: int = 20251, sides=(512, 2048, 32), tpml: int = 20,
+                f0: float = 20.0, dt: float = 1e-4, h: float = 1.0, n_rec: int = 512) -> list[tuple[int, dict]]:
+    """Per-shot parameters of the batched workload: each grid side drawn
+    uniformly from {lo, lo+step, ..., hi}, the source uniformly in the upper
+    quarter, the layered random medium of :func:`layered` with a per-shot
+    seed.  Returns (shot seed, keyword arguments of :func:`batch_shot`)."""
+    rng = np.random.default_rng(seed)
+    lo, hi, step = sides
+    choices = np.arange(lo, hi + 1, step)
+    out = []
+    for k in range(n_shots):
+        mx, mz = (int(v) for v in rng.choice(choices, size=2))
+        xs = float(rng.uniform(0.05, 0.95) * mx * h)
+        zs = float(rng.uniform(0.01, 0.25) * mz * h)
+        out.append((seed * 1000 + k, dict(mx=mx, mz=mz, nsteps=nsteps, tpml=tpml, f0=f0, dt=dt, h=h, n_rec=n_rec,
+                                          x_source=xs, z_source=zs)))
+    return out
+
+
+def batch_shot(seed: int, mx: int, mz: int, nsteps: int, tpml: int, f0: float, dt: float, h: float, n_rec: int,
+               x_source: float, z_source: float) -> tuple[JobConfig, Medium]:
+    """One shot of :func:`batch_shots`."""
+    cfg, med = layered(mx=mx, mz=mz, nsteps=nsteps, tpml=tpml, f0=f0, dt=dt, h=h, n_rec=min(n_rec, mx), seed=seed)
+    cfg.x_source, cfg.z_source = x_source, z_source
+    return cfg, med

@@ -70,29 +70,21 @@ def biot_table(rho_s, rho_f, phi, k_s, k_f, k_frame, mu, kappa, eta, tortuosity)
     m = tortuosity * rho_f / phi
     delta = rho * m - rho_f * rho_f
     b = eta / kappa
-    t = np.zeros(alpha.shape + (24,), dtype=np.float64)
-    t[..., COL["MU"]] = mu
-    t[..., COL["SIG_XX_1"]] = l2mc
-    t[..., COL["SIG_XX_2"]] = lamc
-    t[..., COL["SIG_XX_3"]] = am
-    t[..., COL["SIG_ZZ_1"]] = lamc
-    t[..., COL["SIG_ZZ_2"]] = l2mc
-    t[..., COL["SIG_ZZ_3"]] = am
-    t[..., COL["PRES_1"]] = -am
-    t[..., COL["PRES_2"]] = -am
-    t[..., COL["PRES_3"]] = -M
-    for s in ("U", "W"):
-        t[..., COL["REL1_" + s]] = m / delta
-        t[..., COL["REL2_" + s]] = rho_f * b / delta
-        t[..., COL["REL3_" + s]] = rho_f / delta
-    for s in ("QX", "QZ"):
-        t[..., COL["REL1_" + s]] = rho_f / delta
-        t[..., COL["REL2_" + s]] = rho / delta
-        t[..., COL["REL3_" + s]] = rho * b / delta
     dry = l2mc - am * am / np.where(M == 0, 1.0, M)
-    t[..., COL["AUXIL_W"]] = np.where(M == 0, lamc / l2mc, (lamc - am * am / np.where(M == 0, 1.0, M)) / dry)
-    t[..., COL["AUXIL_QZ"]] = np.where(M == 0, 0.0, (am / np.where(M == 0, 1.0, M)) * 2.0 * mu / dry)
-    return t
+    auxw = np.where(M == 0, lamc / l2mc, (lamc - am * am / np.where(M == 0, 1.0, M)) / dry)
+    auxqz = np.where(M == 0, 0.0, (am / np.where(M == 0, 1.0, M)) * 2.0 * mu / dry)
+    col = {"MU": mu, "SIG_XX_1": l2mc, "SIG_XX_2": lamc, "SIG_XX_3": am, "SIG_ZZ_1": lamc, "SIG_ZZ_2": l2mc,
+           "SIG_ZZ_3": am, "PRES_1": -am, "PRES_2": -am, "PRES_3": -M, "AUXIL_W": auxw, "AUXIL_QZ": auxqz}
+    for s in ("U", "W"):
+        col["REL1_" + s] = m / delta
+        col["REL2_" + s] = rho_f * b / delta
+        col["REL3_" + s] = rho_f / delta
+    for s in ("QX", "QZ"):
+        col["REL1_" + s] = rho_f / delta
+        col["REL2_" + s] = rho / delta
+        col["REL3_" + s] = rho * b / delta
+    # one pass into the interleaved (..., 24) layout
+    return np.stack([np.asarray(col[n], dtype=np.float64) for n in MO_COLUMNS], axis=-1)
 
 
 def rock_table(rock: Rock) -> np.ndarray:

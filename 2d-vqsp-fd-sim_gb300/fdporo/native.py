@@ -78,6 +78,15 @@ SIGNATURES = {
     "fdp_receivers_noalloc": (C.c_int, [_I32, _VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _I32, _I32, _VP, _I32,
                                         _I32, _D, _I32, _VP, _VP]),
     "fdp_destroy": (None, [_VP]),
+    "fdp_batch_create": (C.c_int, [C.POINTER(_VP), _I32, C.POINTER(_VP)]),
+    "fdp_batch_run": (C.c_int, [_VP, _I32, _I32]),
+    "fdp_batch_set_shape": (C.c_int, [_VP, _I32, _I32]),
+    "fdp_batch_get_shape": (C.c_int, [_VP, _PI32, _PI32]),
+    "fdp_batch_synchronize": (C.c_int, [_VP]),
+    "fdp_batch_kernel_launches": (C.c_int64, [_VP]),
+    "fdp_batch_get_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "fdp_batch_last_error": (C.c_char_p, [_VP]),
+    "fdp_batch_destroy": (None, [_VP]),
     "fdp_prep_velocities": (C.c_int, [_I32, _D, _D, _D, _D, _D, _D, _D, _PD, _PD, _PD]),
     "fdp_prep_scale_table": (C.c_int, [_I32, _I32, _D, _D, _VP]),
     "fdp_prep_expand_jm": (C.c_int, [_I32, _I32, _I32, _I32, _PI32, _PI32]),

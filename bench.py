@@ -278,6 +278,22 @@ def run_gpu(args) -> None:
                "scope": f"one whole shot of {WORKLOAD['mt2']} levels: fdp_create, fdp_set_* from host buffers, "
                         "fdp_run, fdp_get_receivers"}
 
+    # ---- seismogram error of this precision against the FP64 engine, whose
+    # every value the parity tests pin bit for bit to the FP64 oracle
+    accuracy = None
+    if e2e is not None and args.precision == "f32" and not args.no_accuracy:
+        inp64 = prepare_inputs("f64", WORKLOAD["mt2"])
+        e64 = job.make_engine(inp64, device=dev)
+        e64.time_loop(1, WORKLOAD["mt2"])
+        rec64 = e64.receivers(1, WORKLOAD["mt2"])
+        e64.close()
+        cols = [0, 1, 8, 9]  # SSU, SSW (u, -w) and SSP, SST (p, -txx)
+        ref = rec64[:, :, cols]
+        diff = rec.astype(np.float64)[:, :, cols] - ref
+        accuracy = {"seismogram_rel_l2": float(np.linalg.norm(diff) / np.linalg.norm(ref)),
+                    "against": "FP64 engine over the same whole shot (u, -w, p, -txx at all receivers and levels)",
+                    "target": 1e-3}
+
     # ---- CPU baseline on a bounded sample (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -310,9 +326,101 @@ def run_gpu(args) -> None:
                      "kernel_ms": {k: prof[k][0] / max(prof[k][1], 1) for k in prof},
                      "medium": medium, "kernel_share": shares},
         "e2e": e2e,
+        "accuracy": accuracy,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
+
+
+BATCH = dict(shots=64, mt2=3000, seed=20251)
+
+
+def _prepare_batch_shot(item):
+    """Prepared FP32 inputs of one shot of the batched workload (runs in a
+    worker process; the result is uploaded by the parent)."""
+    from fdporo import job
+    seed, kw = item
+    cfg, med = job.batch_shot(seed, **kw)
+    return job.prepare(cfg, med, "f32")
+
+
+def run_batch(args) -> None:
+    """Batched workload: BATCH['shots'] shots with grid sides drawn from
+    512..2048 (multiples of 32), per-shot layered random media, sources in
+    the upper quarter, 20-cell PML, FP32, advanced together by fdp_batch
+    (one launch per phase per level, tile shape tuned on the warm-up
+    levels), against the same shots run one after another with fdp_run."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    import torch
+    from fdporo import job
+    from fdporo.engine import Batch
+    ws, rank, local = _dist()
+    dev = local if torch.cuda.is_available() else 0
+    shots = job.batch_shots(args.shots, nsteps=BATCH["mt2"], seed=BATCH["seed"])
+    engines, cells = [], []
+    t0 = time.perf_counter()
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as pool:
+        for inp in pool.map(_prepare_batch_shot, shots):
+            engines.append(job.make_engine(inp, device=dev))
+            cells.append(inp.cells)
+    setup_s = time.perf_counter() - t0
+    total = sum(cells)
+    K, W = args.steps, max(args.warmup, 20)  # the batch tunes its shape on its first 18 levels
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    b = Batch(engines)
+    ext = torch.cuda.ExternalStream(b.stream(), device=dev)
+    b.time_loop(1, W)
+    b.synchronize()
+    launches0 = b.kernel_launches()
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        e0.record(ext)
+        b.time_loop(W + 1, W + K)
+        e1.record(ext)
+        e1.synchronize()
+    ms_batch = e0.elapsed_time(e1) / K
+    launches = b.kernel_launches() - launches0
+    shape = b.shape()
+    b.synchronize()
+    b.close()
+
+    # the same shots one after another, each with its own stream and graphs
+    lo = W + K + 1
+    for e in engines:
+        e.time_loop(lo, lo + W - 1)
+    for e in engines:
+        e.synchronize()
+    lo += W
+    ms_seq = 0.0
+    for e in engines:
+        s = torch.cuda.ExternalStream(e.stream(), device=dev)
+        e0.record(s)
+        e.time_loop(lo, lo + K - 1)
+        e1.record(s)
+        e1.synchronize()
+        ms_seq += e0.elapsed_time(e1) / K
+    for e in engines:
+        e.close()
+    per_shot = lambda ms: args.shots * 3600.0 / (BATCH["mt2"] * ms / 1e3)
+    line = {
+        "metric": "shots/hour", "value": per_shot(ms_batch), "unit": "shots/hour", "n_gpus": 1, "steps": K,
+        "warmup": W, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded layered media with Gaussian random fields, one per shot)",
+        "config": {"workload": f"batch-{args.shots}", "shots": args.shots, "cells_per_level": total,
+                   "sides": "512..2048 step 32", "tpml": 20, "levels_per_shot": BATCH["mt2"],
+                   "l2": "inputs larger than L2 (no flush)", "setup_s": setup_s},
+        "gcell_updates_per_s": total / (ms_batch / 1e3) / 1e9,
+        "sequential": {"ms_per_level": ms_seq, "shots_per_hour": per_shot(ms_seq),
+                       "gcell_updates_per_s": total / (ms_seq / 1e3) / 1e9},
+        "speedup_vs_sequential": ms_seq / ms_batch,
+        "tile_shape": {"units_per_item": shape[0], "waves": shape[1]},
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def main() -> None:
@@ -324,12 +432,17 @@ def main() -> None:
     ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--workload", choices=["layered", "batch"], default="layered")
+    ap.add_argument("--shots", type=int, default=BATCH["shots"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 

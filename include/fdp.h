@@ -175,8 +175,13 @@ int64_t fdp_kernel_launches(fdp_ctx* ctx);
 /* How the medium is held on the device after fdp_set_medium: *mode is 0
  * when the kernels index the material table through JM, 1 when each
  * distinct coefficient column is a per-cell plane (columns equal up to sign
- * share a plane, constant columns need none); *planes_stress and
- * *planes_velocity count the planes each phase reads per cell. */
+ * share a plane, constant columns need none), 2 when those planes are the
+ * ten of an isotropic Biot medium (lambda+2mu in SIG_XX_1 and SIG_ZZ_2,
+ * lambda in SIG_XX_2 and SIG_ZZ_1, alpha*M in SIG_XX_3, SIG_ZZ_3 and
+ * -PRES_1, -PRES_2, the same relaxation columns for x and z, REL1_Q equal
+ * to REL3_U), so the kernels resolve the aliases at compile
+ * time; *planes_stress and *planes_velocity count the planes each phase
+ * reads per cell. */
 int fdp_medium_info(fdp_ctx* ctx, int32_t* mode, int32_t* planes_stress, int32_t* planes_velocity);
 
 /* Last error message of the context (or of the last failed call that has
@@ -216,6 +221,47 @@ int fdp_receivers_noalloc(int32_t precision, const void* um, const void* wm, con
 /* Frees the context and all its device memory (the DEALLOCATEs the
  * reference leaves to program exit). */
 void fdp_destroy(fdp_ctx* ctx);
+
+/* ---------------------------------------------------------------------------
+ * Batched shots.  No counterpart in the reference, which runs one shot per
+ * job.  A batch advances many prepared contexts together: each level is one
+ * launch per phase for the whole batch, over a work queue of (shot, tile)
+ * items that persistent CTAs take round-robin, and runs of levels are
+ * replayed from CUDA graphs.  Shots may differ in grid size, medium and
+ * its device representation (fdp_medium_info), free-surface mode, source,
+ * receivers and PML width; they must share precision and device.  Shots
+ * are grouped by free-surface mode and medium representation, one launch
+ * per phase per group.  Every shot's values are bit-identical to running it
+ * alone with fdp_run. */
+typedef struct fdp_batch fdp_batch;
+
+/* Groups n contexts, each with medium, PML, bottom coefficients and source
+ * set.  The contexts stay owned by the caller and must outlive the batch;
+ * while it exists, run them only through it.  After fdp_batch_synchronize
+ * their receivers, snapshots and fields are read with the fdp_get_* calls. */
+int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out);
+
+/* Advances every shot over levels it_begin..it_end (within every shot's
+ * MT2).  Asynchronous.  Unless a shape was set, the first run tunes the
+ * tile shape on its own first levels (each candidate computes the same
+ * values, so no level is wasted or altered) and keeps the fastest. */
+int fdp_batch_run(fdp_batch* b, int32_t it_begin, int32_t it_end);
+
+/* Tile shape of the work queue: units_per_item vertically adjacent units
+ * (32 columns by 8 or 32 rows each) per item, and `waves` persistent CTAs
+ * per resident CTA slot of the GPU (0: one CTA per item).  units_per_item
+ * = 0 asks the next run to tune again. */
+int fdp_batch_set_shape(fdp_batch* b, int32_t units_per_item, int32_t waves);
+int fdp_batch_get_shape(fdp_batch* b, int32_t* units_per_item, int32_t* waves);
+
+/* Waits for the batch and reports a failed kernel of any shot. */
+int fdp_batch_synchronize(fdp_batch* b);
+int64_t fdp_batch_kernel_launches(fdp_batch* b);
+int fdp_batch_get_stream(fdp_batch* b, void** stream);
+/* Last error of the batch (of the last failed fdp_batch_create when NULL). */
+const char* fdp_batch_last_error(const fdp_batch* b);
+/* Frees the batch (not its contexts). */
+void fdp_batch_destroy(fdp_batch* b);
 
 #ifdef __cplusplus
 }
