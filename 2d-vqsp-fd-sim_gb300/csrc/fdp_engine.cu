@@ -65,6 +65,17 @@ struct fdp_ctx {
   // the default)
   fdp::TmaMaps tma_vel{}, tma_str{};
   bool use_tma = false;
+  // frame/core split (the default; FDP_KERNEL_VARIANT=global runs the unit
+  // kernels over the whole grid): core rectangles of each phase and the
+  // units holding any cell outside them
+  bool use_core = false;
+  int cs[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0};  // x0, x1, z0, z1
+  DevArr frame_s, frame_v;
+  int nframe_s = 0, nframe_v = 0;
+  // the frame kernel of a phase runs on `side`, concurrently with the core
+  // kernel on `stream` (fork and join through events, also inside graphs)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   int jmnum = 0;
   int mt2 = 0;
   int mr = 0, rec_flags = 0;
@@ -192,6 +203,8 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   p.MX = c->MX; p.MZ = c->MZ; p.TPML = c->TPML; p.PMLL = c->PMLL; p.PMLXH = c->PMLXH; p.PMLZH = c->PMLZH;
   p.NX = c->NX; p.NZ = c->NZ; p.MX1 = c->MX1; p.LIN_X = c->g.lin_x; p.LIN_Z = c->g.lin_z;
   p.pitch = c->pitch;
+  p.cs_x0 = c->cs[0]; p.cs_x1 = c->cs[1]; p.cs_z0 = c->cs[2]; p.cs_z1 = c->cs[3];
+  p.cv_x0 = c->cv[0]; p.cv_x1 = c->cv[1]; p.cv_z0 = c->cv[2]; p.cv_z1 = c->cv[3];
   // mod_auxil.F90:19-20 (default-real constants) and aux1.F90:44-46
   const T H = (T)c->g.h;
   p.A = (T)(-1.0f / 24.0f);
@@ -250,15 +263,85 @@ dim3 tile_grid(const fdp_ctx* c) {
   return dim3((c->NX + fdp::kTX - 1) / fdp::kTX, (c->NZ + fdp::kTZ - 1) / fdp::kTZ, 1);
 }
 
+// core grid of a phase: 4 cells per thread along x
+dim3 core_grid(const int r[4]) {
+  const int threads_x = (r[1] - r[0]) / 4;
+  return dim3((threads_x + fdp::kBX - 1) / fdp::kBX, (r[3] - r[2] + fdp::kBZ - 1) / fdp::kBZ, 1);
+}
+
 template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
   const dim3 blk(fdp::kBX, fdp::kBZ, 1);
   const dim3 tblk(fdp::kTX, 4, 1);
   if (kind == 0 && c->use_tma) fdp::k_stress_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_vel, it_off);
   else if (kind == 1 && c->use_tma) fdp::k_velocity_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_str, it_off);
+  else if ((kind == 0 || kind == 1) && c->use_core) {
+    const int* r = kind == 0 ? c->cs : c->cv;
+    const bool core = r[1] > r[0];
+    cudaStream_t fs = core ? c->side : c->stream;
+    if (core) {
+      cudaEventRecord(c->fork, c->stream);
+      cudaStreamWaitEvent(c->side, c->fork, 0);
+    }
+    if (kind == 0) fdp::k_stress_frame<T, SI, MODE><<<c->nframe_s, blk, 0, fs>>>(p, (const int2*)c->frame_s.p, it_off);
+    else fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v, blk, 0, fs>>>(p, (const int2*)c->frame_v.p);
+    if (core) {
+      if (kind == 0) fdp::k_stress_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
+      else fdp::k_velocity_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
+      cudaEventRecord(c->join, c->side);
+      cudaStreamWaitEvent(c->stream, c->join, 0);
+      c->launches += 1;
+    }
+  }
   else if (kind == 0) fdp::k_stress<T, SI, MODE><<<cell_grid(c, 0), blk, 0, c->stream>>>(p, it_off);
   else if (kind == 1) fdp::k_velocity<T, SI, MODE><<<cell_grid(c, 1), blk, 0, c->stream>>>(p, it_off);
   else fdp::k_edge<T, SI><<<(edge_threads(c) + kBlockX - 1) / kBlockX, kBlockX, 0, c->stream>>>(p, it_off);
   c->launches += 1;
+}
+
+// Core rectangles and frame unit lists.  A core cell of the stress phase
+// needs 3 <= I <= MX-2, 2 <= L <= MZ-2, L != LIN_Z; of the velocity phase
+// 4 <= I <= MX-2, 2 <= L <= MZ-2 (the interior branches).  The core starts
+// on a 16-byte-aligned column and spans whole groups of four.
+int plan_core(fdp_ctx* c) {
+  auto rect = [&](int r[4], int xmin, int zmin) {
+    int x0 = xmin;
+    while ((x0 - c->PMLL) % 4 != 0) ++x0;
+    const int n4 = (c->MX - 2 - x0 + 1) / 4;
+    r[0] = x0; r[1] = x0 + 4 * std::max(n4, 0);
+    r[2] = zmin; r[3] = c->MZ - 1;
+    if (r[1] <= r[0] || r[3] <= r[2]) { r[0] = r[1] = r[2] = r[3] = 0; }
+  };
+  // under stress imaging, rows 2..4 stay with the stress frame, whose unit
+  // holding them also writes the mirror rows 0 and 1 from them
+  rect(c->cs, 3, c->g.stress_imaging ? 5 : 2);
+  rect(c->cv, 4, 2);
+  auto in = [](const int r[4], int I, int L) { return I >= r[0] && I < r[1] && L >= r[2] && L < r[3]; };
+  const int gx = (c->NX + fdp::kBX - 1) / fdp::kBX;
+  std::vector<int> us, uv;
+  for (int ph = 0; ph < 2; ++ph) {
+    const int rows = fdp::kBZ * (ph == 0 ? fdp::kRZS : fdp::kRZV);
+    const int gy = (c->NZ + rows - 1) / rows;
+    const int* r = ph == 0 ? c->cs : c->cv;
+    std::vector<int>& out = ph == 0 ? us : uv;
+    for (int by = 0; by < gy; ++by)
+      for (int bx = 0; bx < gx; ++bx) {
+        // rows of the unit: stress from row 0 down, velocity from row PMLZH up
+        const int la = ph == 0 ? by * rows : c->PMLZH - (by + 1) * rows + 1;
+        const int lb = la + rows - 1;
+        bool frame = false;
+        for (int L = std::max(la, 0); L <= std::min(lb, c->PMLZH) && !frame; ++L)
+          for (int I = c->PMLL + bx * fdp::kBX; I <= std::min(c->PMLL + bx * fdp::kBX + fdp::kBX - 1, c->PMLXH); ++I)
+            if (!in(r, I, L) || (ph == 0 && L == c->g.lin_z)) { frame = true; break; }
+        if (frame) { out.push_back(bx); out.push_back(by); }
+      }
+  }
+  c->nframe_s = (int)us.size() / 2;
+  c->nframe_v = (int)uv.size() / 2;
+  int rc;
+  if ((rc = dev_alloc(c, c->frame_s, us.size() * sizeof(int))) != FDP_OK) return rc;
+  if ((rc = dev_alloc(c, c->frame_v, uv.size() * sizeof(int))) != FDP_OK) return rc;
+  if ((rc = copy_sync(c, c->frame_s.p, us.data(), us.size() * sizeof(int), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  return copy_sync(c, c->frame_v.p, uv.data(), uv.size() * sizeof(int), cudaMemcpyHostToDevice);
 }
 
 template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
@@ -309,7 +392,8 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) { c->graph = nullptr; return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
   }
-  const int per_level = 2 + (edge_threads(c) > 0 ? 1 : 0);
+  const int per_level = 2 + (edge_threads(c) > 0 ? 1 : 0) +
+                        (c->use_core ? (c->cs[1] > c->cs[0]) + (c->cv[1] > c->cv[0]) : 0);
   while (it_end - it + 1 >= kChunk && c->graph) {
     CK(c, cudaGraphLaunch(c->graph, c->stream));
     c->launches += (long long)kChunk * per_level + 1;
@@ -506,6 +590,14 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   if ((rc = dev_alloc(c, c->errbuf, sizeof(int))) != FDP_OK) return bail(rc);
   const char* variant = std::getenv("FDP_KERNEL_VARIANT");
   c->use_tma = variant && std::strcmp(variant, "tma") == 0;
+  c->use_core = !(variant && (std::strcmp(variant, "tma") == 0 || std::strcmp(variant, "global") == 0));
+  if (c->use_core) {
+    if ((rc = plan_core(c)) != FDP_OK) return bail(rc);
+    e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+    if (e != cudaSuccess) { c->err = std::string("side stream: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
+  }
   if (c->use_tma) {
     for (int k = 0; k < 4; ++k) {
       if ((rc = make_field_map(c, &c->tma_vel.m[k], c->fields[k].p)) != FDP_OK) return bail(rc);
@@ -794,11 +886,16 @@ void fdp_destroy(fdp_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase, &c->errbuf};
+  DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase,
+                   &c->errbuf, &c->frame_s, &c->frame_v};
   for (auto* a : all) if (a->p) cudaFree(a->p);
   for (auto& a : c->fields) if (a.p) cudaFree(a.p);
   for (auto& a : c->prof) if (a.p) cudaFree(a.p);
   for (auto& a : c->mem) if (a.p) cudaFree(a.p);
+  if (c->side) cudaStreamSynchronize(c->side);
+  if (c->fork) cudaEventDestroy(c->fork);
+  if (c->join) cudaEventDestroy(c->join);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -850,6 +947,12 @@ int bfail(fdp_batch* b, int code, const char* fmt, ...) {
     cudaError_t e_ = (call);                                                                \
     if (e_ != cudaSuccess) return bfail((b), FDP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
+
+// The batched kernels run the unit code over every cell of a shot.
+template <class T> void clear_core(Params<T>& p) {
+  p.cs_x0 = p.cs_x1 = p.cs_z0 = p.cs_z1 = 0;
+  p.cv_x0 = p.cv_x1 = p.cv_z0 = p.cv_z1 = 0;
+}
 
 // first-item offsets of group g inside b->first
 size_t group_first_offset(const fdp_batch* b, size_t g) {
@@ -1087,11 +1190,13 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
       Params<double> p;
       fill_params<double>(b->shots[s], p);
       p.it_base = (const int*)b->itbase.p;
+      clear_core(p);
       std::memcpy(&host[psize * s], &p, psize);
     } else {
       Params<float> p;
       fill_params<float>(b->shots[s], p);
       p.it_base = (const int*)b->itbase.p;
+      clear_core(p);
       std::memcpy(&host[psize * s], &p, psize);
     }
   }

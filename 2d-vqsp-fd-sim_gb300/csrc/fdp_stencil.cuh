@@ -96,6 +96,10 @@ __host__ __device__ constexpr bool biot_neg(int k) { return k == 7 || k == 8; }
 template <class T> struct Params {
   int MX, MZ, TPML, PMLL, PMLXH, PMLZH, NX, NZ, MX1, LIN_X, LIN_Z;
   int pitch;    // field row pitch in elements
+  // core rectangles [x0, x1) x [z0, z1) of each phase (stress excluding row
+  // LIN_Z), updated by the vectorised core kernels; the unit kernels then
+  // skip them.  Empty (x0 == x1) when the unit kernels update every cell.
+  int cs_x0, cs_x1, cs_z0, cs_z1, cv_x0, cv_x1, cv_z0, cv_z1;
   T AH, BH, CH, BC, A, B, DT, DTE;
   T *UM, *WM, *QX, *QZ, *TXX, *TZZ, *TXZ, *PRES;
   // medium, table mode
@@ -492,14 +496,17 @@ template <class T, bool SI, int MODE>
 __device__ __forceinline__ void stress_unit(const Params<T>& p, int bx, int by, int it_off) {
   const int I = p.PMLL + (int)(bx * kBX + threadIdx.x);
   const int L0 = (int)(by * kBZ + threadIdx.y) * kRZS;  // rows L0 .. L0+kRZS-1
-  if (stress_fast_rows(p, I, L0)) {
+  const bool core = p.cs_x1 > p.cs_x0;  // the core kernel updates the core cells
+  if (!core && stress_fast_rows(p, I, L0)) {
     stress_interior_rows<T, MODE>(p, I, L0);
   } else if (I <= p.PMLXH) {
     const int it = *p.it_base + it_off;
     const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
+    const bool incol = I >= p.cs_x0 && I < p.cs_x1;
 #pragma unroll 1
     for (int L = L0; L < L0 + kRZS; ++L)
-      if (L <= p.PMLZH && (!SI || L >= 2)) stress_cell<T, SI, MODE>(p, rd, I, L, it);
+      if (L <= p.PMLZH && (!SI || L >= 2) && !(incol && L >= p.cs_z0 && L < p.cs_z1 && L != p.LIN_Z))
+        stress_cell<T, SI, MODE>(p, rd, I, L, it);
   }
   if (SI && by == 0) {
     __syncthreads();  // rows 2..4 of this unit are final
@@ -778,13 +785,16 @@ __device__ __forceinline__ void velocity_unit(const Params<T>& p, int bx, int by
       old[k][2][tx] = FDP_F(p.QX, I, L1 - k); old[k][3][tx] = FDP_F(p.QZ, I, L1 - k);
     }
   }
-  if (velocity_fast_rows(p, I, L0)) {
+  const bool core = p.cv_x1 > p.cv_x0;  // the core kernel updates the core cells
+  if (!core && velocity_fast_rows(p, I, L0)) {
     velocity_interior_rows<T, MODE>(p, I, L0);
   } else if (inx) {
     const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
+    const bool incol = I >= p.cv_x0 && I < p.cv_x1;
 #pragma unroll 1
     for (int L = L0; L <= L1; ++L)
-      if (L >= (SI ? 2 : 0) && L < p.PMLZH) velocity_cell<T, SI, MODE>(p, rd, I, L);
+      if (L >= (SI ? 2 : 0) && L < p.PMLZH && !(incol && L >= p.cv_z0 && L < p.cv_z1))
+        velocity_cell<T, SI, MODE>(p, rd, I, L);
   }
   if (me) {
     // hplane_pmlzh0_velocity.F90:34-63
@@ -811,6 +821,194 @@ template <class T, bool SI, int MODE>
 __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity(const __grid_constant__ Params<T> p, int it_off) {
   (void)it_off;
   velocity_unit<T, SI, MODE>(p, (int)blockIdx.x, (int)blockIdx.y);
+}
+
+// ---------------------------------------------------------------------------
+// Frame and core.  With a core rectangle set, each phase is two launches:
+// the frame kernels run the unit code over the listed units (those holding
+// any cell outside the core), skipping core cells; the core kernels update
+// the core, four consecutive cells of a row per thread with 16-byte loads
+// and stores.  The core holds only interior cells of the phase (4th-order
+// stencils everywhere, no source row), so the core kernels are the interior
+// branches of stress_cell / velocity_cell, same expressions in the same
+// order, for four cells at a time.
+template <class T, bool SI, int MODE>
+__global__ void __launch_bounds__(kBX * kBZ) k_stress_frame(const __grid_constant__ Params<T> p,
+                                                            const int2* __restrict__ units, int it_off) {
+  const int2 u = units[blockIdx.x];
+  stress_unit<T, SI, MODE>(p, u.x, u.y, it_off);
+}
+
+template <class T, bool SI, int MODE>
+__global__ void FDP_VELOCITY_BOUNDS(T) k_velocity_frame(const __grid_constant__ Params<T> p,
+                                                        const int2* __restrict__ units) {
+  const int2 u = units[blockIdx.x];
+  velocity_unit<T, SI, MODE>(p, u.x, u.y);
+}
+
+template <class T> struct V4 { T v[4]; };
+
+// four consecutive values at a 16-byte-aligned address, read-only path
+__device__ __forceinline__ V4<float> ld4(const float* a) {
+  const float4 x = __ldg(reinterpret_cast<const float4*>(a));
+  return {{x.x, x.y, x.z, x.w}};
+}
+__device__ __forceinline__ V4<double> ld4(const double* a) {
+  const double2 x = __ldg(reinterpret_cast<const double2*>(a)), y = __ldg(reinterpret_cast<const double2*>(a) + 1);
+  return {{x.x, x.y, y.x, y.y}};
+}
+// the same through the coherent path, for the fields the kernel updates
+__device__ __forceinline__ V4<float> ld4c(const float* a) {
+  const float4 x = *reinterpret_cast<const float4*>(a);
+  return {{x.x, x.y, x.z, x.w}};
+}
+__device__ __forceinline__ V4<double> ld4c(const double* a) {
+  const double2 x = reinterpret_cast<const double2*>(a)[0], y = reinterpret_cast<const double2*>(a)[1];
+  return {{x.x, x.y, y.x, y.y}};
+}
+__device__ __forceinline__ void st4(float* a, const V4<float>& v) {
+  *reinterpret_cast<float4*>(a) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+}
+__device__ __forceinline__ void st4(double* a, const V4<double>& v) {
+  reinterpret_cast<double2*>(a)[0] = make_double2(v.v[0], v.v[1]);
+  reinterpret_cast<double2*>(a)[1] = make_double2(v.v[2], v.v[3]);
+}
+
+// Coefficient k of cell j (0..3) of a core thread: from the vectors of the
+// Biot planes (slots s0.. of `bio`), else through coef().
+template <class T, int MODE>
+__device__ __forceinline__ T core_coef(const Params<T>& p, int k, long long cell, int J, const V4<T>* bio, int s0,
+                                       int j) {
+  if constexpr (MODE == M_BIOT) {
+    const T v = bio[biot_slot(k) - s0].v[j];
+    return biot_neg(k) ? -v : v;
+  } else {
+    return coef<T, MODE>(p, k, cell, J);
+  }
+}
+
+#define FDP_CORE_BOUNDS(T) __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? 2 : 1)
+
+template <class T, int MODE>
+__global__ void FDP_CORE_BOUNDS(T) k_stress_core(const __grid_constant__ Params<T> p) {
+  const int I0 = p.cs_x0 + 4 * (int)(blockIdx.x * kBX + threadIdx.x);
+  const int L = p.cs_z0 + (int)(blockIdx.y * kBZ + threadIdx.y);
+  if (I0 >= p.cs_x1 || L >= p.cs_z1 || L == p.LIN_Z) return;
+  const long long P = p.pitch;
+  const long long c0 = (long long)L * P + (I0 - p.PMLL);
+  const T* U = p.UM + c0;
+  const T* W = p.WM + c0;
+  const T* X = p.QX + c0;
+  const T* Z = p.QZ + c0;
+  // row L of u, w, qx with the vectors either side (columns I0-4 .. I0+7),
+  // and the column values the z stencils need
+  const V4<T> ur[3] = {ld4(U - 4), ld4(U), ld4(U + 4)};
+  const V4<T> wr[3] = {ld4(W - 4), ld4(W), ld4(W + 4)};
+  const V4<T> xr[3] = {ld4(X - 4), ld4(X), ld4(X + 4)};
+  const V4<T> um2 = ld4(U - 2 * P), um1 = ld4(U - P), up1 = ld4(U + P);
+  const V4<T> wm1 = ld4(W - P), wp1 = ld4(W + P), wp2 = ld4(W + 2 * P);
+  const V4<T> zm1 = ld4(Z - P), z0 = ld4(Z), zp1 = ld4(Z + P), zp2 = ld4(Z + 2 * P);
+  V4<T> oxz = ld4c(p.TXZ + c0), oxx = ld4c(p.TXX + c0), ozz = ld4c(p.TZZ + c0), opr = ld4c(p.PRES + c0);
+  V4<T> bio[5];
+  if constexpr (MODE == M_BIOT) {
+#pragma unroll
+    for (int s = 0; s < 5; ++s) bio[s] = ld4(p.bplane[s] + c0);
+  }
+  // value of row vector r at column I0 + j + d, d in -4..7
+  auto at = [](const V4<T>* r, int j, int d) { return r[(j + d + 4) >> 2].v[(j + d + 4) & 3]; };
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const long long cell_ = c0 + j;
+    const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+    auto C = [&](int k) { return core_coef<T, MODE>(p, k, cell_, J_, bio, 0, j); };
+    // strain_uw_xz.F90:201-204
+    const T exz = p.AH * (up1.v[j] - um2.v[j] + at(wr, j, 1) - at(wr, j, -2))
+                + p.BH * (ur[1].v[j] - um1.v[j] + wr[1].v[j] - at(wr, j, -1));
+    // strain_uw_zz.F90:43,49 and strain_q_zz.F90:43,49
+    T ezz = (p.CH * (wp1.v[j] - wr[1].v[j]));
+    ezz = p.AH * (wp2.v[j] - wm1.v[j]) + p.BC * ezz;
+    T qzz = (p.CH * (zp1.v[j] - z0.v[j]));
+    qzz = p.AH * (zp2.v[j] - zm1.v[j]) + p.BC * qzz;
+    // strain_uw_xx.F90:71-72 and strain_q_xx.F90:70-71
+    const T exx = p.AH * (at(ur, j, 2) - at(ur, j, -1)) + p.BH * (at(ur, j, 1) - ur[1].v[j]);
+    const T qxx = p.AH * (at(xr, j, 2) - at(xr, j, -1)) + p.BH * (at(xr, j, 1) - xr[1].v[j]);
+    // stress_xz.F90:44-46 and stress_nn.F90:53-59
+    const T TXZv = C(C_MU) * exz;
+    oxz.v[j] = oxz.v[j] + p.DTE * TXZv;
+    const T s1 = C(C_SXX1), s2 = C(C_SXX2), s3 = C(C_SXX3);
+    const T z1 = C(C_SZZ1), z2 = C(C_SZZ2), z3 = C(C_SZZ3);
+    const T q1 = C(C_P1), q2 = C(C_P2), q3 = C(C_P3);
+    const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
+    const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
+    const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
+    oxx.v[j] = oxx.v[j] + p.DTE * TXXv;
+    ozz.v[j] = ozz.v[j] + p.DTE * TZZv;
+    opr.v[j] = opr.v[j] + p.DTE * PRv;
+  }
+  st4(p.TXZ + c0, oxz);
+  st4(p.TXX + c0, oxx);
+  st4(p.TZZ + c0, ozz);
+  st4(p.PRES + c0, opr);
+}
+
+template <class T, int MODE>
+__global__ void FDP_CORE_BOUNDS(T) k_velocity_core(const __grid_constant__ Params<T> p) {
+  const int I0 = p.cv_x0 + 4 * (int)(blockIdx.x * kBX + threadIdx.x);
+  const int L = p.cv_z0 + (int)(blockIdx.y * kBZ + threadIdx.y);
+  if (I0 >= p.cv_x1 || L >= p.cv_z1) return;
+  const long long P = p.pitch;
+  const long long c0 = (long long)L * P + (I0 - p.PMLL);
+  const T A = p.A, B = p.B;
+  const T* XX = p.TXX + c0;
+  const T* ZZ = p.TZZ + c0;
+  const T* XZ = p.TXZ + c0;
+  const T* PR = p.PRES + c0;
+  const V4<T> xxr[3] = {ld4(XX - 4), ld4(XX), ld4(XX + 4)};
+  const V4<T> prr[3] = {ld4(PR - 4), ld4(PR), ld4(PR + 4)};
+  const V4<T> xzr[3] = {ld4(XZ - 4), ld4(XZ), ld4(XZ + 4)};
+  const V4<T> prm2 = ld4(PR - 2 * P), prm1 = ld4(PR - P), prp1 = ld4(PR + P);
+  const V4<T> xzm1 = ld4(XZ - P), xzp1 = ld4(XZ + P), xzp2 = ld4(XZ + 2 * P);
+  const V4<T> zzm2 = ld4(ZZ - 2 * P), zzm1 = ld4(ZZ - P), zz0 = ld4(ZZ), zzp1 = ld4(ZZ + P);
+  V4<T> oqx = ld4c(p.QX + c0), oum = ld4c(p.UM + c0), oqz = ld4c(p.QZ + c0), owm = ld4c(p.WM + c0);
+  V4<T> bio[5];
+  if constexpr (MODE == M_BIOT) {
+#pragma unroll
+    for (int s = 0; s < 5; ++s) bio[s] = ld4(p.bplane[5 + s] + c0);
+  }
+  auto at = [](const V4<T>* r, int j, int d) { return r[(j + d + 4) >> 2].v[(j + d + 4) & 3]; };
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const long long cell_ = c0 + j;
+    const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+    auto C = [&](int k) { return core_coef<T, MODE>(p, k, cell_, J_, bio, 5, j); };
+    const T pr0 = prr[1].v[j];
+    {
+      // inh_qx_int.F90:44-52 and inh_v_uv_int.F90:45-54
+      const T E = C(C_EQX), Cu = C(C_CU);
+      const T R1 = C(C_R1QX), R2 = C(C_R2QX), R1u = C(C_R1U), R3u = C(C_R3U);
+      const T qx0 = oqx.v[j], u0 = oum.v[j];
+      const T Xs = A * (at(xxr, j, 1) - at(xxr, j, -2) + xzp2.v[j] - xzm1.v[j])
+                 + B * (xxr[1].v[j] - at(xxr, j, -1) + xzp1.v[j] - xzr[1].v[j]);
+      const T Pp = A * (at(prr, j, 1) - at(prr, j, -2)) + B * (pr0 - at(prr, j, -1));
+      oqx.v[j] = E * qx0 - R1 * Xs - R2 * Pp;
+      oum.v[j] = u0 + Cu * qx0 + R1u * Xs + R3u * Pp;
+    }
+    {
+      // inh_qz_int.F90:45-53 and inh_v_w_int.F90:47-56
+      const T E = C(C_EQZ), Cw = C(C_CW);
+      const T R1 = C(C_R1QZ), R2 = C(C_R2QZ), R1w = C(C_R1W), R3w = C(C_R3W);
+      const T qz0 = oqz.v[j], w0 = owm.v[j];
+      const T Xs = A * (zzp1.v[j] - zzm2.v[j] + at(xzr, j, 2) - at(xzr, j, -1))
+                 + B * (zz0.v[j] - zzm1.v[j] + at(xzr, j, 1) - xzr[1].v[j]);
+      const T Pp = A * (prp1.v[j] - prm2.v[j]) + B * (pr0 - prm1.v[j]);
+      oqz.v[j] = E * qz0 - R1 * Xs - R2 * Pp;
+      owm.v[j] = w0 + Cw * qz0 + R1w * Xs + R3w * Pp;
+    }
+  }
+  st4(p.QX + c0, oqx);
+  st4(p.UM + c0, oum);
+  st4(p.QZ + c0, oqz);
+  st4(p.WM + c0, owm);
 }
 
 // ---------------------------------------------------------------------------

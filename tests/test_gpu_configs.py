@@ -1,0 +1,62 @@
+"""Parity at the benchmark configurations' own sizes.
+
+* The small homogeneous case (300 x 300 sandstone, 20-cell PML, 60 Hz
+  Ricker at the centre, 101 receivers at z = 50 m, FP64, 1500 levels): the
+  whole shot, bit for bit against the oracle (OpenMP build), every field,
+  memory variable and receiver value.
+* The layered 2048 x 2048 case (per-cell Gaussian-random-field Biot medium,
+  free surface, 512 receivers): the full grid for 200 levels in FP32, bit
+  for bit against the oracle.
+* The FP32 error of the small case's seismograms against FP64 stays within
+  the 1e-3 relative L2 the FP32 mode is held to.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import compare_state
+
+pytestmark = pytest.mark.gpu
+
+THREADS = min(16, os.cpu_count() or 1)
+
+
+def _rel_l2(a, b):
+    return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+
+
+def test_small_homogeneous_whole_shot_fp64():
+    from fdporo import job
+    from oracle.oracle import make_oracle
+    cfg, med = job.small_homogeneous()
+    inp = job.prepare(cfg, med, "f64")
+    eng, orc = job.make_engine(inp), make_oracle(inp, threads=THREADS)
+    # one material: every coefficient is a constant folded into the kernels
+    assert eng.medium_info() == {"mode": "planes", "planes_stress": 0, "planes_velocity": 0}
+    eng.time_loop(1, 1500)
+    orc.time_loop(1, 1500)
+    compare_state(eng, orc)
+    rec = eng.receivers(1, 1500)
+    np.testing.assert_array_equal(rec, orc.receivers(1, 1500))
+    assert np.abs(rec).max() > 0
+    # FP32 against FP64: u, -w, p, -txx at all receivers and levels
+    inp32 = job.prepare(cfg, med, "f32")
+    e32 = job.make_engine(inp32)
+    e32.time_loop(1, 1500)
+    cols = [0, 1, 8, 9]
+    err = _rel_l2(e32.receivers(1, 1500)[:, :, cols], rec[:, :, cols])
+    assert err < 1e-3, err
+
+
+def test_layered_2048_full_grid_fp32():
+    from fdporo import job
+    from oracle.oracle import make_oracle
+    cfg, med = job.layered(mx=2048, mz=2048, nsteps=200)
+    inp = job.prepare(cfg, med, "f32")
+    eng, orc = job.make_engine(inp), make_oracle(inp, threads=THREADS)
+    assert eng.medium_info()["mode"] == "biot"
+    eng.time_loop(1, 200)
+    orc.time_loop(1, 200)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 200), orc.receivers(1, 200))

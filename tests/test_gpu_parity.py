@@ -14,10 +14,11 @@ from helpers import compare_state, randomize_state, small_job
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(autouse=True, params=["tma", "global"])
+@pytest.fixture(autouse=True, params=["core", "global", "tma"])
 def kernel_variant(request, monkeypatch):
-    """Runs every test with the TMA-staged kernels and with the global-load
-    kernels (fdp_create reads FDP_KERNEL_VARIANT)."""
+    """Runs every test with each kernel variant fdp_create can select through
+    FDP_KERNEL_VARIANT: the frame/core split (default), the unit kernels
+    over the whole grid, and the TMA-staged kernels."""
     monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
     return request.param
 
