@@ -1,0 +1,77 @@
+// Private to the library: the context of one shot (include/fdp.h) as the
+// engine and the learned-edge code both see it.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "fdp.h"
+#include "fdp_stencil.cuh"
+
+struct DevArr {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct fdp_edge;
+struct EdgeState;  // per-context state of an attached learned edge
+
+struct fdp_ctx {
+  fdp_grid g{};
+  int prec = 4;
+  int MX = 0, MZ = 0, TPML = 0, PMLL = 0, PMLXH = 0, PMLZH = 0, NX = 0, NZ = 0, MX1 = 0;
+  int pitch = 0, rows_alloc = 0;
+  int medium_mode = fdp::M_TABLE;
+  int src[fdp::C_NCOEF], neg[fdp::C_NCOEF];
+  double cval_d[fdp::C_NCOEF];
+  float cval_f[fdp::C_NCOEF];
+  int nplanes = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // device memory
+  DevArr fields[8];
+  DevArr jm, coef, planes, aux, prof[24], mem[27], ab, hist, stf, rec, raw, itbase, errbuf;
+  // TMA descriptors of the input fields of each phase; use_tma selects the
+  // TMA-staged kernels (FDP_KERNEL_VARIANT=tma; the global-load kernels are
+  // the default)
+  fdp::TmaMaps tma_vel{}, tma_str{};
+  bool use_tma = false;
+  // frame/core split (the default; FDP_KERNEL_VARIANT=global runs the unit
+  // kernels over the whole grid): core rectangles of each phase and the
+  // units holding any cell outside them
+  bool use_core = false;
+  int cs[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0};  // x0, x1, z0, z1
+  DevArr frame_s, frame_v;
+  int nframe_s = 0, nframe_v = 0;
+  // the frame kernel of a phase runs on `side`, concurrently with the core
+  // kernel on `stream` (fork and join through events, also inside graphs)
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  // fdp_profile_run: events around each phase's core kernel
+  cudaEvent_t core_ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  int jmnum = 0;
+  int mt2 = 0;
+  int mr = 0, rec_flags = 0;
+  bool have_medium = false, have_pml = false, have_nr = false, have_source = false;
+  // graph of kChunk levels
+  cudaGraphExec_t graph = nullptr;
+  bool params_dirty = true;
+  long long launches = 0;
+  int last_it = 0;  // highest level run so far
+  // learned absorbing edge: state (history, tiles) once the context has
+  // trained or carried an edge; applied after every level while attached
+  EdgeState* edge = nullptr;
+  bool edge_attached = false;
+};
+
+namespace fdp {
+// Launches the attached learned edge's kernels for level *it_base + it_off
+// on the context's stream (none when no edge is attached); returns the
+// number of launches.
+int edge_launch(fdp_ctx* c, int it_off);
+// Frees the context's learned-edge state.
+void edge_release(fdp_ctx* c);
+}  // namespace fdp
+
+

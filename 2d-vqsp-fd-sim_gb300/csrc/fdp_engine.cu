@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "fdp.h"
+#include "fdp_ctx.h"
 #include "fdp_stencil.cuh"
 
 using fdp::Params;
@@ -33,59 +34,12 @@ constexpr int kBlockX = 128;     // threads per block (x)
 
 std::string g_create_error;
 
-struct DevArr {
-  void* p = nullptr;
-  size_t bytes = 0;
-};
-
 }  // namespace
 
 namespace fdp {
 // Error message of calls that have no context (fdp_create, fdp_receivers_noalloc).
 void set_global_error(const char* msg) { g_create_error = msg; }
 }  // namespace fdp
-
-struct fdp_ctx {
-  fdp_grid g{};
-  int prec = 4;
-  int MX = 0, MZ = 0, TPML = 0, PMLL = 0, PMLXH = 0, PMLZH = 0, NX = 0, NZ = 0, MX1 = 0;
-  int pitch = 0, rows_alloc = 0;
-  int medium_mode = fdp::M_TABLE;
-  int src[fdp::C_NCOEF], neg[fdp::C_NCOEF];
-  double cval_d[fdp::C_NCOEF];
-  float cval_f[fdp::C_NCOEF];
-  int nplanes = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  // device memory
-  DevArr fields[8];
-  DevArr jm, coef, planes, aux, prof[24], mem[27], ab, hist, stf, rec, raw, itbase, errbuf;
-  // TMA descriptors of the input fields of each phase; use_tma selects the
-  // TMA-staged kernels (FDP_KERNEL_VARIANT=tma; the global-load kernels are
-  // the default)
-  fdp::TmaMaps tma_vel{}, tma_str{};
-  bool use_tma = false;
-  // frame/core split (the default; FDP_KERNEL_VARIANT=global runs the unit
-  // kernels over the whole grid): core rectangles of each phase and the
-  // units holding any cell outside them
-  bool use_core = false;
-  int cs[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0};  // x0, x1, z0, z1
-  DevArr frame_s, frame_v;
-  int nframe_s = 0, nframe_v = 0;
-  // the frame kernel of a phase runs on `side`, concurrently with the core
-  // kernel on `stream` (fork and join through events, also inside graphs)
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
-  int jmnum = 0;
-  int mt2 = 0;
-  int mr = 0, rec_flags = 0;
-  bool have_medium = false, have_pml = false, have_nr = false, have_source = false;
-  // graph of kChunk levels
-  cudaGraphExec_t graph = nullptr;
-  bool params_dirty = true;
-  long long launches = 0;
-  int last_it = 0;  // highest level run so far
-};
 
 namespace {
 
@@ -285,8 +239,10 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
     if (kind == 0) fdp::k_stress_frame<T, SI, MODE><<<c->nframe_s, blk, 0, fs>>>(p, (const int2*)c->frame_s.p, it_off);
     else fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v, blk, 0, fs>>>(p, (const int2*)c->frame_v.p);
     if (core) {
+      if (c->core_ev[kind][0]) cudaEventRecord(c->core_ev[kind][0], c->stream);
       if (kind == 0) fdp::k_stress_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
       else fdp::k_velocity_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
+      if (c->core_ev[kind][1]) cudaEventRecord(c->core_ev[kind][1], c->stream);
       cudaEventRecord(c->join, c->side);
       cudaStreamWaitEvent(c->stream, c->join, 0);
       c->launches += 1;
@@ -362,6 +318,7 @@ template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_o
   launch<T>(c, p, 0, it_off);
   launch<T>(c, p, 1, it_off);
   if (edge_threads(c) > 0) launch<T>(c, p, 2, it_off);
+  c->launches += fdp::edge_launch(c, it_off);  // learned absorbing edge, when attached
   return FDP_OK;
 }
 
@@ -393,7 +350,8 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
     if (e != cudaSuccess) { c->graph = nullptr; return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
   }
   const int per_level = 2 + (edge_threads(c) > 0 ? 1 : 0) +
-                        (c->use_core ? (c->cs[1] > c->cs[0]) + (c->cv[1] > c->cv[0]) : 0);
+                        (c->use_core ? (c->cs[1] > c->cs[0]) + (c->cv[1] > c->cv[0]) : 0) +
+                        (c->edge && c->edge_attached ? 3 : 0);
   while (it_end - it + 1 >= kChunk && c->graph) {
     CK(c, cudaGraphLaunch(c->graph, c->stream));
     c->launches += (long long)kChunk * per_level + 1;
@@ -830,6 +788,15 @@ int fdp_medium_info(fdp_ctx* c, int32_t* mode, int32_t* planes_stress, int32_t* 
   return FDP_OK;
 }
 
+int fdp_core_info(fdp_ctx* c, int32_t* rect8) {
+  if (!c || !rect8) return fail(c, FDP_ERR_ARG, "null argument");
+  for (int k = 0; k < 4; ++k) {
+    rect8[k] = c->use_core ? c->cs[k] : 0;
+    rect8[4 + k] = c->use_core ? c->cv[k] : 0;
+  }
+  return FDP_OK;
+}
+
 int fdp_get_stream(fdp_ctx* c, void** stream) {
   if (!c || !stream) return fail(c, FDP_ERR_ARG, "null argument");
   *stream = (void*)c->stream;
@@ -843,7 +810,7 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
   if (it_begin < 1 || it_end > c->mt2 || it_end < it_begin)
     return fail(c, FDP_ERR_ARG, "levels %d..%d outside 1..MT2=%d", it_begin, it_end, c->mt2);
   CK(c, cudaSetDevice(c->g.device));
-  for (int k = 0; k < 3; ++k) { ms_out[k] = 0.0; launches_out[k] = 0; }
+  for (int k = 0; k < 5; ++k) { ms_out[k] = 0.0; launches_out[k] = 0; }
   auto body = [&](auto zero) -> int {
     using T = decltype(zero);
     Params<T> p;
@@ -851,6 +818,9 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
     const int nedge = edge_threads(c);
     cudaEvent_t ev[4];
     for (auto& e : ev) CK(c, cudaEventCreate(&e));
+    const bool core[2] = {c->use_core && c->cs[1] > c->cs[0], c->use_core && c->cv[1] > c->cv[0]};
+    for (int k = 0; k < 2; ++k)
+      if (core[k]) for (auto& e : c->core_ev[k]) CK(c, cudaEventCreate(&e));
     fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
     for (int it = it_begin; it <= it_end; ++it) {
       const int off = it - it_begin;
@@ -860,6 +830,7 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
       launch<T>(c, p, 1, off);
       CK(c, cudaEventRecord(ev[2], c->stream));
       if (nedge > 0) launch<T>(c, p, 2, off);
+      c->launches += fdp::edge_launch(c, off);
       CK(c, cudaEventRecord(ev[3], c->stream));
       CK(c, cudaEventSynchronize(ev[3]));
       float t;
@@ -867,11 +838,20 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
         CK(c, cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
         ms_out[k] += t;
       }
+      for (int k = 0; k < 2; ++k)
+        if (core[k]) {
+          CK(c, cudaEventElapsedTime(&t, c->core_ev[k][0], c->core_ev[k][1]));
+          ms_out[3 + k] += t;
+          launches_out[3 + k] += 1;
+        }
       launches_out[0] += 1; launches_out[1] += 1; launches_out[2] += nedge > 0 ? 1 : 0;
     }
     fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_end - it_begin + 1);
     c->launches += 2;
     for (auto& e : ev) cudaEventDestroy(e);
+    for (auto& pair : c->core_ev)
+      for (auto& e : pair)
+        if (e) { cudaEventDestroy(e); e = nullptr; }
     CK(c, cudaStreamSynchronize(c->stream));
     CK(c, cudaGetLastError());
     if (it_end > c->last_it) c->last_it = it_end;
@@ -885,6 +865,7 @@ const char* fdp_last_error(const fdp_ctx* c) { return c ? c->err.c_str() : g_cre
 void fdp_destroy(fdp_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  fdp::edge_release(c);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase,
                    &c->errbuf, &c->frame_s, &c->frame_v};

@@ -1,9 +1,10 @@
 // Fused time-stepping kernels for the 2-D velocity-stress Biot poroelastic
-// scheme.  One launch of k_stress performs the whole stress phase of a time
-// level (time_loop.F90:93-124), one launch of k_velocity the whole velocity
-// phase including the bottom non-reflecting row (time_loop.F90:133-179), and
-// k_edge the one step with a cross-column dependency (the stress-imaging
-// row 1, hplane_1_velocity.F90:61-76) plus receiver sampling
+// scheme.  The stress phase of a time level (time_loop.F90:93-124) is one
+// launch of k_stress, or k_stress_frame beside k_stress_core (frame/core
+// split); the velocity phase including the bottom non-reflecting row
+// (time_loop.F90:133-179) likewise with k_velocity; k_edge is the one step
+// with a cross-column dependency (the stress-imaging row 1,
+// hplane_1_velocity.F90:61-76) plus receiver sampling
 // (store_seismograms.F90:47-104, store_seismograms_pressure.F90:45-58).
 //
 // Every row routine of the reference (strain_*, stress_*, inh_*, sto_*)
@@ -12,8 +13,10 @@
 // order and the code is compiled without FMA contraction, so a kernel's
 // results equal a serial CPU evaluation of the same routines bit for bit.
 //
-// Threads: one cell per thread, blocks of 32 (x) x 8 (z) cells; a warp is
-// 32 consecutive cells of one row, so every row class is warp-uniform.
+// Threads: blocks of 32 (x) x 8 (z) threads; a warp spans 32 consecutive
+// columns, so every row class is warp-uniform.  The unit kernels give a
+// thread kRZS (stress) or kRZV (velocity) consecutive rows of one column;
+// the core kernels give a thread four consecutive columns of one row.
 //
 // Layout (all arrays x-fastest, the reference's column-major order):
 //   fields   T[NZ + 2*PADZ][pitch], pointer p.F points at (I=PMLL, L=0)
@@ -1374,8 +1377,8 @@ __global__ void __launch_bounds__(kTX * 4) k_velocity_tma(const __grid_constant_
   if (!ok) mbar_wait_bounded(&bar, 0);
 }
 
-__global__ void k_set_base(int* base, int v) { *base = v; }
-__global__ void k_add_base(int* base, int v) { *base += v; }
+static __global__ void k_set_base(int* base, int v) { *base = v; }
+static __global__ void k_add_base(int* base, int v) { *base += v; }
 
 #undef FDP_F
 #undef FDP_R

@@ -31,7 +31,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "--fmad=false", "-std=c++17",
                      "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-SOURCES = ["fdp_engine.cu", "fdp_noalloc.cu", "fdp_prep.cpp", "fdp_io.cpp"]
+SOURCES = ["fdp_engine.cu", "fdp_edge.cu", "fdp_noalloc.cu", "fdp_prep.cpp", "fdp_io.cpp"]
 HOST_EXE = LIB_DIR / "fdp_host"
 
 

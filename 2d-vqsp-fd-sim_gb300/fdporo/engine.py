@@ -139,12 +139,22 @@ class Engine:
         return {"mode": {0: "table", 1: "planes", 2: "biot"}[v[0].value], "planes_stress": v[1].value,
                 "planes_velocity": v[2].value}
 
+    def core_info(self) -> dict:
+        """Core rectangles {phase: (x0, x1, z0, z1)} of the frame/core split
+        (all zero when another kernel variant runs)."""
+        r = np.zeros(8, np.int32)
+        self._check(self.lib.fdp_core_info(self._ctx, _iptr(r)))
+        return {"stress": tuple(int(v) for v in r[:4]), "velocity": tuple(int(v) for v in r[4:])}
+
     def profile(self, it_begin: int, it_end: int) -> dict:
-        """Per-kernel device time (ms) and launch counts over levels it_begin..it_end."""
-        ms = (C.c_double * 3)()
-        n = (C.c_int64 * 3)()
+        """Device time (ms) and launch counts over levels it_begin..it_end of
+        each phase (frame and core together), of the row-1/receiver kernel,
+        and of each phase's core kernel alone."""
+        ms = (C.c_double * 5)()
+        n = (C.c_int64 * 5)()
         self._check(self.lib.fdp_profile_run(self._ctx, it_begin, it_end, ms, n))
-        return {k: (ms[i], n[i]) for i, k in enumerate(("stress", "velocity", "edge"))}
+        return {k: (ms[i], n[i]) for i, k in enumerate(("stress", "velocity", "edge", "stress_core",
+                                                            "velocity_core"))}
 
     # -- state ----------------------------------------------------------------
     def bounds(self, name: str) -> tuple[int, int, int, int]:

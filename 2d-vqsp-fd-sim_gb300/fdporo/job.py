@@ -125,6 +125,14 @@ class Inputs:
         return self.sourtf.shape[0]
 
     @property
+    def pmll(self) -> int:
+        return 1 - self.tpml
+
+    @property
+    def pmlxh(self) -> int:
+        return self.mx + self.tpml
+
+    @property
     def cells(self) -> int:
         return self.nx * self.nz
 

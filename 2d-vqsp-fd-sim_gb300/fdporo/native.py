@@ -1,4 +1,4 @@
-"""ctypes binding of ``libfdp.so`` (include/fdp.h and include/fdp_prep.h).
+"""ctypes binding of ``libfdp.so`` (include/fdp.h, fdp_prep.h, fdp_io.h, fdp_edge.h).
 
 The library is built in-tree by :mod:`fdporo.build`; loading fails loudly if
 it is missing -- there is no CPU fallback for the time-stepping path.
@@ -73,6 +73,7 @@ SIGNATURES = {
     "fdp_kernel_launches": (C.c_int64, [_VP]),
     "fdp_get_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
     "fdp_medium_info": (C.c_int, [_VP, _PI32, _PI32, _PI32]),
+    "fdp_core_info": (C.c_int, [_VP, _PI32]),
     "fdp_profile_run": (C.c_int, [_VP, _I32, _I32, _PD, C.POINTER(C.c_int64)]),
     "fdp_last_error": (C.c_char_p, [_VP]),
     "fdp_receivers_noalloc": (C.c_int, [_I32, _VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _I32, _I32, _VP, _I32,
@@ -87,6 +88,21 @@ SIGNATURES = {
     "fdp_batch_get_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
     "fdp_batch_last_error": (C.c_char_p, [_VP]),
     "fdp_batch_destroy": (None, [_VP]),
+    "fdp_edge_create": (C.c_int, [_I32, C.POINTER(C.c_float), C.c_uint64, C.POINTER(_VP)]),
+    "fdp_edge_set_output": (C.c_int, [_VP, _I32]),
+    "fdp_edge_get_params": (C.c_int, [_VP, C.POINTER(C.c_float)]),
+    "fdp_edge_set_params": (C.c_int, [_VP, C.POINTER(C.c_float)]),
+    "fdp_edge_get_scale": (C.c_int, [_VP, C.POINTER(C.c_float)]),
+    "fdp_edge_set_scale": (C.c_int, [_VP, C.POINTER(C.c_float)]),
+    "fdp_edge_forward": (C.c_int, [_VP, _I32, _PI32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "fdp_edge_gradients": (C.c_int, [_VP, _I32, _PI32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                     C.POINTER(C.c_float), _PD]),
+    "fdp_edge_train_batch": (C.c_int, [_VP, _I32, _PI32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
+                                       _PD]),
+    "fdp_edge_train_level": (C.c_int, [_VP, _VP, _VP, _I32, _I32, C.c_float, _I32, _PD]),
+    "fdp_edge_attach": (C.c_int, [_VP, _VP]),
+    "fdp_edge_last_error": (C.c_char_p, [_VP]),
+    "fdp_edge_destroy": (None, [_VP]),
     "fdp_prep_velocities": (C.c_int, [_I32, _D, _D, _D, _D, _D, _D, _D, _PD, _PD, _PD]),
     "fdp_prep_scale_table": (C.c_int, [_I32, _I32, _D, _D, _VP]),
     "fdp_prep_expand_jm": (C.c_int, [_I32, _I32, _I32, _I32, _PI32, _PI32]),

@@ -74,13 +74,15 @@ def prepare_inputs(precision: str, mt2: int):
     return job.prepare(cfg, med, precision)
 
 
-def algorithmic_bytes(inp, s: int, medium: dict) -> dict:
-    """Compulsory DRAM bytes per launch of each kernel for this workload:
-    every wavefield value the kernel reads or read-modify-writes, the
+def algorithmic_bytes(inp, s: int, medium: dict, core: dict | None = None) -> dict:
+    """Compulsory DRAM bytes per launch of each phase for this workload:
+    every wavefield value the phase reads or read-modify-writes, the
     material coefficients of each cell as the engine holds them (one value
     per distinct coefficient plane, or the JM index in table mode), and
     every PML memory variable it updates (read + write).  Damping profiles
-    and a material table are small and cache-resident and are not counted."""
+    and a material table are small and cache-resident and are not counted.
+    With the core rectangles, also the bytes of each core kernel (its cells
+    only: no PML memory)."""
     nx, nz, tp = inp.nx, inp.nz, inp.tpml
     cells = nx * nz
     if medium["mode"] == "table":
@@ -95,8 +97,19 @@ def algorithmic_bytes(inp, s: int, medium: dict) -> dict:
     vel_mem = (4 * side(tp + 3) + 4 * side(tp + 2) + 2 * side(tp + 2) + 2 * side(tp + 2) + 6 * bottom(tp + 1))
     stress = cells * (4 * s + 8 * s + med_s) + 2 * s * stress_mem
     velocity = cells * (4 * s + 8 * s + med_v) + 2 * s * vel_mem + 2 * s * 12 * nx
-    return {"stress": stress, "velocity": velocity, "per_cell_stress": stress / cells,
-            "per_cell_velocity": velocity / cells}
+    out = {"stress": stress, "velocity": velocity, "per_cell_stress": stress / cells,
+           "per_cell_velocity": velocity / cells}
+    if core:
+        x0, x1, z0, z1 = core["stress"]
+        ns = max(x1 - x0, 0) * max(z1 - z0, 0)
+        if ns and z0 <= inp.lin_z < z1:
+            ns -= x1 - x0  # the source row is not a core row
+        x0, x1, z0, z1 = core["velocity"]
+        nv = max(x1 - x0, 0) * max(z1 - z0, 0)
+        out["stress_core"] = ns * (12 * s + med_s)
+        out["velocity_core"] = nv * (12 * s + med_v)
+        out["core_cells"] = {"stress": ns, "velocity": nv}
+    return out
 
 
 class ClockSampler:
@@ -249,12 +262,18 @@ def run_gpu(args) -> None:
     lo = args.warmup + args.steps + 1
     prof = eng.profile(lo, lo + prof_levels - 1)
     medium = eng.medium_info()
-    alg = algorithmic_bytes(inp, s, medium)
-    kern = max(("stress", "velocity"), key=lambda k: prof[k][0])
-    avg_ms = prof[kern][0] / prof[kern][1]
+    core = eng.core_info()
+    alg = algorithmic_bytes(inp, s, medium, core)
+    phases = ("stress", "velocity", "edge")
+    shares = {k: prof[k][0] / sum(prof[q][0] for q in phases) for k in phases}
     peak, peak_kind = measured_peak_gbs()
+    # the dominant kernel: the longer core kernel (the whole phase when the
+    # engine runs one kernel per phase)
+    cand = [k for k in ("stress_core", "velocity_core") if prof[k][1] > 0] or ["stress", "velocity"]
+    kern = max(cand, key=lambda k: prof[k][0])
+    avg_ms = prof[kern][0] / prof[kern][1]
     achieved = alg[kern] / (avg_ms / 1e3) / 1e9
-    shares = {k: prof[k][0] / sum(v[0] for v in prof.values()) for k in prof}
+    phase_gbs = {k: alg[k] / (prof[k][0] / prof[k][1] / 1e3) / 1e9 for k in ("stress", "velocity")}
     eng.close()
 
     # ---- end to end through the C ABI: one whole shot (create, upload, run, download)
@@ -324,7 +343,8 @@ def run_gpu(args) -> None:
                      "alg_bytes_per_launch": alg[kern], "avg_launch_ms": avg_ms,
                      "alg_bytes_per_cell": {"stress": alg["per_cell_stress"], "velocity": alg["per_cell_velocity"]},
                      "kernel_ms": {k: prof[k][0] / max(prof[k][1], 1) for k in prof},
-                     "medium": medium, "kernel_share": shares},
+                     "phase_gbs": phase_gbs, "phase_frac": {k: v / peak for k, v in phase_gbs.items()},
+                     "core_cells": alg.get("core_cells"), "medium": medium, "phase_share": shares},
         "e2e": e2e,
         "accuracy": accuracy,
         "cpu_baseline": cpu,
@@ -423,6 +443,91 @@ def run_batch(args) -> None:
         print(json.dumps(line), flush=True)
 
 
+EDGE = dict(n=512, margin=256, depth_margin=512, levels=2000, f0=20.0, seed=40000)
+
+
+def _make_edge_pair(item):
+    """One (region, wide target) pair of the learned-edge workload (worker)."""
+    from fdporo import edge as E
+    seed, strip = item
+    return E.make_pair(seed, n=EDGE["n"], margin=EDGE["margin"], depth_margin=EDGE["depth_margin"],
+                       nsteps=EDGE["levels"], f0=EDGE["f0"], strip=strip)
+
+
+def run_edge(args) -> None:
+    """Learned absorbing edge: networks trained on args.edge_train seeded
+    media (region EDGE['n']^2 with a transparent 4-cell strip, target a
+    wide run with the reference 20-cell PML), with runs on their own
+    between teacher-forced levels; evaluated on args.edge_held other media
+    against the strip alone, a 4-cell PML and the reference 20-cell PML.
+    Also times a level of the region with the edge against the region
+    with the 20-cell PML."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    import torch
+    from fdporo import edge as E
+    from fdporo import job
+    L = EDGE["levels"]
+    t0 = time.perf_counter()
+    train_seeds = [(EDGE["seed"] + k, "plain") for k in range(args.edge_train)]
+    held_seeds = [(EDGE["seed"] + 100000 + k, "plain") for k in range(args.edge_held)]
+    ctx = mp.get_context("spawn")
+    ed = None
+    losses = []
+    with ProcessPoolExecutor(max_workers=min(8, os.cpu_count() or 1), mp_context=ctx) as pool:
+        for epoch in range(args.edge_epochs):
+            for k, pair in enumerate(pool.map(_make_edge_pair, train_seeds)):
+                if ed is None:
+                    ed = E.Edge(scale=E.field_scales(pair, levels=L, every=50), seed=EDGE["seed"])
+                    ed.set_output("correct")
+                losses += E.train_pair(ed, pair, levels=L, lr=3e-4, report_every=L, free_every=50, free_run=25)
+        train_s = time.perf_counter() - t0
+        res = {"strip_alone": [], "learned_edge": [], "pml4": [], "pml20": []}
+        for pair in pool.map(_make_edge_pair, held_seeds):
+            res["strip_alone"].append(E.evaluate(pair, L))
+            res["learned_edge"].append(E.evaluate(pair, L, edge=ed))
+            res["pml4"].append(E.evaluate(E.Pair(job.prepare(pair.cfg, pair.medium, "f32"), pair.ext, pair.ox,
+                                                 pair.cfg, pair.medium), L))
+            res["pml20"].append(E.evaluate(pair, L, tpml=20))
+            last = pair
+    summary = {k: {m: float(np.mean([r[m] for r in v])) for m in ("reflected_energy", "seismogram_rel_l2")}
+               for k, v in res.items()}
+    # time per level of the region: learned edge (4-cell strip) vs 20-cell PML
+    def level_ms(inp, edge=None):
+        eng = job.make_engine(inp)
+        if edge is not None:
+            edge.attach(eng)
+        ext = torch.cuda.ExternalStream(eng.stream())
+        eng.time_loop(1, 40)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        eng.time_loop(41, 40 + 320)
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 320
+        if edge is not None:
+            edge.detach(eng)
+        eng.close()
+        return ms
+    ms_edge = level_ms(last.trunc, ed)
+    ms_pml = level_ms(E._with_pml(last, 20))
+    line = {
+        "metric": "learned-edge reflected energy (relative to the target's)", "impl": "gpu",
+        "value": summary["learned_edge"]["reflected_energy"], "unit": "ratio", "higher_is_better": False,
+        "n_gpus": 1, "dtype": "f32 fields, bf16 networks",
+        "data": "synthetic (seeded layered media with Gaussian random fields)",
+        "config": {"workload": "learned-edge", "region": EDGE["n"], "target_grid":
+                   [EDGE["n"] + 2 * EDGE["margin"], EDGE["n"] + EDGE["depth_margin"]], "levels": L,
+                   "train_media": args.edge_train, "held_out_media": args.edge_held, "epochs": args.edge_epochs,
+                   "strip_cells": 4, "network": "96-64-64-8 tanh, one per side and depth"},
+        "held_out_mean": summary, "train_seconds": train_s, "final_train_loss": losses[-1] if losses else None,
+        "level_ms": {"learned_edge_4_cells": ms_edge, "pml_20_cells": ms_pml},
+        "region_speedup_vs_pml20": ms_pml / ms_edge,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,7 +538,10 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--workload", choices=["layered", "batch"], default="layered")
+    ap.add_argument("--workload", choices=["layered", "batch", "edge"], default="layered")
+    ap.add_argument("--edge-train", type=int, default=32)
+    ap.add_argument("--edge-held", type=int, default=8)
+    ap.add_argument("--edge-epochs", type=int, default=1)
     ap.add_argument("--shots", type=int, default=BATCH["shots"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
@@ -443,6 +551,8 @@ def main() -> None:
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "edge":
+        run_edge(args)
     else:
         run_gpu(args)
 

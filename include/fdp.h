@@ -161,11 +161,14 @@ int fdp_synchronize(fdp_ctx* ctx);
  * work, or record its own events, after the engine's. */
 int fdp_get_stream(fdp_ctx* ctx, void** stream);
 
-/* Diagnostics: advances levels it_begin..it_end like fdp_run but launches
- * each kernel separately between CUDA events, waits, and returns the summed
- * device time in milliseconds of each kernel kind in ms_out[0..2] =
- * {stress, velocity, edge} and the number of launches of each in
- * launches_out[0..2]. */
+/* Diagnostics: advances levels it_begin..it_end like fdp_run but without
+ * graphs, with CUDA events around each part of a level, waits, and returns
+ * the summed device time in milliseconds in ms_out[0..4] and the number of
+ * timed launches in launches_out[0..4]: {stress phase, velocity phase,
+ * row 1 and receivers (and an attached learned edge), stress core kernel,
+ * velocity core kernel}.  A phase is its frame and core kernels together
+ * (one kernel with FDP_KERNEL_VARIANT=global or tma, when the core entries
+ * stay 0). */
 int fdp_profile_run(fdp_ctx* ctx, int32_t it_begin, int32_t it_end, double* ms_out, int64_t* launches_out);
 
 /* Number of CUDA kernel launches this context has enqueued since creation
@@ -183,6 +186,11 @@ int64_t fdp_kernel_launches(fdp_ctx* ctx);
  * time; *planes_stress and *planes_velocity count the planes each phase
  * reads per cell. */
 int fdp_medium_info(fdp_ctx* ctx, int32_t* mode, int32_t* planes_stress, int32_t* planes_velocity);
+
+/* Core rectangles of the frame/core split: rect[0..3] = stress core
+ * columns [x0, x1) and rows [z0, z1) (the source row excluded), rect[4..7]
+ * the velocity core; zeros when the context runs other kernels. */
+int fdp_core_info(fdp_ctx* ctx, int32_t* rect8);
 
 /* Last error message of the context (or of the last failed call that has
  * no context -- fdp_create, fdp_receivers_noalloc -- when ctx is NULL). */
