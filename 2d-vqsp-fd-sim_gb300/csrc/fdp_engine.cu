@@ -892,9 +892,9 @@ void fdp_destroy(fdp_ctx* c) {
 struct BatchGroup {
   bool si = false;
   int mode = 0;
-  int first_shot = 0, n = 0;  // shots [first_shot, first_shot + n) of the sorted order
-  int items[3] = {0, 0, 0};   // stress, velocity, edge items at the current m
-  int resident[3] = {0, 0, 0};  // CTAs of each kernel one SM holds
+  int first_shot = 0, n = 0;     // shots [first_shot, first_shot + n) of the sorted order
+  int items[5] = {0, 0, 0, 0, 0};     // stress, velocity, edge, stress core, velocity core items
+  int resident[5] = {0, 0, 0, 0, 0};  // CTAs of each kernel one SM holds
 };
 
 struct fdp_batch {
@@ -902,7 +902,13 @@ struct fdp_batch {
   std::vector<BatchGroup> groups;
   int prec = 4, device = 0;
   cudaStream_t stream = nullptr;
-  DevArr params, first, itbase;  // Params[shots]; per group [3][n+1] first items
+  DevArr params, first, itbase;  // Params[shots]; per group [5][n+1] first items
+  // frame/core split (every shot has one): frame units of all shots, and
+  // per group [2][n] offsets of each shot's stress / velocity units
+  bool framed = false;
+  DevArr units, ubase;
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   int m = 0, waves = 0;          // units per item; persistent CTAs per resident slot (0: one CTA per item)
   bool tuned = false;            // shape fixed (by the caller or by tuning)
   int sms = 0;
@@ -929,7 +935,7 @@ int bfail(fdp_batch* b, int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return bfail((b), FDP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
-// The batched kernels run the unit code over every cell of a shot.
+// Without the frame/core split the batched unit kernels update every cell.
 template <class T> void clear_core(Params<T>& p) {
   p.cs_x0 = p.cs_x1 = p.cs_z0 = p.cs_z1 = 0;
   p.cv_x0 = p.cv_x1 = p.cv_z0 = p.cv_z1 = 0;
@@ -938,25 +944,32 @@ template <class T> void clear_core(Params<T>& p) {
 // first-item offsets of group g inside b->first
 size_t group_first_offset(const fdp_batch* b, size_t g) {
   size_t off = 0;
-  for (size_t k = 0; k < g; ++k) off += (size_t)3 * (b->groups[k].n + 1);
+  for (size_t k = 0; k < g; ++k) off += (size_t)5 * (b->groups[k].n + 1);
   return off;
 }
 
-// Items of each phase per shot at m units per item; uploads the queues.
+// Items of each kernel per shot at m units (core blocks) per item; uploads
+// the queues.
 int batch_queue(fdp_batch* b) {
   std::vector<int> first;
   for (BatchGroup& G : b->groups) {
-    for (int ph = 0; ph < 3; ++ph) {
+    for (int ph = 0; ph < 5; ++ph) {
       int acc = 0;
       for (int s = 0; s < G.n; ++s) {
         const fdp_ctx* c = b->shots[G.first_shot + s];
         first.push_back(acc);
-        if (ph < 2) {
+        if (ph < 2 && b->framed) {
+          acc += ph == 0 ? c->nframe_s : c->nframe_v;
+        } else if (ph < 2) {
           const int rows = fdp::kBZ * (ph == 0 ? fdp::kRZS : fdp::kRZV);
           const int gx = (c->NX + fdp::kBX - 1) / fdp::kBX, gy = (c->NZ + rows - 1) / rows;
           acc += gx * ((gy + b->m - 1) / b->m);
-        } else {
+        } else if (ph == 2) {
           acc += (edge_threads(c) + fdp::kBX * fdp::kBZ - 1) / (fdp::kBX * fdp::kBZ);
+        } else if (b->framed) {
+          const int* r = ph == 3 ? c->cs : c->cv;
+          const int gx = ((r[1] - r[0]) / 4 + fdp::kBX - 1) / fdp::kBX, gy = (r[3] - r[2] + fdp::kBZ - 1) / fdp::kBZ;
+          acc += (r[1] > r[0]) ? gx * ((gy + b->m - 1) / b->m) : 0;
         }
       }
       first.push_back(acc);
@@ -969,11 +982,39 @@ int batch_queue(fdp_batch* b) {
   return FDP_OK;
 }
 
+// Frame units of every shot, copied from the contexts, and their offsets.
+int batch_units(fdp_batch* b) {
+  size_t total = 0;
+  for (const fdp_ctx* c : b->shots) total += (size_t)c->nframe_s + c->nframe_v;
+  cudaError_t e = cudaMalloc(&b->units.p, std::max<size_t>(total, 1) * 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&b->ubase.p, std::max<size_t>(2 * b->shots.size(), 1) * sizeof(int));
+  if (e != cudaSuccess) return bfail(b, FDP_ERR_ALLOC, "frame unit lists: %s", cudaGetErrorString(e));
+  std::vector<int> base(2 * b->shots.size());
+  size_t off = 0;
+  for (const BatchGroup& G : b->groups)
+    for (int ph = 0; ph < 2; ++ph)
+      for (int s = 0; s < G.n; ++s) {
+        const fdp_ctx* c = b->shots[G.first_shot + s];
+        const int n = ph == 0 ? c->nframe_s : c->nframe_v;
+        base[2 * G.first_shot + ph * G.n + s] = (int)off;
+        e = cudaMemcpyAsync((int*)b->units.p + 2 * off, (ph == 0 ? c->frame_s : c->frame_v).p, (size_t)n * 2 * sizeof(int),
+                            cudaMemcpyDeviceToDevice, b->stream);
+        if (e != cudaSuccess) return bfail(b, FDP_ERR_CUDA, "frame unit lists: %s", cudaGetErrorString(e));
+        off += n;
+      }
+  e = cudaMemcpyAsync(b->ubase.p, base.data(), base.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return bfail(b, FDP_ERR_CUDA, "frame unit lists: %s", cudaGetErrorString(e));
+  return FDP_OK;
+}
+
 template <class T, bool SI, int MODE> int group_occupancy(fdp_batch* b, BatchGroup& G) {
   const int threads = fdp::kBX * fdp::kBZ;
   BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[0], fdp::k_stress_batch<T, SI, MODE>, threads, 0));
   BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[1], fdp::k_velocity_batch<T, SI, MODE>, threads, 0));
   BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[2], fdp::k_edge_batch<T, SI>, threads, 0));
+  BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[3], fdp::k_stress_core_batch<T, MODE>, threads, 0));
+  BCK(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&G.resident[4], fdp::k_velocity_core_batch<T, MODE>, threads, 0));
   return FDP_OK;
 }
 
@@ -994,12 +1035,31 @@ int group_grid(const fdp_batch* b, const BatchGroup& G, int kind) {
 template <class T, bool SI, int MODE> void group_level(fdp_batch* b, size_t g, int it_off) {
   const BatchGroup& G = b->groups[g];
   const size_t psize = sizeof(Params<T>);
+  const int* ubase = b->ubase.p ? (const int*)b->ubase.p + 2 * G.first_shot : nullptr;
   const fdp::BatchQueue q{(const char*)b->params.p + psize * G.first_shot,
-                          (const int*)b->first.p + group_first_offset(b, g), G.n, b->m};
+                          (const int*)b->first.p + group_first_offset(b, g), (const int2*)b->units.p, ubase, G.n,
+                          b->m, b->framed ? 1 : 0};
   const dim3 blk(fdp::kBX, fdp::kBZ, 1);
-  fdp::k_stress_batch<T, SI, MODE><<<group_grid(b, G, 0), blk, 0, b->stream>>>(q, G.items[0], it_off);
-  fdp::k_velocity_batch<T, SI, MODE><<<group_grid(b, G, 1), blk, 0, b->stream>>>(q, G.items[1], it_off);
-  b->launches += 2;
+  for (int ph = 0; ph < 2; ++ph) {
+    const bool core = b->framed && G.items[3 + ph] > 0;
+    cudaStream_t fs = core ? b->side : b->stream;
+    if (core) {
+      cudaEventRecord(b->fork, b->stream);
+      cudaStreamWaitEvent(b->side, b->fork, 0);
+    }
+    if (G.items[ph] > 0) {
+      if (ph == 0) fdp::k_stress_batch<T, SI, MODE><<<group_grid(b, G, 0), blk, 0, fs>>>(q, G.items[0], it_off);
+      else fdp::k_velocity_batch<T, SI, MODE><<<group_grid(b, G, 1), blk, 0, fs>>>(q, G.items[1], it_off);
+      b->launches += 1;
+    }
+    if (core) {
+      if (ph == 0) fdp::k_stress_core_batch<T, MODE><<<group_grid(b, G, 3), blk, 0, b->stream>>>(q, G.items[3]);
+      else fdp::k_velocity_core_batch<T, MODE><<<group_grid(b, G, 4), blk, 0, b->stream>>>(q, G.items[4]);
+      cudaEventRecord(b->join, b->side);
+      cudaStreamWaitEvent(b->stream, b->join, 0);
+      b->launches += 1;
+    }
+  }
   if (G.items[2] > 0) {
     fdp::k_edge_batch<T, SI><<<group_grid(b, G, 2), blk, 0, b->stream>>>(q, G.items[2], it_off);
     b->launches += 1;
@@ -1019,7 +1079,8 @@ template <class T> void batch_level(fdp_batch* b, int it_off) {
 
 int batch_launches_per_level(const fdp_batch* b) {
   int n = 0;
-  for (const BatchGroup& G : b->groups) n += 2 + (G.items[2] > 0 ? 1 : 0);
+  for (const BatchGroup& G : b->groups)
+    for (int k = 0; k < 5; ++k) n += G.items[k] > 0 && (k < 3 || b->framed) ? 1 : 0;
   return n;
 }
 
@@ -1155,6 +1216,17 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
   if (e != cudaSuccess) return bail(bfail(b, FDP_ERR_CUDA, "batch stream: %s", cudaGetErrorString(e)));
   for (fdp_ctx* c : b->shots) cudaStreamSynchronize(c->stream);
+  // the frame/core split when every shot has it (else the unit kernels over
+  // every cell); the frame kernels run on a side stream beside the cores
+  b->framed = true;
+  for (const fdp_ctx* c : b->shots) b->framed = b->framed && c->use_core;
+  if (b->framed) {
+    e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+    if (e != cudaSuccess) return bail(bfail(b, FDP_ERR_CUDA, "batch side stream: %s", cudaGetErrorString(e)));
+    if ((rc = batch_units(b)) != FDP_OK) return bail(rc);
+  }
   const size_t psize = b->prec == 8 ? sizeof(Params<double>) : sizeof(Params<float>);
   auto alloc = [&](DevArr& a, size_t bytes) -> int {
     cudaError_t err = cudaMalloc(&a.p, bytes);
@@ -1162,7 +1234,7 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
     a.bytes = bytes;
     return FDP_OK;
   };
-  if ((rc = alloc(b->params, psize * n)) || (rc = alloc(b->first, sizeof(int) * 3 * (n + b->groups.size()))) ||
+  if ((rc = alloc(b->params, psize * n)) || (rc = alloc(b->first, sizeof(int) * 5 * (n + b->groups.size()))) ||
       (rc = alloc(b->itbase, sizeof(int))))
     return bail(rc);
   std::vector<unsigned char> host(psize * n);
@@ -1171,13 +1243,13 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
       Params<double> p;
       fill_params<double>(b->shots[s], p);
       p.it_base = (const int*)b->itbase.p;
-      clear_core(p);
+      if (!b->framed) clear_core(p);
       std::memcpy(&host[psize * s], &p, psize);
     } else {
       Params<float> p;
       fill_params<float>(b->shots[s], p);
       p.it_base = (const int*)b->itbase.p;
-      clear_core(p);
+      if (!b->framed) clear_core(p);
       std::memcpy(&host[psize * s], &p, psize);
     }
   }
@@ -1248,7 +1320,11 @@ void fdp_batch_destroy(fdp_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  for (DevArr* a : {&b->params, &b->first, &b->itbase}) if (a->p) cudaFree(a->p);
+  if (b->side) cudaStreamSynchronize(b->side);
+  for (DevArr* a : {&b->params, &b->first, &b->itbase, &b->units, &b->ubase}) if (a->p) cudaFree(a->p);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }

@@ -892,10 +892,11 @@ __device__ __forceinline__ T core_coef(const Params<T>& p, int k, long long cell
 
 #define FDP_CORE_BOUNDS(T) __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? 2 : 1)
 
+// core block (bx, by) of a phase: 4*kBX columns by kBZ rows of its core
 template <class T, int MODE>
-__global__ void FDP_CORE_BOUNDS(T) k_stress_core(const __grid_constant__ Params<T> p) {
-  const int I0 = p.cs_x0 + 4 * (int)(blockIdx.x * kBX + threadIdx.x);
-  const int L = p.cs_z0 + (int)(blockIdx.y * kBZ + threadIdx.y);
+__device__ __forceinline__ void stress_core_block(const Params<T>& p, int bx, int by) {
+  const int I0 = p.cs_x0 + 4 * (int)(bx * kBX + threadIdx.x);
+  const int L = p.cs_z0 + (int)(by * kBZ + threadIdx.y);
   if (I0 >= p.cs_x1 || L >= p.cs_z1 || L == p.LIN_Z) return;
   const long long P = p.pitch;
   const long long c0 = (long long)L * P + (I0 - p.PMLL);
@@ -955,9 +956,14 @@ __global__ void FDP_CORE_BOUNDS(T) k_stress_core(const __grid_constant__ Params<
 }
 
 template <class T, int MODE>
-__global__ void FDP_CORE_BOUNDS(T) k_velocity_core(const __grid_constant__ Params<T> p) {
-  const int I0 = p.cv_x0 + 4 * (int)(blockIdx.x * kBX + threadIdx.x);
-  const int L = p.cv_z0 + (int)(blockIdx.y * kBZ + threadIdx.y);
+__global__ void FDP_CORE_BOUNDS(T) k_stress_core(const __grid_constant__ Params<T> p) {
+  stress_core_block<T, MODE>(p, (int)blockIdx.x, (int)blockIdx.y);
+}
+
+template <class T, int MODE>
+__device__ __forceinline__ void velocity_core_block(const Params<T>& p, int bx, int by) {
+  const int I0 = p.cv_x0 + 4 * (int)(bx * kBX + threadIdx.x);
+  const int L = p.cv_z0 + (int)(by * kBZ + threadIdx.y);
   if (I0 >= p.cv_x1 || L >= p.cv_z1) return;
   const long long P = p.pitch;
   const long long c0 = (long long)L * P + (I0 - p.PMLL);
@@ -1012,6 +1018,11 @@ __global__ void FDP_CORE_BOUNDS(T) k_velocity_core(const __grid_constant__ Param
   st4(p.UM + c0, oum);
   st4(p.QZ + c0, oqz);
   st4(p.WM + c0, owm);
+}
+
+template <class T, int MODE>
+__global__ void FDP_CORE_BOUNDS(T) k_velocity_core(const __grid_constant__ Params<T> p) {
+  velocity_core_block<T, MODE>(p, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -1080,17 +1091,22 @@ __global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> 
 
 // ---------------------------------------------------------------------------
 // Batched shots.  Every shot of a batch advances one level per launch of
-// each phase.  A phase's work is a queue of items: an item of a cell phase
-// is `m` vertically adjacent units of one shot's grid, an edge item is
-// kBX * kBZ consecutive edge threads of one shot.  Persistent CTAs take the
-// items round-robin and hold the current shot's parameters in shared memory.
+// each kernel.  A kernel's work is a queue of items, taken round-robin by
+// persistent CTAs that hold the current shot's parameters in shared memory:
+// without a core (framed = 0), an item of a cell phase is `m` vertically
+// adjacent units of one shot's grid; with the frame/core split, a frame
+// item is one listed frame unit of a shot and a core item `m` vertically
+// adjacent core blocks; an edge item is kBX * kBZ consecutive edge threads.
 // Shots may differ in grid size, medium, source and receivers, and share
 // precision, free-surface mode and medium representation.
 struct BatchQueue {
   const void* params;  // Params<T>[n]
-  const int* first;    // [3][n+1]: first item of each shot for stress, velocity, edge
+  const int* first;    // [5][n+1]: first item of each shot: stress, velocity, edge, stress core, velocity core
+  const int2* units;   // frame units (bx, by) of every shot and phase
+  const int* ubase;    // [2][n]: offset in `units` of shot s's stress / velocity frame units
   int n;               // shots
-  int m;               // units per cell item
+  int m;               // units (core blocks) per cell item
+  int framed;          // 1: frame/core split
 };
 
 // largest s with first[s] <= item (first[0] = 0, first[n] = items)
@@ -1112,17 +1128,25 @@ __device__ __forceinline__ void batch_load_params(Params<T>& dst, const BatchQue
   for (int k = tid; k < (int)(sizeof(Params<T>) / 4); k += (int)(blockDim.x * blockDim.y)) d[k] = __ldg(src + k);
 }
 
-// phase 0 stress, 1 velocity: units along x and y of a shot's grid
+// units (phase 0 stress, 1 velocity) or core blocks (2 stress, 3 velocity)
+// along x and y of a shot's grid
 template <class T>
 __device__ __forceinline__ int2 batch_units(const Params<T>& p, int phase) {
+  if (phase >= 2) {
+    const int x0 = phase == 2 ? p.cs_x0 : p.cv_x0, x1 = phase == 2 ? p.cs_x1 : p.cv_x1;
+    const int z0 = phase == 2 ? p.cs_z0 : p.cv_z0, z1 = phase == 2 ? p.cs_z1 : p.cv_z1;
+    return make_int2(((x1 - x0) / 4 + kBX - 1) / kBX, (z1 - z0 + kBZ - 1) / kBZ);
+  }
   const int rows = kBZ * (phase == 0 ? kRZS : kRZV);
   return make_int2((p.NX + kBX - 1) / kBX, (p.PMLZH + 1 + rows - 1) / rows);
 }
 
+// PHASE 0/1: units (all of them, or the listed frame units); 2/3: core blocks
 template <class T, bool SI, int MODE, int PHASE>
 __device__ __forceinline__ void batch_cells(const BatchQueue& q, int items, int it_off) {
   __shared__ Params<T> sp;
-  const int* first = q.first + PHASE * (q.n + 1);
+  // queues: 0 stress, 1 velocity, 2 edge, 3 stress core, 4 velocity core
+  const int* first = q.first + (PHASE < 2 ? PHASE : PHASE + 1) * (q.n + 1);
   int cur = -1;
   for (int item = (int)blockIdx.x; item < items; item += (int)gridDim.x) {
     const int s = batch_shot(first, q.n, item);
@@ -1132,13 +1156,21 @@ __device__ __forceinline__ void batch_cells(const BatchQueue& q, int items, int 
       __syncthreads();
       cur = s;
     }
-    const int2 g = batch_units(sp, PHASE);
     const int j = item - __ldg(first + s);
+    if (PHASE < 2 && q.framed) {
+      const int2 u = q.units[__ldg(q.ubase + PHASE * q.n + s) + j];
+      if (PHASE == 0) stress_unit<T, SI, MODE>(sp, u.x, u.y, it_off);
+      else velocity_unit<T, SI, MODE>(sp, u.x, u.y);
+      continue;
+    }
+    const int2 g = batch_units(sp, PHASE);
     const int bx = j % g.x, by0 = (j / g.x) * q.m;
     const int by1 = min(by0 + q.m, g.y);
     for (int by = by0; by < by1; ++by) {
       if (PHASE == 0) stress_unit<T, SI, MODE>(sp, bx, by, it_off);
-      else velocity_unit<T, SI, MODE>(sp, bx, by);
+      else if (PHASE == 1) velocity_unit<T, SI, MODE>(sp, bx, by);
+      else if (PHASE == 2) stress_core_block<T, MODE>(sp, bx, by);
+      else velocity_core_block<T, MODE>(sp, bx, by);
     }
   }
 }
@@ -1151,6 +1183,16 @@ __global__ void __launch_bounds__(kBX * kBZ) k_stress_batch(const __grid_constan
 template <class T, bool SI, int MODE>
 __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity_batch(const __grid_constant__ BatchQueue q, int items, int it_off) {
   batch_cells<T, SI, MODE, 1>(q, items, it_off);
+}
+
+template <class T, int MODE>
+__global__ void FDP_CORE_BOUNDS(T) k_stress_core_batch(const __grid_constant__ BatchQueue q, int items) {
+  batch_cells<T, false, MODE, 2>(q, items, 0);
+}
+
+template <class T, int MODE>
+__global__ void FDP_CORE_BOUNDS(T) k_velocity_core_batch(const __grid_constant__ BatchQueue q, int items) {
+  batch_cells<T, false, MODE, 3>(q, items, 0);
 }
 
 template <class T, bool SI>
