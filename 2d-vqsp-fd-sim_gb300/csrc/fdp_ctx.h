@@ -48,6 +48,7 @@ struct fdp_ctx {
   // kernel on `stream` (fork and join through events, also inside graphs)
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+
   // fdp_profile_run: events around each phase's core kernel
   cudaEvent_t core_ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   int jmnum = 0;

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fdp.h"
@@ -210,7 +211,7 @@ dim3 cell_grid(const fdp_ctx* c, int kind) {
   return dim3((c->NX + fdp::kBX - 1) / fdp::kBX, (c->NZ + rows - 1) / rows, 1);
 }
 
-int edge_threads(const fdp_ctx* c) { return std::max(c->g.stress_imaging ? c->NX : 0, c->mr); }
+int edge_threads(const fdp_ctx* c) { return (c->g.stress_imaging ? c->NX : 0) + c->mr; }
 
 // kind 0 = stress phase, 1 = velocity phase, 2 = edge (imaging row 1 and receivers)
 dim3 tile_grid(const fdp_ctx* c) {
@@ -236,8 +237,8 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
       cudaEventRecord(c->fork, c->stream);
       cudaStreamWaitEvent(c->side, c->fork, 0);
     }
-    if (kind == 0) fdp::k_stress_frame<T, SI, MODE><<<c->nframe_s, blk, 0, fs>>>(p, (const int2*)c->frame_s.p, it_off);
-    else fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v, blk, 0, fs>>>(p, (const int2*)c->frame_v.p);
+    if (kind == 0) fdp::k_stress_frame<T, SI, MODE><<<c->nframe_s, blk, 0, fs>>>(p, (const int4*)c->frame_s.p, it_off);
+    else fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v, blk, 0, fs>>>(p, (const int4*)c->frame_v.p);
     if (core) {
       if (c->core_ev[kind][0]) cudaEventRecord(c->core_ev[kind][0], c->stream);
       if (kind == 0) fdp::k_stress_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
@@ -272,27 +273,46 @@ int plan_core(fdp_ctx* c) {
   rect(c->cs, 3, c->g.stress_imaging ? 5 : 2);
   rect(c->cv, 4, 2);
   auto in = [](const int r[4], int I, int L) { return I >= r[0] && I < r[1] && L >= r[2] && L < r[3]; };
-  const int gx = (c->NX + fdp::kBX - 1) / fdp::kBX;
+  // frame units: the columns split at the core's edges ([PMLL, x0), [x0,
+  // x1), [x1, PMLXH]) so that no unit straddles a core edge, units of kBX
+  // columns from each segment's start; a unit is listed when it holds a
+  // cell outside the core
   std::vector<int> us, uv;
   for (int ph = 0; ph < 2; ++ph) {
     const int rows = fdp::kBZ * (ph == 0 ? fdp::kRZS : fdp::kRZV);
     const int gy = (c->NZ + rows - 1) / rows;
     const int* r = ph == 0 ? c->cs : c->cv;
     std::vector<int>& out = ph == 0 ? us : uv;
-    for (int by = 0; by < gy; ++by)
-      for (int bx = 0; bx < gx; ++bx) {
-        // rows of the unit: stress from row 0 down, velocity from row PMLZH up
-        const int la = ph == 0 ? by * rows : c->PMLZH - (by + 1) * rows + 1;
-        const int lb = la + rows - 1;
-        bool frame = false;
-        for (int L = std::max(la, 0); L <= std::min(lb, c->PMLZH) && !frame; ++L)
-          for (int I = c->PMLL + bx * fdp::kBX; I <= std::min(c->PMLL + bx * fdp::kBX + fdp::kBX - 1, c->PMLXH); ++I)
-            if (!in(r, I, L) || (ph == 0 && L == c->g.lin_z)) { frame = true; break; }
-        if (frame) { out.push_back(bx); out.push_back(by); }
+    std::vector<std::pair<int, int>> segs;
+    if (r[1] > r[0]) segs = {{c->PMLL, r[0]}, {r[0], r[1]}, {r[1], c->PMLXH + 1}};
+    else segs = {{c->PMLL, c->PMLXH + 1}};
+    // stress: units of kBZ*kRZS rows from row 0 down; velocity: units of
+    // kBZ rows with one row per thread up to row PMLZH-3 (short threads for
+    // the latency-bound PML cells), then the bottom three rows, one column
+    // per thread, kBX*kBZ columns per unit
+    if (ph == 1)
+      for (int I0 = c->PMLL; I0 <= c->PMLXH; I0 += fdp::kBX * fdp::kBZ) {
+        out.push_back(I0); out.push_back(std::min(I0 + fdp::kBX * fdp::kBZ, c->PMLXH + 1));
+        out.push_back(0); out.push_back(2);
       }
+    const int nbands = ph == 0 ? gy : (c->PMLZH - 3 + 1 + fdp::kBZ - 1) / fdp::kBZ;
+    for (int by = 0; by < nbands; ++by) {
+      int la, lb, tag, w;
+      if (ph == 0) { la = by * rows; lb = la + rows - 1; tag = by; w = 0; }
+      else { la = by * fdp::kBZ; lb = std::min(la + fdp::kBZ - 1, c->PMLZH - 3); tag = la; w = 1; }
+      for (const auto& sg : segs)
+        for (int I0 = sg.first; I0 < sg.second; I0 += fdp::kBX) {
+          const int I1 = std::min(I0 + fdp::kBX, sg.second);
+          bool frame = false;
+          for (int L = std::max(la, 0); L <= std::min(lb, c->PMLZH) && !frame; ++L)
+            for (int I = I0; I < I1; ++I)
+              if (!in(r, I, L) || (ph == 0 && L == c->g.lin_z)) { frame = true; break; }
+          if (frame) { out.push_back(I0); out.push_back(I1); out.push_back(tag); out.push_back(w); }
+        }
+    }
   }
-  c->nframe_s = (int)us.size() / 2;
-  c->nframe_v = (int)uv.size() / 2;
+  c->nframe_s = (int)us.size() / 4;
+  c->nframe_v = (int)uv.size() / 4;
   int rc;
   if ((rc = dev_alloc(c, c->frame_s, us.size() * sizeof(int))) != FDP_OK) return rc;
   if ((rc = dev_alloc(c, c->frame_v, uv.size() * sizeof(int))) != FDP_OK) return rc;
@@ -322,6 +342,11 @@ template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_o
   return FDP_OK;
 }
 
+int level_launches(const fdp_ctx* c) {
+  const int cores = c->use_core ? (c->cs[1] > c->cs[0]) + (c->cv[1] > c->cv[0]) : 0;
+  return 2 + cores + (edge_threads(c) > 0 ? 1 : 0) + (c->edge && c->edge_attached ? 3 : 0);
+}
+
 template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
   Params<T> p;
   fill_params<T>(c, p);
@@ -349,9 +374,7 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) { c->graph = nullptr; return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
   }
-  const int per_level = 2 + (edge_threads(c) > 0 ? 1 : 0) +
-                        (c->use_core ? (c->cs[1] > c->cs[0]) + (c->cv[1] > c->cv[0]) : 0) +
-                        (c->edge && c->edge_attached ? 3 : 0);
+  const int per_level = level_launches(c);
   while (it_end - it + 1 >= kChunk && c->graph) {
     CK(c, cudaGraphLaunch(c->graph, c->stream));
     c->launches += (long long)kChunk * per_level + 1;
@@ -367,6 +390,16 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
   return FDP_OK;
 }
 
+// Runs fn(begin, end) over [0, n) split across the host's cores.
+template <class F> void parallel_for(size_t n, F fn) {
+  const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t nt = std::min(hw, std::max<size_t>(1, n / 65536));
+  if (nt <= 1) { fn((size_t)0, n); return; }
+  std::vector<std::thread> th;
+  for (size_t t = 0; t < nt; ++t) th.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+  for (auto& x : th) x.join();
+}
+
 template <class T>
 void derive_table(const int32_t jmnum, const T* tab, std::vector<T>& out) {
   // table24 columns (.MO record order, read_model_par.F90:147-155)
@@ -374,7 +407,8 @@ void derive_table(const int32_t jmnum, const T* tab, std::vector<T>& out) {
          R1QX, R1QZ, R2QX, R2QZ, R3QX, R3QZ, AUXW, AUXQZ };
   const size_t ld = (size_t)jmnum + 1;
   out.assign(ld * fdp::C_NCOEF, T(0));
-  for (int j = 1; j <= jmnum; ++j) {
+  parallel_for((size_t)jmnum, [&](size_t jb, size_t je) {
+  for (int j = (int)jb + 1; j <= (int)je; ++j) {
     const T* r = tab + (size_t)(j - 1) * 24;
     auto put = [&](int k, T v) { out[(size_t)k * ld + j] = v; };
     put(fdp::C_MU, r[MU]);
@@ -392,11 +426,25 @@ void derive_table(const int32_t jmnum, const T* tab, std::vector<T>& out) {
     put(fdp::C_R1W, r[R1W]); put(fdp::C_R3W, r[R3W]);
     put(fdp::C_AUXW, r[AUXW]); put(fdp::C_AUXQZ, r[AUXQZ]);
   }
+  });
 }
 
 // Materials at most this many use table mode when some coefficient varies;
 // a larger table (one material per cell) is expanded into per-cell planes.
 constexpr int kMaxTableMaterials = 4096;
+
+// 64-bit FNV-1a hash of a column's bit patterns (negated when asked).
+template <class T> uint64_t column_hash(const T* a, size_t n, bool negate) {
+  using U = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
+  const U sign = (U)1 << (sizeof(T) * 8 - 1);
+  uint64_t h = 1469598103934665603ULL;
+  for (size_t i = 0; i < n; ++i) {
+    U x;
+    std::memcpy(&x, &a[i], sizeof(T));
+    h = (h ^ (uint64_t)(negate ? (x ^ sign) : x)) * 1099511628211ULL;
+  }
+  return h;
+}
 
 template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate) {
   using U = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
@@ -429,23 +477,43 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
   }
   if ((rc = dev_alloc(c, c->aux, aux.size() * sizeof(T))) != FDP_OK) return rc;
   if ((rc = copy_sync(c, c->aux.p, aux.data(), aux.size() * sizeof(T), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
-  // column classification (the AUXIL columns are served by `aux` above)
+  // column classification (the AUXIL columns are served by `aux` above):
+  // constant columns, and hashes of every column and of its negation, in
+  // parallel; a hash match is confirmed by comparing every bit
+  bool constant[fdp::C_NCOEF];
+  uint64_t hpos[fdp::C_NCOEF], hneg[fdp::C_NCOEF];
+  {
+    auto classify = [&](int k) {
+      const T* col = &t[(size_t)k * ld + 1];
+      bool cst = true;
+      for (int j = 1; j < jmnum && cst; ++j) cst = same_bits(&col[0], &col[j], 1, false);
+      constant[k] = cst;
+      hpos[k] = cst ? 0 : column_hash(col, (size_t)jmnum, false);
+      hneg[k] = cst ? 0 : column_hash(col, (size_t)jmnum, true);
+    };
+    if (jmnum < 65536) {
+      for (int k = 0; k < fdp::C_NCOEF; ++k) classify(k);
+    } else {
+      std::vector<std::thread> th;
+      for (int k = 0; k < fdp::C_NCOEF; ++k) th.emplace_back(classify, k);
+      for (auto& x : th) x.join();
+    }
+  }
   std::vector<int> plane_col;
   for (int k = 0; k < fdp::C_NCOEF; ++k) {
     c->src[k] = -1; c->neg[k] = 0; c->cval_d[k] = 0; c->cval_f[k] = 0;
     if (k == fdp::C_AUXW || k == fdp::C_AUXQZ) continue;
     const T* col = &t[(size_t)k * ld + 1];
-    bool constant = true;
-    for (int j = 1; j < jmnum && constant; ++j) constant = same_bits(&col[0], &col[j], 1, false);
-    if (constant) {
+    if (constant[k]) {
       c->cval_d[k] = (double)col[0];
       c->cval_f[k] = (float)col[0];
       continue;
     }
     for (size_t q = 0; q < plane_col.size() && c->src[k] < 0; ++q) {
-      const T* other = &t[(size_t)plane_col[q] * ld + 1];
-      if (same_bits(other, col, (size_t)jmnum, false)) { c->src[k] = (int)q; c->neg[k] = 0; }
-      else if (same_bits(other, col, (size_t)jmnum, true)) { c->src[k] = (int)q; c->neg[k] = 1; }
+      const int o = plane_col[q];
+      const T* other = &t[(size_t)o * ld + 1];
+      if (hpos[o] == hpos[k] && same_bits(other, col, (size_t)jmnum, false)) { c->src[k] = (int)q; c->neg[k] = 0; }
+      else if (hpos[o] == hneg[k] && same_bits(other, col, (size_t)jmnum, true)) { c->src[k] = (int)q; c->neg[k] = 1; }
     }
     if (c->src[k] < 0) { c->src[k] = (int)plane_col.size(); plane_col.push_back(k); }
   }
@@ -472,19 +540,23 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
     dev_alloc(c, c->jm, 0);
     dev_alloc(c, c->coef, 0);
     if ((rc = dev_alloc(c, c->planes, std::max<size_t>(1, (size_t)c->nplanes * cells) * sizeof(T))) != FDP_OK) return rc;
-    std::vector<T> pl(cells);
-    for (int q = 0; q < c->nplanes; ++q) {
-      const T* col = &t[(size_t)plane_col[q] * ld];
-      std::fill(pl.begin(), pl.end(), col[1]);
-      for (int L = 0; L < c->NZ; ++L) {
-        T* dst = &pl[(size_t)(L + kPadZ) * c->pitch + kPadX];
+    // every plane expanded over the padded layout (padding holds material
+    // 1), rows in parallel, then one copy
+    std::vector<T> pl((size_t)c->nplanes * cells);
+    parallel_for((size_t)c->nplanes * c->rows_alloc, [&](size_t b, size_t e) {
+      for (size_t r = b; r < e; ++r) {
+        const int q = (int)(r / c->rows_alloc), row = (int)(r % c->rows_alloc);
+        const T* col = &t[(size_t)plane_col[q] * ld];
+        T* dst = &pl[(size_t)q * cells + (size_t)row * c->pitch];
+        const int L = row - kPadZ;
+        if (L < 0 || L >= c->NZ) { std::fill(dst, dst + c->pitch, col[1]); continue; }
+        std::fill(dst, dst + kPadX, col[1]);
         const int32_t* src = jm + (size_t)L * c->NX;
-        for (int x = 0; x < c->NX; ++x) dst[x] = col[src[x]];
+        for (int x = 0; x < c->NX; ++x) dst[kPadX + x] = col[src[x]];
+        std::fill(dst + kPadX + c->NX, dst + c->pitch, col[1]);
       }
-      if ((rc = copy_sync(c, (T*)c->planes.p + (size_t)q * cells, pl.data(), cells * sizeof(T),
-                          cudaMemcpyHostToDevice)) != FDP_OK)
-        return rc;
-    }
+    });
+    if ((rc = copy_sync(c, c->planes.p, pl.data(), pl.size() * sizeof(T), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
   }
   return FDP_OK;
 }
@@ -554,6 +626,7 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
     e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+
     if (e != cudaSuccess) { c->err = std::string("side stream: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
   }
   if (c->use_tma) {
@@ -876,6 +949,7 @@ void fdp_destroy(fdp_ctx* c) {
   if (c->side) cudaStreamSynchronize(c->side);
   if (c->fork) cudaEventDestroy(c->fork);
   if (c->join) cudaEventDestroy(c->join);
+
   if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -986,7 +1060,7 @@ int batch_queue(fdp_batch* b) {
 int batch_units(fdp_batch* b) {
   size_t total = 0;
   for (const fdp_ctx* c : b->shots) total += (size_t)c->nframe_s + c->nframe_v;
-  cudaError_t e = cudaMalloc(&b->units.p, std::max<size_t>(total, 1) * 2 * sizeof(int));
+  cudaError_t e = cudaMalloc(&b->units.p, std::max<size_t>(total, 1) * 4 * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&b->ubase.p, std::max<size_t>(2 * b->shots.size(), 1) * sizeof(int));
   if (e != cudaSuccess) return bfail(b, FDP_ERR_ALLOC, "frame unit lists: %s", cudaGetErrorString(e));
   std::vector<int> base(2 * b->shots.size());
@@ -997,7 +1071,7 @@ int batch_units(fdp_batch* b) {
         const fdp_ctx* c = b->shots[G.first_shot + s];
         const int n = ph == 0 ? c->nframe_s : c->nframe_v;
         base[2 * G.first_shot + ph * G.n + s] = (int)off;
-        e = cudaMemcpyAsync((int*)b->units.p + 2 * off, (ph == 0 ? c->frame_s : c->frame_v).p, (size_t)n * 2 * sizeof(int),
+        e = cudaMemcpyAsync((int*)b->units.p + 4 * off, (ph == 0 ? c->frame_s : c->frame_v).p, (size_t)n * 4 * sizeof(int),
                             cudaMemcpyDeviceToDevice, b->stream);
         if (e != cudaSuccess) return bfail(b, FDP_ERR_CUDA, "frame unit lists: %s", cudaGetErrorString(e));
         off += n;
@@ -1037,7 +1111,7 @@ template <class T, bool SI, int MODE> void group_level(fdp_batch* b, size_t g, i
   const size_t psize = sizeof(Params<T>);
   const int* ubase = b->ubase.p ? (const int*)b->ubase.p + 2 * G.first_shot : nullptr;
   const fdp::BatchQueue q{(const char*)b->params.p + psize * G.first_shot,
-                          (const int*)b->first.p + group_first_offset(b, g), (const int2*)b->units.p, ubase, G.n,
+                          (const int*)b->first.p + group_first_offset(b, g), (const int4*)b->units.p, ubase, G.n,
                           b->m, b->framed ? 1 : 0};
   const dim3 blk(fdp::kBX, fdp::kBZ, 1);
   for (int ph = 0; ph < 2; ++ph) {

@@ -491,18 +491,18 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
 }
 
 // One thread per kRZS cells of a column; a unit of kBX x kBZ threads covers
-// kBX columns and kBZ*kRZS rows.  Units tile the grid from row 0 down, so
-// unit row 0 holds rows 2..4 that the stress-imaging mirror rows 0 and 1
-// copy.  (bx, by) is the unit's position; k_stress runs one unit per block,
-// the batched kernels several per block.
+// kBX columns (from I0, none at or beyond I1 <= PMLXH+1) and kBZ*kRZS rows.
+// Unit rows tile the grid from row 0 down, so unit row 0 holds rows 2..4
+// that the stress-imaging mirror rows 0 and 1 copy.  k_stress runs one unit
+// per block, the frame and batched kernels the units of their lists.
 template <class T, bool SI, int MODE>
-__device__ __forceinline__ void stress_unit(const Params<T>& p, int bx, int by, int it_off) {
-  const int I = p.PMLL + (int)(bx * kBX + threadIdx.x);
+__device__ __forceinline__ void stress_unit(const Params<T>& p, int I0, int I1, int by, int it_off) {
+  const int I = I0 + (int)threadIdx.x;
   const int L0 = (int)(by * kBZ + threadIdx.y) * kRZS;  // rows L0 .. L0+kRZS-1
   const bool core = p.cs_x1 > p.cs_x0;  // the core kernel updates the core cells
-  if (!core && stress_fast_rows(p, I, L0)) {
+  if (!core && I1 > p.PMLXH && stress_fast_rows(p, I, L0)) {
     stress_interior_rows<T, MODE>(p, I, L0);
-  } else if (I <= p.PMLXH) {
+  } else if (I < I1) {
     const int it = *p.it_base + it_off;
     const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
     const bool incol = I >= p.cs_x0 && I < p.cs_x1;
@@ -513,7 +513,7 @@ __device__ __forceinline__ void stress_unit(const Params<T>& p, int bx, int by, 
   }
   if (SI && by == 0) {
     __syncthreads();  // rows 2..4 of this unit are final
-    if (I <= p.PMLXH && threadIdx.y == 0) {
+    if (I < I1 && threadIdx.y == 0) {
       // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53
       FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
       FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
@@ -528,7 +528,7 @@ __device__ __forceinline__ void stress_unit(const Params<T>& p, int bx, int by, 
 
 template <class T, bool SI, int MODE>
 __global__ void __launch_bounds__(kBX * kBZ) k_stress(const __grid_constant__ Params<T> p, int it_off) {
-  stress_unit<T, SI, MODE>(p, (int)blockIdx.x, (int)blockIdx.y, it_off);
+  stress_unit<T, SI, MODE>(p, p.PMLL + (int)blockIdx.x * kBX, p.PMLXH + 1, (int)blockIdx.y, it_off);
 }
 
 // ---------------------------------------------------------------------------
@@ -772,13 +772,13 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
 // values wait in the thread's own slots of shared memory while it updates
 // those rows.
 template <class T, bool SI, int MODE>
-__device__ __forceinline__ void velocity_unit(const Params<T>& p, int bx, int by) {
+__device__ __forceinline__ void velocity_unit(const Params<T>& p, int I0, int I1, int by) {
   static_assert(kRZV >= 3, "the bottom row needs two rows above it in the same thread");
   __shared__ T old[3][4][kBX];  // pre-phase values of rows PMLZH-k, k = 0..2
-  const int I = p.PMLL + (int)(bx * kBX + threadIdx.x);
+  const int I = I0 + (int)threadIdx.x;
   const int L1 = p.PMLZH - (int)(by * kBZ + (kBZ - 1 - threadIdx.y)) * kRZV;  // last row
   const int L0 = L1 - kRZV + 1;                                                         // first row
-  const bool inx = I <= p.PMLXH;
+  const bool inx = I < I1;
   const bool me = inx && L1 == p.PMLZH;  // this thread updates the bottom row
   const int tx = threadIdx.x;
   if (me) {
@@ -789,7 +789,7 @@ __device__ __forceinline__ void velocity_unit(const Params<T>& p, int bx, int by
     }
   }
   const bool core = p.cv_x1 > p.cv_x0;  // the core kernel updates the core cells
-  if (!core && velocity_fast_rows(p, I, L0)) {
+  if (!core && I1 > p.PMLXH && velocity_fast_rows(p, I, L0)) {
     velocity_interior_rows<T, MODE>(p, I, L0);
   } else if (inx) {
     const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
@@ -823,7 +823,7 @@ __device__ __forceinline__ void velocity_unit(const Params<T>& p, int bx, int by
 template <class T, bool SI, int MODE>
 __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity(const __grid_constant__ Params<T> p, int it_off) {
   (void)it_off;
-  velocity_unit<T, SI, MODE>(p, (int)blockIdx.x, (int)blockIdx.y);
+  velocity_unit<T, SI, MODE>(p, p.PMLL + (int)blockIdx.x * kBX, p.PMLXH + 1, (int)blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -835,18 +835,77 @@ __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity(const __grid_constant__ Params
 // stencils everywhere, no source row), so the core kernels are the interior
 // branches of stress_cell / velocity_cell, same expressions in the same
 // order, for four cells at a time.
+// A frame unit: columns [x, y) (at most kBX), unit row z.
 template <class T, bool SI, int MODE>
 __global__ void __launch_bounds__(kBX * kBZ) k_stress_frame(const __grid_constant__ Params<T> p,
-                                                            const int2* __restrict__ units, int it_off) {
-  const int2 u = units[blockIdx.x];
-  stress_unit<T, SI, MODE>(p, u.x, u.y, it_off);
+                                                            const int4* __restrict__ units, int it_off) {
+  const int4 u = units[blockIdx.x];
+  stress_unit<T, SI, MODE>(p, u.x, u.y, u.z, it_off);
+}
+
+// Velocity frame cells up to row PMLZH-3, one row per thread: columns
+// [I0, I1), rows L0 .. L0+kBZ-1.
+template <class T, bool SI, int MODE>
+__device__ __forceinline__ void velocity_row_unit(const Params<T>& p, int I0, int I1, int L0) {
+  const int I = I0 + (int)threadIdx.x;
+  const int L = L0 + (int)threadIdx.y;
+  const bool incore = I >= p.cv_x0 && I < p.cv_x1 && L >= p.cv_z0 && L < p.cv_z1;
+  if (I < I1 && L <= p.PMLZH - 3 && L >= (SI ? 2 : 0) && !incore) {
+    const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
+    velocity_cell<T, SI, MODE>(p, rd, I, L);
+  }
+}
+
+// The bottom three rows of columns [I0, I1) (at most kBX*kBZ), one column
+// per thread: rows PMLZH-2 and PMLZH-1, then the bottom row from their new
+// and pre-phase values and the history (time_loop.F90:133-155,
+// hplane_pmlzh0_velocity.F90:34-63).
+template <class T, bool SI, int MODE>
+__device__ __forceinline__ void velocity_bottom_unit(const Params<T>& p, int I0, int I1) {
+  const int I = I0 + (int)(threadIdx.y * kBX + threadIdx.x);
+  if (I >= I1) return;
+  const int LST = p.PMLZH;
+  T old[3][4];  // pre-phase values of rows PMLZH-k of u, w, qx, qz
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    old[k][0] = FDP_F(p.UM, I, LST - k); old[k][1] = FDP_F(p.WM, I, LST - k);
+    old[k][2] = FDP_F(p.QX, I, LST - k); old[k][3] = FDP_F(p.QZ, I, LST - k);
+  }
+  const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
+  const bool incol = I >= p.cv_x0 && I < p.cv_x1;
+  for (int L = LST - 2; L < LST; ++L)
+    if (L >= (SI ? 2 : 0) && !(incol && L >= p.cv_z0 && L < p.cv_z1)) velocity_cell<T, SI, MODE>(p, rd, I, L);
+  const int x = I - p.PMLL;
+  T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
+    T* hist = p.HIST + (long long)c * 3 * p.NX;
+    const T sp0 = hist[x], sp1 = hist[p.NX + x], sp2 = hist[2 * p.NX + x];
+    const T v = ab[0] * FDP_F(f[c], I, LST - 1) + ab[1] * FDP_F(f[c], I, LST - 2)
+              + ab[2] * old[0][c] + ab[3] * old[1][c] + ab[4] * old[2][c]
+              + ab[5] * sp0 + ab[6] * sp1 + ab[7] * sp2;
+    FDP_F(f[c], I, LST) = v;
+    hist[x] = old[0][c];
+    hist[p.NX + x] = old[1][c];
+    hist[2 * p.NX + x] = old[2][c];
+  }
+}
+
+// A velocity frame unit: (first column, end column, first row, 1) one row
+// per thread up to row PMLZH-3; (first column, end column, 0, 2) the bottom
+// three rows; (first column, end column, unit row, 0) the four-row layout.
+template <class T, bool SI, int MODE>
+__device__ __forceinline__ void velocity_frame_unit(const Params<T>& p, const int4 u) {
+  if (u.w == 1) velocity_row_unit<T, SI, MODE>(p, u.x, u.y, u.z);
+  else if (u.w == 2) velocity_bottom_unit<T, SI, MODE>(p, u.x, u.y);
+  else velocity_unit<T, SI, MODE>(p, u.x, u.y, u.z);
 }
 
 template <class T, bool SI, int MODE>
 __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity_frame(const __grid_constant__ Params<T> p,
-                                                        const int2* __restrict__ units) {
-  const int2 u = units[blockIdx.x];
-  velocity_unit<T, SI, MODE>(p, u.x, u.y);
+                                                        const int4* __restrict__ units) {
+  velocity_frame_unit<T, SI, MODE>(p, units[blockIdx.x]);
 }
 
 template <class T> struct V4 { T v[4]; };
@@ -1050,13 +1109,16 @@ __device__ __forceinline__ T final_value(const Params<T>& p, int c, int I, int L
   return FDP_F(f, I, L);
 }
 
-// Row 1 under stress imaging (threads 0..NX-1) and receiver sampling
-// (threads 0..MR-1).  Sampling recomputes row-1 values instead of reading
-// them, so it does not depend on the order in which threads write row 1.
+// Row 1 under stress imaging (threads 0..NX-1) and receiver sampling (the
+// next MR threads): no thread does both, so neither chain of loads waits
+// for the other.
+// Sampling recomputes row-1 values instead of reading them, so it does not
+// depend on the order in which threads write row 1.
 // g is the thread's index within the shot.
 template <class T, bool SI>
 __device__ __forceinline__ void edge_thread(const Params<T>& p, int g, int it_off) {
-  if (SI) {
+  const int nsi = SI ? p.NX : 0;  // threads 0..nsi-1: row 1; the next MR: receivers
+  if (g < nsi) {
     const int I = p.PMLL + g;
     if (I <= p.PMLXH && I >= 3 - p.TPML && I <= p.MX - 1 + p.TPML) {
       const T u = si_row1(p, 0, I), qx = si_row1(p, 2, I);
@@ -1070,23 +1132,39 @@ __device__ __forceinline__ void edge_thread(const Params<T>& p, int g, int it_of
       if (wq) { FDP_F(p.WM, I, 1) = w; FDP_F(p.QZ, I, 1) = qz; }
     }
   }
-  if (g < p.MR) {
+  g -= nsi;
+  if (g >= 0 && g < p.MR) {
     const int it = *p.it_base + it_off;
     const int IX = p.REC[4 * g], LX = p.REC[4 * g + 1], IZ = p.REC[4 * g + 2], LZ = p.REC[4 * g + 3];
     auto inside = [&](int i, int l) { return i >= p.PMLL && i <= p.PMLXH && l >= 0 && l <= p.PMLZH; };
-    T s[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    T s[4] = {T(0), T(0), T(0), T(0)};
     if (inside(IX, LX)) { s[0] = final_value<T, SI>(p, 0, IX, LX); s[2] = final_value<T, SI>(p, 2, IX, LX); }
     if (inside(IZ, LZ)) { s[1] = -final_value<T, SI>(p, 1, IZ, LZ); s[3] = -final_value<T, SI>(p, 3, IZ, LZ); }
-    if (inside(IZ, LX)) { s[4] = FDP_F(p.PRES, IZ, LX); s[5] = -FDP_F(p.TXX, IZ, LX); }
     T* out = p.RAW + ((long long)(it - 1) * p.MR + g) * 6;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) out[k] = s[k];
+    for (int k = 0; k < 4; ++k) out[k] = s[k];
   }
+}
+
+// The stress samples of receiver g (store_seismograms_pressure.F90:45-58):
+// p and -txx at (IRECZ, LRECX).  The velocity phase leaves the stresses
+// alone, so they can be taken any time after the stress phase.
+template <class T>
+__device__ __forceinline__ void stress_sample_thread(const Params<T>& p, int g, int it_off) {
+  if (g < 0 || g >= p.MR) return;
+  const int it = *p.it_base + it_off;
+  const int LX = p.REC[4 * g + 1], IZ = p.REC[4 * g + 2];
+  const bool in = IZ >= p.PMLL && IZ <= p.PMLXH && LX >= 0 && LX <= p.PMLZH;
+  T* out = p.RAW + ((long long)(it - 1) * p.MR + g) * 6;
+  out[4] = in ? FDP_F(p.PRES, IZ, LX) : T(0);
+  out[5] = in ? -FDP_F(p.TXX, IZ, LX) : T(0);
 }
 
 template <class T, bool SI>
 __global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> p, int it_off) {
-  edge_thread<T, SI>(p, (int)(blockIdx.x * blockDim.x + threadIdx.x), it_off);
+  const int g = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  edge_thread<T, SI>(p, g, it_off);
+  stress_sample_thread<T>(p, g - (SI ? p.NX : 0), it_off);
 }
 
 // ---------------------------------------------------------------------------
@@ -1102,7 +1180,7 @@ __global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> 
 struct BatchQueue {
   const void* params;  // Params<T>[n]
   const int* first;    // [5][n+1]: first item of each shot: stress, velocity, edge, stress core, velocity core
-  const int2* units;   // frame units (bx, by) of every shot and phase
+  const int4* units;   // frame units (first column, end column, unit row) of every shot and phase
   const int* ubase;    // [2][n]: offset in `units` of shot s's stress / velocity frame units
   int n;               // shots
   int m;               // units (core blocks) per cell item
@@ -1158,17 +1236,17 @@ __device__ __forceinline__ void batch_cells(const BatchQueue& q, int items, int 
     }
     const int j = item - __ldg(first + s);
     if (PHASE < 2 && q.framed) {
-      const int2 u = q.units[__ldg(q.ubase + PHASE * q.n + s) + j];
-      if (PHASE == 0) stress_unit<T, SI, MODE>(sp, u.x, u.y, it_off);
-      else velocity_unit<T, SI, MODE>(sp, u.x, u.y);
+      const int4 u = q.units[__ldg(q.ubase + PHASE * q.n + s) + j];
+      if (PHASE == 0) stress_unit<T, SI, MODE>(sp, u.x, u.y, u.z, it_off);
+      else velocity_frame_unit<T, SI, MODE>(sp, u);
       continue;
     }
     const int2 g = batch_units(sp, PHASE);
     const int bx = j % g.x, by0 = (j / g.x) * q.m;
     const int by1 = min(by0 + q.m, g.y);
     for (int by = by0; by < by1; ++by) {
-      if (PHASE == 0) stress_unit<T, SI, MODE>(sp, bx, by, it_off);
-      else if (PHASE == 1) velocity_unit<T, SI, MODE>(sp, bx, by);
+      if (PHASE == 0) stress_unit<T, SI, MODE>(sp, sp.PMLL + bx * kBX, sp.PMLXH + 1, by, it_off);
+      else if (PHASE == 1) velocity_unit<T, SI, MODE>(sp, sp.PMLL + bx * kBX, sp.PMLXH + 1, by);
       else if (PHASE == 2) stress_core_block<T, MODE>(sp, bx, by);
       else velocity_core_block<T, MODE>(sp, bx, by);
     }
@@ -1209,7 +1287,9 @@ __global__ void __launch_bounds__(kBX * kBZ) k_edge_batch(const __grid_constant_
       __syncthreads();
       cur = s;
     }
-    edge_thread<T, SI>(sp, (item - __ldg(first + s)) * (kBX * kBZ) + tid, it_off);
+    const int g = (item - __ldg(first + s)) * (kBX * kBZ) + tid;
+    edge_thread<T, SI>(sp, g, it_off);
+    stress_sample_thread<T>(sp, g - (SI ? sp.NX : 0), it_off);
   }
 }
 
