@@ -41,6 +41,9 @@ struct fdp_ctx {
   // kernels over the whole grid): core rectangles of each phase and the
   // units holding any cell outside them
   bool use_core = false;
+  // frame and core of a phase in one launch (else on two streams), per
+  // phase: stress, velocity
+  bool fused[2] = {false, false};
   int cs[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0};  // x0, x1, z0, z1
   DevArr frame_s, frame_v;
   int nframe_s = 0, nframe_v = 0;

@@ -229,6 +229,19 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
   const dim3 tblk(fdp::kTX, 4, 1);
   if (kind == 0 && c->use_tma) fdp::k_stress_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_vel, it_off);
   else if (kind == 1 && c->use_tma) fdp::k_velocity_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_str, it_off);
+  else if ((kind == 0 || kind == 1) && c->use_core && c->fused[kind]) {
+    const int* r = kind == 0 ? c->cs : c->cv;
+    fdp::FusedGrid g{};
+    g.units = (const int4*)(kind == 0 ? c->frame_s.p : c->frame_v.p);
+    g.nframe = kind == 0 ? c->nframe_s : c->nframe_v;
+    const dim3 cg = r[1] > r[0] ? core_grid(r) : dim3(0, 0, 1);
+    g.gx = (int)cg.x;
+    g.ncore = (int)(cg.x * cg.y);
+    g.per = g.nframe > 0 ? (g.ncore + g.nframe - 1) / g.nframe : 0;
+    const int total = g.nframe > 0 ? g.nframe * (g.per + 1) : g.ncore;
+    if (kind == 0) fdp::k_stress_fused<T, SI, MODE><<<total, blk, 0, c->stream>>>(p, g, it_off);
+    else fdp::k_velocity_fused<T, SI, MODE><<<total, blk, 0, c->stream>>>(p, g);
+  }
   else if ((kind == 0 || kind == 1) && c->use_core) {
     const int* r = kind == 0 ? c->cs : c->cv;
     const bool core = r[1] > r[0];
@@ -343,7 +356,7 @@ template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_o
 }
 
 int level_launches(const fdp_ctx* c) {
-  const int cores = c->use_core ? (c->cs[1] > c->cs[0]) + (c->cv[1] > c->cv[0]) : 0;
+  const int cores = c->use_core ? (!c->fused[0] && c->cs[1] > c->cs[0]) + (!c->fused[1] && c->cv[1] > c->cv[0]) : 0;
   return 2 + cores + (edge_threads(c) > 0 ? 1 : 0) + (c->edge && c->edge_attached ? 3 : 0);
 }
 
@@ -621,6 +634,13 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   const char* variant = std::getenv("FDP_KERNEL_VARIANT");
   c->use_tma = variant && std::strcmp(variant, "tma") == 0;
   c->use_core = !(variant && (std::strcmp(variant, "tma") == 0 || std::strcmp(variant, "global") == 0));
+  // frame and core on two streams; "fused" puts each phase's frame units
+  // among its core blocks in one launch instead (measured on the layered
+  // 2048^2 workload: a level takes 0.1085 ms split, 0.121 ms fused, 0.1105
+  // ms with only the velocity phase fused)
+  const bool fused = variant && std::strcmp(variant, "fused") == 0;
+  c->fused[0] = c->use_core && fused;
+  c->fused[1] = c->use_core && fused;
   if (c->use_core) {
     if ((rc = plan_core(c)) != FDP_OK) return bail(rc);
     e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
@@ -891,7 +911,8 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
     const int nedge = edge_threads(c);
     cudaEvent_t ev[4];
     for (auto& e : ev) CK(c, cudaEventCreate(&e));
-    const bool core[2] = {c->use_core && c->cs[1] > c->cs[0], c->use_core && c->cv[1] > c->cv[0]};
+    const bool core[2] = {c->use_core && !c->fused[0] && c->cs[1] > c->cs[0],
+                          c->use_core && !c->fused[1] && c->cv[1] > c->cv[0]};
     for (int k = 0; k < 2; ++k)
       if (core[k]) for (auto& e : c->core_ev[k]) CK(c, cudaEventCreate(&e));
     fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);

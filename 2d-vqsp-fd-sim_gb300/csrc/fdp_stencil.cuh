@@ -1084,6 +1084,50 @@ __global__ void FDP_CORE_BOUNDS(T) k_velocity_core(const __grid_constant__ Param
   velocity_core_block<T, MODE>(p, (int)blockIdx.x, (int)blockIdx.y);
 }
 
+// Frame and core of a phase in one launch.  Blocks are dispatched in index
+// order, so the frame units are spread through the grid -- one after every
+// `per` core blocks -- and their latency-bound cells ride along with the
+// bandwidth-bound core instead of queueing before or after it.  Block b:
+// k = b / (per + 1); the first block of group k < nframe is frame unit k,
+// the others are core blocks k*per .. k*per + per - 1 (those past the last
+// core block do nothing).
+struct FusedGrid {
+  const int4* units;  // frame units of the phase
+  int nframe;
+  int per;            // core blocks per frame unit
+  int ncore;          // core blocks
+  int gx;             // core blocks along x
+};
+
+__device__ __forceinline__ int fused_role(const FusedGrid& g, int b, int& idx) {
+  if (g.nframe == 0) { idx = b; return 1; }
+  const int k = b / (g.per + 1), r = b % (g.per + 1);
+  if (k < g.nframe && r == 0) { idx = k; return 0; }
+  idx = k < g.nframe ? k * g.per + r - 1 : g.nframe * g.per + (b - g.nframe * (g.per + 1));
+  return idx < g.ncore ? 1 : -1;
+}
+
+template <class T, bool SI, int MODE>
+__global__ void FDP_CORE_BOUNDS(T) k_stress_fused(const __grid_constant__ Params<T> p, const FusedGrid g,
+                                                  int it_off) {
+  int idx;
+  const int role = fused_role(g, (int)blockIdx.x, idx);
+  if (role == 0) {
+    const int4 u = g.units[idx];
+    stress_unit<T, SI, MODE>(p, u.x, u.y, u.z, it_off);
+  } else if (role == 1) {
+    stress_core_block<T, MODE>(p, idx % g.gx, idx / g.gx);
+  }
+}
+
+template <class T, bool SI, int MODE>
+__global__ void FDP_CORE_BOUNDS(T) k_velocity_fused(const __grid_constant__ Params<T> p, const FusedGrid g) {
+  int idx;
+  const int role = fused_role(g, (int)blockIdx.x, idx);
+  if (role == 0) velocity_frame_unit<T, SI, MODE>(p, g.units[idx]);
+  else if (role == 1) velocity_core_block<T, MODE>(p, idx % g.gx, idx / g.gx);
+}
+
 // ---------------------------------------------------------------------------
 // Stress-imaging row 1 (inh_v_qx_int_1_si.F90:26-31, inh_w_qz_int_1_si.F90:30-44),
 // from the final rows 2 and 3.  Returns the row-1 value of u (c=0), w (1),

@@ -267,10 +267,11 @@ def run_gpu(args) -> None:
     phases = ("stress", "velocity", "edge")
     shares = {k: prof[k][0] / sum(prof[q][0] for q in phases) for k in phases}
     peak, peak_kind = measured_peak_gbs()
-    # the dominant kernel: the longer core kernel (the whole phase when the
-    # engine runs one kernel per phase)
-    cand = [k for k in ("stress_core", "velocity_core") if prof[k][1] > 0] or ["stress", "velocity"]
-    kern = max(cand, key=lambda k: prof[k][0])
+    # the dominant kernel: that of the longer phase -- its core kernel when
+    # the phase runs as frame and core kernels on two streams, else the
+    # phase's one kernel
+    phase = max(("stress", "velocity"), key=lambda k: prof[k][0])
+    kern = f"{phase}_core" if prof[f"{phase}_core"][1] > 0 else phase
     avg_ms = prof[kern][0] / prof[kern][1]
     achieved = alg[kern] / (avg_ms / 1e3) / 1e9
     phase_gbs = {k: alg[k] / (prof[k][0] / prof[k][1] / 1e3) / 1e9 for k in ("stress", "velocity")}
