@@ -7,7 +7,7 @@
 #include <string>
 
 #include "fdp.h"
-#include "fdp_stencil.cuh"
+#include "fdp_core_tma.cuh"
 
 struct DevArr {
   void* p = nullptr;
@@ -44,6 +44,12 @@ struct fdp_ctx {
   // frame and core of a phase in one launch (else on two streams), per
   // phase: stress, velocity
   bool fused[2] = {false, false};
+  // TMA-staged persistent core kernels (FDP_KERNEL_VARIANT=coretma; FP32
+  // contexts with a Biot-plane medium): the maps of each phase's 13 copies
+  // and the CTAs a launch runs (one per SM)
+  bool core_tma_req = false, core_tma = false;
+  fdp::CoreMaps cmaps[2]{};
+  int core_ctas = 0;
   int cs[4] = {0, 0, 0, 0}, cv[4] = {0, 0, 0, 0};  // x0, x1, z0, z1
   DevArr frame_s, frame_v;
   int nframe_s = 0, nframe_v = 0;

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <type_traits>
 #include <cmath>
@@ -22,7 +23,7 @@
 
 #include "fdp.h"
 #include "fdp_ctx.h"
-#include "fdp_stencil.cuh"
+#include "fdp_core_tma.cuh"
 
 using fdp::Params;
 using fdp::kPadX;
@@ -118,10 +119,10 @@ int copy2d_sync(fdp_ctx* c, void* dst, size_t dpitch, const void* src, size_t sp
 
 size_t count_of(const int b[4]) { return (size_t)(b[1] - b[0] + 1) * (size_t)(b[3] - b[2] + 1); }
 
-// TMA descriptor of one padded field (whole allocation, kSX x kSZ boxes).
-// cuTensorMapEncodeTiled is reached through the runtime's driver entry
-// point, so the library does not link libcuda itself.
-int make_field_map(fdp_ctx* c, CUtensorMap* map, void* base) {
+// TMA descriptor of one padded field (whole allocation, boxes of bw x bh
+// elements).  cuTensorMapEncodeTiled is reached through the runtime's
+// driver entry point, so the library does not link libcuda itself.
+int make_field_map(fdp_ctx* c, CUtensorMap* map, void* base, int bw = fdp::kSX, int bh = fdp::kSZ) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -133,12 +134,45 @@ int make_field_map(fdp_ctx* c, CUtensorMap* map, void* base) {
   }
   const cuuint64_t dims[2] = {(cuuint64_t)c->pitch, (cuuint64_t)c->rows_alloc};
   const cuuint64_t strides[1] = {(cuuint64_t)c->pitch * (cuuint64_t)c->prec};
-  const cuuint32_t box[2] = {(cuuint32_t)fdp::kSX, (cuuint32_t)fdp::kSZ};
+  const cuuint32_t box[2] = {(cuuint32_t)bw, (cuuint32_t)bh};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = encode(map, c->prec == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
                             base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(c, FDP_ERR_CUDA, "cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+  return FDP_OK;
+}
+
+// Maps of the TMA-staged core kernels (fdp_core_tma.cuh), built once the
+// medium is known: FP32 fields and the 10 Biot planes.  Phase 0 reads u, w,
+// qx, qz and updates the stresses; phase 1 reads the stresses and updates
+// qx, u, qz, w.
+int make_core_maps(fdp_ctx* c) {
+  c->core_tma = false;
+  if (!c->core_tma_req || c->prec != 4 || c->medium_mode != fdp::M_BIOT) return FDP_OK;
+  static const int in[2][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}};
+  static const int upd[2][4] = {{4, 5, 6, 7}, {2, 0, 3, 1}};
+  const size_t pstride = (size_t)c->rows_alloc * c->pitch;
+  int rc;
+  for (int ph = 0; ph < 2; ++ph) {
+    fdp::CoreMaps& m = c->cmaps[ph];
+    for (int k = 0; k < 4; ++k) {
+      if ((rc = make_field_map(c, &m.m[k], c->fields[in[ph][k]].p, fdp::kCHW, fdp::core_box_rows(ph, k))) != FDP_OK)
+        return rc;
+      if ((rc = make_field_map(c, &m.m[4 + k], c->fields[upd[ph][k]].p, fdp::kCTW, fdp::kCTH)) != FDP_OK) return rc;
+    }
+    for (int k = 0; k < 5; ++k)
+      if ((rc = make_field_map(c, &m.m[8 + k], (float*)c->planes.p + (size_t)(5 * ph + k) * pstride, fdp::kCTW,
+                               fdp::kCTH)) != FDP_OK)
+        return rc;
+  }
+  int dev = 0, nsm = 0;
+  CK(c, cudaGetDevice(&dev));
+  CK(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  CK(c, cudaFuncSetAttribute(fdp::k_core_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fdp::kCoreTmaSmem));
+  CK(c, cudaFuncSetAttribute(fdp::k_core_tma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fdp::kCoreTmaSmem));
+  c->core_ctas = nsm;
+  c->core_tma = true;
   return FDP_OK;
 }
 
@@ -224,6 +258,20 @@ dim3 core_grid(const int r[4]) {
   return dim3((threads_x + fdp::kBX - 1) / fdp::kBX, (r[3] - r[2] + fdp::kBZ - 1) / fdp::kBZ, 1);
 }
 
+// The TMA-staged core kernel of phase `kind`, where the context uses it
+// (FP32, Biot planes); false leaves the phase to the per-thread-load core.
+template <class T, int MODE> bool launch_core_tma(fdp_ctx* c, const Params<T>& p, int kind) {
+  if constexpr (std::is_same<T, float>::value && MODE == fdp::M_BIOT) {
+    if (!c->core_tma) return false;
+    const dim3 blk(fdp::kBX, fdp::kBZ, 1);
+    const int g = std::min(fdp::core_tiles(p, kind).n, c->core_ctas);
+    if (kind == 0) fdp::k_core_tma<0><<<g, blk, fdp::kCoreTmaSmem, c->stream>>>(p, c->cmaps[0]);
+    else fdp::k_core_tma<1><<<g, blk, fdp::kCoreTmaSmem, c->stream>>>(p, c->cmaps[1]);
+    return true;
+  }
+  return false;
+}
+
 template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
   const dim3 blk(fdp::kBX, fdp::kBZ, 1);
   const dim3 tblk(fdp::kTX, 4, 1);
@@ -254,7 +302,8 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
     else fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v, blk, 0, fs>>>(p, (const int4*)c->frame_v.p);
     if (core) {
       if (c->core_ev[kind][0]) cudaEventRecord(c->core_ev[kind][0], c->stream);
-      if (kind == 0) fdp::k_stress_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
+      if (launch_core_tma<T, MODE>(c, p, kind)) {}
+      else if (kind == 0) fdp::k_stress_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
       else fdp::k_velocity_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
       if (c->core_ev[kind][1]) cudaEventRecord(c->core_ev[kind][1], c->stream);
       cudaEventRecord(c->join, c->side);
@@ -459,6 +508,17 @@ template <class T> uint64_t column_hash(const T* a, size_t n, bool negate) {
   return h;
 }
 
+template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate);
+
+// same_bits over many elements, split across the host's cores.
+template <class T> bool same_bits_par(const T* a, const T* b, size_t n, bool negate) {
+  std::atomic<bool> same{true};
+  parallel_for(n, [&](size_t lo, size_t hi) {
+    if (!same_bits(a + lo, b + lo, hi - lo, negate)) same = false;
+  });
+  return same;
+}
+
 template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate) {
   using U = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
   const U sign = (U)1 << (sizeof(T) * 8 - 1);
@@ -525,8 +585,8 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
     for (size_t q = 0; q < plane_col.size() && c->src[k] < 0; ++q) {
       const int o = plane_col[q];
       const T* other = &t[(size_t)o * ld + 1];
-      if (hpos[o] == hpos[k] && same_bits(other, col, (size_t)jmnum, false)) { c->src[k] = (int)q; c->neg[k] = 0; }
-      else if (hpos[o] == hneg[k] && same_bits(other, col, (size_t)jmnum, true)) { c->src[k] = (int)q; c->neg[k] = 1; }
+      if (hpos[o] == hpos[k] && same_bits_par(other, col, (size_t)jmnum, false)) { c->src[k] = (int)q; c->neg[k] = 0; }
+      else if (hpos[o] == hneg[k] && same_bits_par(other, col, (size_t)jmnum, true)) { c->src[k] = (int)q; c->neg[k] = 1; }
     }
     if (c->src[k] < 0) { c->src[k] = (int)plane_col.size(); plane_col.push_back(k); }
   }
@@ -641,6 +701,7 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   const bool fused = variant && std::strcmp(variant, "fused") == 0;
   c->fused[0] = c->use_core && fused;
   c->fused[1] = c->use_core && fused;
+  c->core_tma_req = c->use_core && variant && std::strcmp(variant, "coretma") == 0;
   if (c->use_core) {
     if ((rc = plan_core(c)) != FDP_OK) return bail(rc);
     e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
@@ -665,14 +726,26 @@ int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_
   if (!c || !jm || !table24) return fail(c, FDP_ERR_ARG, "null argument");
   if (nx != c->NX || nz != c->NZ) return fail(c, FDP_ERR_ARG, "JM is %dx%d, grid is %dx%d", nx, nz, c->NX, c->NZ);
   if (jmnum < 1) return fail(c, FDP_ERR_ARG, "JMNUM must be >= 1");
-  for (size_t k = 0; k < (size_t)nx * nz; ++k)
-    if (jm[k] < 1 || jm[k] > jmnum) return fail(c, FDP_ERR_ARG, "JM value %d at %zu outside 1..%d", jm[k], k, jmnum);
+  std::atomic<size_t> bad{(size_t)-1};
+  parallel_for((size_t)nx * nz, [&](size_t lo, size_t hi) {
+    for (size_t k = lo; k < hi; ++k)
+      if (jm[k] < 1 || jm[k] > jmnum) {
+        size_t cur = bad.load();
+        while (k < cur && !bad.compare_exchange_weak(cur, k)) {}
+        break;
+      }
+  });
+  if (bad.load() != (size_t)-1) {
+    const size_t k = bad.load();
+    return fail(c, FDP_ERR_ARG, "JM value %d at %zu outside 1..%d", jm[k], k, jmnum);
+  }
   int rc;
   CK(c, cudaStreamSynchronize(c->stream));
   rc = (c->prec == 8) ? build_medium<double>(c, jm, jmnum, (const double*)table24)
                       : build_medium<float>(c, jm, jmnum, (const float*)table24);
   if (rc != FDP_OK) return rc;
   CK(c, cudaStreamSynchronize(c->stream));
+  if ((rc = make_core_maps(c)) != FDP_OK) return rc;
   c->jmnum = jmnum;
   c->have_medium = true;
   c->params_dirty = true;

@@ -893,18 +893,17 @@ __device__ __forceinline__ void velocity_bottom_unit(const Params<T>& p, int I0,
 }
 
 // A velocity frame unit: (first column, end column, first row, 1) one row
-// per thread up to row PMLZH-3; (first column, end column, 0, 2) the bottom
-// three rows; (first column, end column, unit row, 0) the four-row layout.
+// per thread up to row PMLZH-3, or (first column, end column, 0, 2) the
+// bottom three rows.
 template <class T, bool SI, int MODE>
 __device__ __forceinline__ void velocity_frame_unit(const Params<T>& p, const int4 u) {
-  if (u.w == 1) velocity_row_unit<T, SI, MODE>(p, u.x, u.y, u.z);
-  else if (u.w == 2) velocity_bottom_unit<T, SI, MODE>(p, u.x, u.y);
-  else velocity_unit<T, SI, MODE>(p, u.x, u.y, u.z);
+  if (u.w == 2) velocity_bottom_unit<T, SI, MODE>(p, u.x, u.y);
+  else velocity_row_unit<T, SI, MODE>(p, u.x, u.y, u.z);
 }
 
 template <class T, bool SI, int MODE>
-__global__ void FDP_VELOCITY_BOUNDS(T) k_velocity_frame(const __grid_constant__ Params<T> p,
-                                                        const int4* __restrict__ units) {
+__global__ void __launch_bounds__(kBX * kBZ, 4) k_velocity_frame(const __grid_constant__ Params<T> p,
+                                                              const int4* __restrict__ units) {
   velocity_frame_unit<T, SI, MODE>(p, units[blockIdx.x]);
 }
 

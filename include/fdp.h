@@ -97,7 +97,13 @@ enum fdp_field_id {
 
 /* Creates a context and allocates the device state, zeroed as TL_ALLOC,
  * PPML and ALLOC_NR do (tl_alloc.F90:253-265, ppml.F90:115-153,
- * alloc_nr.F90:42-54).  Replaces the allocations of TL_ALLOC/PPML/ALLOC_NR. */
+ * alloc_nr.F90:42-54).  Replaces the allocations of TL_ALLOC/PPML/ALLOC_NR.
+ * The environment variable FDP_KERNEL_VARIANT, read here, selects the
+ * kernels, all bit-identical: unset, the interior ("core") of each phase
+ * runs vectorised beside a frame kernel for the PML, free-surface, source
+ * and bottom cells on a second stream; "fused" runs frame and core of a
+ * phase in one launch; "global" runs one unit kernel per phase over the
+ * whole grid; "tma" the TMA-staged variant of the latter. */
 int fdp_create(const fdp_grid* grid, fdp_ctx** out);
 
 /* Medium: JM(PMLL:PMLXH, 0:PMLZH) (nx = MX+2*TPML, nz = PMLZH+1) after

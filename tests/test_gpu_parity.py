@@ -14,12 +14,13 @@ from helpers import compare_state, randomize_state, small_job
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(autouse=True, params=["core", "fused", "global", "tma"])
+@pytest.fixture(autouse=True, params=["core", "fused", "global", "tma", "coretma"])
 def kernel_variant(request, monkeypatch):
     """Runs every test with each kernel variant fdp_create can select through
     FDP_KERNEL_VARIANT: the frame/core split on two streams (the default)
-    or in one launch per phase, the unit kernels over the whole grid, and
-    the TMA-staged kernels."""
+    or in one launch per phase, the unit kernels over the whole grid, the
+    TMA-staged kernels, and the split with TMA-staged persistent core
+    kernels (FP32 Biot media; the others keep the per-thread-load core)."""
     monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
     return request.param
 
