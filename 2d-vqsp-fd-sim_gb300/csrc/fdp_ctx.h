@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <string>
 
 #include "fdp.h"
@@ -12,6 +13,16 @@
 struct DevArr {
   void* p = nullptr;
   size_t bytes = 0;
+};
+
+// Device arrays of a medium that several contexts use (fdp_share_medium):
+// freed when the last context holding the share lets go of it.
+struct MediumShare {
+  DevArr jm, coef, planes, aux;
+  ~MediumShare() {
+    for (DevArr* a : {&jm, &coef, &planes, &aux})
+      if (a->p) cudaFree(a->p);
+  }
 };
 
 struct fdp_edge;
@@ -64,9 +75,16 @@ struct fdp_ctx {
   int mt2 = 0;
   int mr = 0, rec_flags = 0;
   bool have_medium = false, have_pml = false, have_nr = false, have_source = false;
+  // set while jm, coef, planes and aux belong to a share with other
+  // contexts (the share frees them, not this context)
+  std::shared_ptr<MediumShare> medium_share;
   // graph of kChunk levels
   cudaGraphExec_t graph = nullptr;
   bool params_dirty = true;
+  // bumped by every change of the device parameters (set_*, a shared
+  // medium, an attached edge); a batch refuses to run a shot whose count
+  // moved after fdp_batch_create
+  unsigned long long gen = 0;
   long long launches = 0;
   int last_it = 0;  // highest level run so far
   // learned absorbing edge: state (history, tiles) once the context has
@@ -74,6 +92,13 @@ struct fdp_ctx {
   EdgeState* edge = nullptr;
   bool edge_attached = false;
 };
+
+// Marks the context's device parameters changed: its captured graph is
+// rebuilt before the next run, and batches made earlier refuse to run it.
+inline void params_changed(fdp_ctx* c) {
+  c->params_dirty = true;
+  ++c->gen;
+}
 
 namespace fdp {
 // Launches the attached learned edge's kernels for level *it_base + it_off
@@ -83,5 +108,3 @@ int edge_launch(fdp_ctx* c, int it_off);
 // Frees the context's learned-edge state.
 void edge_release(fdp_ctx* c);
 }  // namespace fdp
-
-

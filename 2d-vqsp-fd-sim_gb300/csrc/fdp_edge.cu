@@ -821,7 +821,7 @@ int fdp_edge_attach(fdp_ctx* trunc, fdp_edge* e) {
     s->net = e;
     trunc->edge_attached = true;
   }
-  trunc->params_dirty = true;  // the captured graph gains or loses the edge kernels
+  params_changed(trunc);  // the captured graph gains or loses the edge kernels
   return FDP_OK;
 }
 

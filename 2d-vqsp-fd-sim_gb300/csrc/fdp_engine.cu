@@ -365,10 +365,12 @@ int plan_core(fdp_ctx* c) {
       for (const auto& sg : segs)
         for (int I0 = sg.first; I0 < sg.second; I0 += fdp::kBX) {
           const int I1 = std::min(I0 + fdp::kBX, sg.second);
+          // a unit is listed when some cell of it lies outside the core
+          // rectangle (or on the source row, for the stress phase)
+          const int lo = std::max(la, 0), hi = std::min(lb, c->PMLZH);
           bool frame = false;
-          for (int L = std::max(la, 0); L <= std::min(lb, c->PMLZH) && !frame; ++L)
-            for (int I = I0; I < I1; ++I)
-              if (!in(r, I, L) || (ph == 0 && L == c->g.lin_z)) { frame = true; break; }
+          if (lo <= hi)
+            frame = !(in(r, I0, lo) && in(r, I1 - 1, hi)) || (ph == 0 && c->g.lin_z >= lo && c->g.lin_z <= hi);
           if (frame) { out.push_back(I0); out.push_back(I1); out.push_back(tag); out.push_back(w); }
         }
     }
@@ -452,23 +454,38 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
   return FDP_OK;
 }
 
-// Runs fn(begin, end) over [0, n) split across the host's cores.
-template <class F> void parallel_for(size_t n, F fn) {
+// Runs fn(begin, end) over [0, n) split across the host's cores, at least
+// `grain` items per thread.
+template <class F> void parallel_for(size_t n, F fn, size_t grain = 65536) {
   const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const size_t nt = std::min(hw, std::max<size_t>(1, n / 65536));
+  const size_t nt = std::min(hw, std::max<size_t>(1, n / grain));
   if (nt <= 1) { fn((size_t)0, n); return; }
   std::vector<std::thread> th;
   for (size_t t = 0; t < nt; ++t) th.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
   for (auto& x : th) x.join();
 }
 
+// A host array left uninitialised at allocation: the set-up writes every
+// element it uploads from its worker threads, so a single-threaded zero
+// fill of hundreds of MB (and its page faults) is not paid up front.
+template <class T> struct HostBuf {
+  std::unique_ptr<T[]> p;
+  size_t n = 0;
+  void reset(size_t m) { p.reset(new T[m]); n = m; }
+  T& operator[](size_t i) { return p[i]; }
+  const T& operator[](size_t i) const { return p[i]; }
+  T* data() { return p.get(); }
+  size_t size() const { return n; }
+};
+
 template <class T>
-void derive_table(const int32_t jmnum, const T* tab, std::vector<T>& out) {
+void derive_table(const int32_t jmnum, const T* tab, HostBuf<T>& out) {
   // table24 columns (.MO record order, read_model_par.F90:147-155)
   enum { MU, SXX1, SXX2, SXX3, SZZ1, SZZ2, SZZ3, P1, P2, P3, R1U, R1W, R2U, R2W, R3U, R3W,
          R1QX, R1QZ, R2QX, R2QZ, R3QX, R3QZ, AUXW, AUXQZ };
   const size_t ld = (size_t)jmnum + 1;
-  out.assign(ld * fdp::C_NCOEF, T(0));
+  out.reset(ld * fdp::C_NCOEF);
+  for (int k = 0; k < fdp::C_NCOEF; ++k) out[(size_t)k * ld] = T(0);  // index 0: no material
   parallel_for((size_t)jmnum, [&](size_t jb, size_t je) {
   for (int j = (int)jb + 1; j <= (int)je; ++j) {
     const T* r = tab + (size_t)(j - 1) * 24;
@@ -495,17 +512,34 @@ void derive_table(const int32_t jmnum, const T* tab, std::vector<T>& out) {
 // a larger table (one material per cell) is expanded into per-cell planes.
 constexpr int kMaxTableMaterials = 4096;
 
-// 64-bit FNV-1a hash of a column's bit patterns (negated when asked).
-template <class T> uint64_t column_hash(const T* a, size_t n, bool negate) {
+// Hashes of a column's bit patterns and of its negation's: four
+// interleaved 64-bit FNV-1a lanes each (independent multiply chains),
+// folded together at the end.
+template <class T> void column_hash(const T* a, size_t n, uint64_t& hpos, uint64_t& hneg) {
   using U = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
   const U sign = (U)1 << (sizeof(T) * 8 - 1);
-  uint64_t h = 1469598103934665603ULL;
-  for (size_t i = 0; i < n; ++i) {
+  const uint64_t prime = 1099511628211ULL;
+  uint64_t p[4], q[4];
+  for (int l = 0; l < 4; ++l) p[l] = q[l] = 1469598103934665603ULL + (uint64_t)l;
+  size_t i = 0;
+  for (; i + 4 <= n; i += 4)
+    for (int l = 0; l < 4; ++l) {
+      U x;
+      std::memcpy(&x, &a[i + l], sizeof(T));
+      p[l] = (p[l] ^ (uint64_t)x) * prime;
+      q[l] = (q[l] ^ (uint64_t)(U)(x ^ sign)) * prime;
+    }
+  for (; i < n; ++i) {
     U x;
     std::memcpy(&x, &a[i], sizeof(T));
-    h = (h ^ (uint64_t)(negate ? (x ^ sign) : x)) * 1099511628211ULL;
+    p[0] = (p[0] ^ (uint64_t)x) * prime;
+    q[0] = (q[0] ^ (uint64_t)(U)(x ^ sign)) * prime;
   }
-  return h;
+  hpos = hneg = 0;
+  for (int l = 0; l < 4; ++l) {
+    hpos = (hpos ^ p[l]) * prime;
+    hneg = (hneg ^ q[l]) * prime;
+  }
 }
 
 template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate);
@@ -537,7 +571,7 @@ template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate)
 // or distinct; distinct columns become per-cell planes when the material
 // table is large, else the kernels index the table through JM.
 template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum, const T* table24) {
-  std::vector<T> t;
+  HostBuf<T> t;
   derive_table<T>(jmnum, table24, t);
   const size_t ld = (size_t)jmnum + 1;
   int rc;
@@ -561,8 +595,8 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
       bool cst = true;
       for (int j = 1; j < jmnum && cst; ++j) cst = same_bits(&col[0], &col[j], 1, false);
       constant[k] = cst;
-      hpos[k] = cst ? 0 : column_hash(col, (size_t)jmnum, false);
-      hneg[k] = cst ? 0 : column_hash(col, (size_t)jmnum, true);
+      hpos[k] = hneg[k] = 0;
+      if (!cst) column_hash(col, (size_t)jmnum, hpos[k], hneg[k]);
     };
     if (jmnum < 65536) {
       for (int k = 0; k < fdp::C_NCOEF; ++k) classify(k);
@@ -572,23 +606,49 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
       for (auto& x : th) x.join();
     }
   }
+  // plane assignment: first on the hashes alone, then every column placed
+  // on an earlier plane is confirmed bit for bit in one parallel pass; a
+  // failed confirmation (a hash collision) redoes the assignment with a
+  // full comparison before each match
   std::vector<int> plane_col;
-  for (int k = 0; k < fdp::C_NCOEF; ++k) {
-    c->src[k] = -1; c->neg[k] = 0; c->cval_d[k] = 0; c->cval_f[k] = 0;
-    if (k == fdp::C_AUXW || k == fdp::C_AUXQZ) continue;
-    const T* col = &t[(size_t)k * ld + 1];
-    if (constant[k]) {
-      c->cval_d[k] = (double)col[0];
-      c->cval_f[k] = (float)col[0];
-      continue;
+  auto assign = [&](bool exact) {
+    plane_col.clear();
+    for (int k = 0; k < fdp::C_NCOEF; ++k) {
+      c->src[k] = -1; c->neg[k] = 0; c->cval_d[k] = 0; c->cval_f[k] = 0;
+      if (k == fdp::C_AUXW || k == fdp::C_AUXQZ) continue;
+      const T* col = &t[(size_t)k * ld + 1];
+      if (constant[k]) {
+        c->cval_d[k] = (double)col[0];
+        c->cval_f[k] = (float)col[0];
+        continue;
+      }
+      for (size_t q = 0; q < plane_col.size() && c->src[k] < 0; ++q) {
+        const int o = plane_col[q];
+        const T* other = &t[(size_t)o * ld + 1];
+        if (hpos[o] == hpos[k] && (!exact || same_bits_par(other, col, (size_t)jmnum, false))) {
+          c->src[k] = (int)q; c->neg[k] = 0;
+        } else if (hpos[o] == hneg[k] && (!exact || same_bits_par(other, col, (size_t)jmnum, true))) {
+          c->src[k] = (int)q; c->neg[k] = 1;
+        }
+      }
+      if (c->src[k] < 0) { c->src[k] = (int)plane_col.size(); plane_col.push_back(k); }
     }
-    for (size_t q = 0; q < plane_col.size() && c->src[k] < 0; ++q) {
-      const int o = plane_col[q];
-      const T* other = &t[(size_t)o * ld + 1];
-      if (hpos[o] == hpos[k] && same_bits_par(other, col, (size_t)jmnum, false)) { c->src[k] = (int)q; c->neg[k] = 0; }
-      else if (hpos[o] == hneg[k] && same_bits_par(other, col, (size_t)jmnum, true)) { c->src[k] = (int)q; c->neg[k] = 1; }
-    }
-    if (c->src[k] < 0) { c->src[k] = (int)plane_col.size(); plane_col.push_back(k); }
+  };
+  assign(false);
+  {
+    std::vector<int> alias;  // columns placed on another column's plane
+    for (int k = 0; k < fdp::C_NCOEF; ++k)
+      if (c->src[k] >= 0 && plane_col[c->src[k]] != k) alias.push_back(k);
+    std::atomic<bool> same{true};
+    if (!alias.empty())
+      parallel_for((size_t)jmnum, [&](size_t lo, size_t hi) {
+        for (int k : alias) {
+          const T* col = &t[(size_t)k * ld + 1 + lo];
+          const T* other = &t[(size_t)plane_col[c->src[k]] * ld + 1 + lo];
+          if (!same_bits(other, col, hi - lo, c->neg[k] != 0)) { same = false; return; }
+        }
+      });
+    if (!same) assign(true);
   }
   c->nplanes = (int)plane_col.size();
   const bool table_mode = c->nplanes > 0 && jmnum <= kMaxTableMaterials;
@@ -615,7 +675,8 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
     if ((rc = dev_alloc(c, c->planes, std::max<size_t>(1, (size_t)c->nplanes * cells) * sizeof(T))) != FDP_OK) return rc;
     // every plane expanded over the padded layout (padding holds material
     // 1), rows in parallel, then one copy
-    std::vector<T> pl((size_t)c->nplanes * cells);
+    HostBuf<T> pl;
+    pl.reset((size_t)c->nplanes * cells);
     parallel_for((size_t)c->nplanes * c->rows_alloc, [&](size_t b, size_t e) {
       for (size_t r = b; r < e; ++r) {
         const int q = (int)(r / c->rows_alloc), row = (int)(r % c->rows_alloc);
@@ -628,7 +689,7 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
         for (int x = 0; x < c->NX; ++x) dst[kPadX + x] = col[src[x]];
         std::fill(dst + kPadX + c->NX, dst + c->pitch, col[1]);
       }
-    });
+    }, 16);
     if ((rc = copy_sync(c, c->planes.p, pl.data(), pl.size() * sizeof(T), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
   }
   return FDP_OK;
@@ -722,6 +783,14 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   return FDP_OK;
 }
 
+// Lets go of a shared medium: the arrays stay with the share (freed by its
+// last holder) and this context's handles are cleared.
+void unshare_medium(fdp_ctx* c) {
+  if (!c->medium_share) return;
+  c->jm = DevArr{}; c->coef = DevArr{}; c->planes = DevArr{}; c->aux = DevArr{};
+  c->medium_share.reset();
+}
+
 int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_t jmnum, const void* table24) {
   if (!c || !jm || !table24) return fail(c, FDP_ERR_ARG, "null argument");
   if (nx != c->NX || nz != c->NZ) return fail(c, FDP_ERR_ARG, "JM is %dx%d, grid is %dx%d", nx, nz, c->NX, c->NZ);
@@ -741,6 +810,7 @@ int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_
   }
   int rc;
   CK(c, cudaStreamSynchronize(c->stream));
+  unshare_medium(c);
   rc = (c->prec == 8) ? build_medium<double>(c, jm, jmnum, (const double*)table24)
                       : build_medium<float>(c, jm, jmnum, (const float*)table24);
   if (rc != FDP_OK) return rc;
@@ -748,8 +818,40 @@ int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_
   if ((rc = make_core_maps(c)) != FDP_OK) return rc;
   c->jmnum = jmnum;
   c->have_medium = true;
-  c->params_dirty = true;
+  params_changed(c);
   return FDP_OK;
+}
+
+int fdp_share_medium(fdp_ctx* dst, fdp_ctx* src) {
+  if (!dst || !src) return fail(dst, FDP_ERR_ARG, "null argument");
+  if (dst == src) return FDP_OK;
+  if (!src->have_medium) return fail(dst, FDP_ERR_STATE, "the source context has no medium yet");
+  if (dst->prec != src->prec || dst->NX != src->NX || dst->NZ != src->NZ || dst->g.device != src->g.device)
+    return fail(dst, FDP_ERR_ARG, "a medium is shared only between contexts of the same grid, precision and device");
+  CK(dst, cudaStreamSynchronize(dst->stream));  // work that may still read dst's own medium
+  CK(dst, cudaStreamSynchronize(src->stream));
+  if (!src->medium_share) {
+    // the source's arrays move into a share; its handles stay valid
+    src->medium_share = std::make_shared<MediumShare>();
+    src->medium_share->jm = src->jm; src->medium_share->coef = src->coef;
+    src->medium_share->planes = src->planes; src->medium_share->aux = src->aux;
+  }
+  unshare_medium(dst);
+  int rc;
+  for (DevArr* a : {&dst->jm, &dst->coef, &dst->planes, &dst->aux})
+    if ((rc = dev_alloc(dst, *a, 0)) != FDP_OK) return rc;
+  dst->jm = src->jm; dst->coef = src->coef; dst->planes = src->planes; dst->aux = src->aux;
+  dst->medium_share = src->medium_share;
+  dst->medium_mode = src->medium_mode;
+  dst->nplanes = src->nplanes;
+  for (int k = 0; k < fdp::C_NCOEF; ++k) {
+    dst->src[k] = src->src[k]; dst->neg[k] = src->neg[k];
+    dst->cval_d[k] = src->cval_d[k]; dst->cval_f[k] = src->cval_f[k];
+  }
+  dst->jmnum = src->jmnum;
+  dst->have_medium = true;
+  params_changed(dst);
+  return make_core_maps(dst);
 }
 
 int fdp_set_pml(fdp_ctx* c, const void* const* prof) {
@@ -795,7 +897,7 @@ int fdp_set_source(fdp_ctx* c, const void* sourtf, int32_t mt2) {
   if ((rc = copy_sync(c, c->stf.p, sourtf, (size_t)2 * mt2 * c->prec, cudaMemcpyHostToDevice)) != FDP_OK) return rc;
   c->mt2 = mt2;
   c->have_source = true;
-  c->params_dirty = true;
+  params_changed(c);
   if (c->mr > 0) {
     if ((rc = dev_alloc(c, c->raw, (size_t)c->mt2 * c->mr * 6 * c->prec)) != FDP_OK) return rc;
   }
@@ -819,7 +921,7 @@ int fdp_set_receivers(fdp_ctx* c, const int32_t* irecx, const int32_t* lrecx, co
     if ((rc = dev_alloc(c, c->raw, (size_t)c->mt2 * mr * 6 * c->prec)) != FDP_OK) return rc;
   }
   CK(c, cudaStreamSynchronize(c->stream));
-  c->params_dirty = true;
+  params_changed(c);
   return FDP_OK;
 }
 
@@ -849,13 +951,17 @@ int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host
   const size_t lev = (size_t)mr * 6;
   auto body = [&](auto zero) -> int {
     using T = decltype(zero);
-    std::vector<T> raw((size_t)nfetch * lev);
+    HostBuf<T> raw;
+    raw.reset((size_t)nfetch * lev);
     int rc = copy_sync(c, raw.data(), (const T*)c->raw.p + (size_t)(first_fetch - 1) * lev,
                        raw.size() * sizeof(T), cudaMemcpyDeviceToHost);
     if (rc != FDP_OK) return rc;
     const T DT = (T)c->g.dt;
     T* out = (T*)host;
-    for (int n = 0; n < n_levels; ++n) {
+    // levels in parallel (each level's values depend on its own and the
+    // previous level's samples only)
+    parallel_for((size_t)n_levels, [&](size_t nb, size_t ne) {
+    for (int n = (int)nb; n < (int)ne; ++n) {
       const int it = it_first + n;
       const T* cur = &raw[(size_t)(it - first_fetch) * lev];
       const T* prv = (it - 1 >= first_fetch) ? &raw[(size_t)(it - 1 - first_fetch) * lev] : nullptr;
@@ -877,6 +983,7 @@ int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host
         if (c->rec_flags & FDP_REC_TLP) { r[8] = s[4]; r[9] = s[5]; }
       }
     }
+    }, 64);
     return FDP_OK;
   };
   return c->prec == 8 ? body(0.0) : body(0.0f);
@@ -1034,6 +1141,7 @@ void fdp_destroy(fdp_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   fdp::edge_release(c);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  unshare_medium(c);
   DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase,
                    &c->errbuf, &c->frame_s, &c->frame_v};
   for (auto* a : all) if (a->p) cudaFree(a->p);
@@ -1067,6 +1175,7 @@ struct BatchGroup {
 
 struct fdp_batch {
   std::vector<fdp_ctx*> shots;  // sorted by group
+  std::vector<unsigned long long> gens;  // each shot's parameter generation at creation
   std::vector<BatchGroup> groups;
   int prec = 4, device = 0;
   cudaStream_t stream = nullptr;
@@ -1406,6 +1515,7 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
       (rc = alloc(b->itbase, sizeof(int))))
     return bail(rc);
   std::vector<unsigned char> host(psize * n);
+  for (int s = 0; s < n; ++s) b->gens.push_back(b->shots[s]->gen);
   for (int s = 0; s < n; ++s) {
     if (b->prec == 8) {
       Params<double> p;
@@ -1456,9 +1566,13 @@ int fdp_batch_get_shape(fdp_batch* b, int32_t* units_per_item, int32_t* waves) {
 int fdp_batch_run(fdp_batch* b, int32_t it_begin, int32_t it_end) {
   if (!b) return bfail(b, FDP_ERR_ARG, "null batch");
   if (it_end < it_begin) return FDP_OK;
-  for (size_t s = 0; s < b->shots.size(); ++s)
+  for (size_t s = 0; s < b->shots.size(); ++s) {
     if (it_begin < 1 || it_end > b->shots[s]->mt2)
       return bfail(b, FDP_ERR_ARG, "levels %d..%d outside 1..MT2=%d of a shot", it_begin, it_end, b->shots[s]->mt2);
+    // the batch holds copies of each shot's device parameters
+    if (b->shots[s]->gen != b->gens[s])
+      return bfail(b, FDP_ERR_STATE, "a shot's medium, source, receivers or edge changed after fdp_batch_create");
+  }
   BCK(b, cudaSetDevice(b->device));
   const int rc = b->prec == 8 ? batch_run_t<double>(b, it_begin, it_end) : batch_run_t<float>(b, it_begin, it_end);
   if (rc == FDP_OK)

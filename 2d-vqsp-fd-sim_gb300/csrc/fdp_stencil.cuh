@@ -495,10 +495,13 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
 // Unit rows tile the grid from row 0 down, so unit row 0 holds rows 2..4
 // that the stress-imaging mirror rows 0 and 1 copy.  k_stress runs one unit
 // per block, the frame and batched kernels the units of their lists.
+// stress_unit's cells of thread (tx, ty) of the unit, without the
+// stress-imaging mirror rows.
 template <class T, bool SI, int MODE>
-__device__ __forceinline__ void stress_unit(const Params<T>& p, int I0, int I1, int by, int it_off) {
-  const int I = I0 + (int)threadIdx.x;
-  const int L0 = (int)(by * kBZ + threadIdx.y) * kRZS;  // rows L0 .. L0+kRZS-1
+__device__ __forceinline__ void stress_unit_cells(const Params<T>& p, int I0, int I1, int by, int it_off, int tx,
+                                                  int ty) {
+  const int I = I0 + tx;
+  const int L0 = (by * kBZ + ty) * kRZS;  // rows L0 .. L0+kRZS-1
   const bool core = p.cs_x1 > p.cs_x0;  // the core kernel updates the core cells
   if (!core && I1 > p.PMLXH && stress_fast_rows(p, I, L0)) {
     stress_interior_rows<T, MODE>(p, I, L0);
@@ -511,18 +514,27 @@ __device__ __forceinline__ void stress_unit(const Params<T>& p, int I0, int I1, 
       if (L <= p.PMLZH && (!SI || L >= 2) && !(incol && L >= p.cs_z0 && L < p.cs_z1 && L != p.LIN_Z))
         stress_cell<T, SI, MODE>(p, rd, I, L, it);
   }
+}
+
+// The stress-imaging mirror rows 0 and 1 of column I from the new rows
+// 2..4 (hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53).
+template <class T>
+__device__ __forceinline__ void stress_mirror(const Params<T>& p, int I) {
+  FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
+  FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
+  FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
+  FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
+  FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
+  FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
+  FDP_F(p.TXZ, I, 2) = T(0);
+}
+
+template <class T, bool SI, int MODE>
+__device__ __forceinline__ void stress_unit(const Params<T>& p, int I0, int I1, int by, int it_off) {
+  stress_unit_cells<T, SI, MODE>(p, I0, I1, by, it_off, (int)threadIdx.x, (int)threadIdx.y);
   if (SI && by == 0) {
     __syncthreads();  // rows 2..4 of this unit are final
-    if (I < I1 && threadIdx.y == 0) {
-      // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53
-      FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
-      FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
-      FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
-      FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
-      FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
-      FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
-      FDP_F(p.TXZ, I, 2) = T(0);
-    }
+    if (I0 + (int)threadIdx.x < I1 && threadIdx.y == 0) stress_mirror(p, I0 + (int)threadIdx.x);
   }
 }
 
@@ -846,9 +858,9 @@ __global__ void __launch_bounds__(kBX * kBZ) k_stress_frame(const __grid_constan
 // Velocity frame cells up to row PMLZH-3, one row per thread: columns
 // [I0, I1), rows L0 .. L0+kBZ-1.
 template <class T, bool SI, int MODE>
-__device__ __forceinline__ void velocity_row_unit(const Params<T>& p, int I0, int I1, int L0) {
-  const int I = I0 + (int)threadIdx.x;
-  const int L = L0 + (int)threadIdx.y;
+__device__ __forceinline__ void velocity_row_unit(const Params<T>& p, int I0, int I1, int L0, int tx, int ty) {
+  const int I = I0 + tx;
+  const int L = L0 + ty;
   const bool incore = I >= p.cv_x0 && I < p.cv_x1 && L >= p.cv_z0 && L < p.cv_z1;
   if (I < I1 && L <= p.PMLZH - 3 && L >= (SI ? 2 : 0) && !incore) {
     const GlobalRd<T> rd{{p.TXX, p.TZZ, p.TXZ, p.PRES}, p.pitch, p.PMLL};
@@ -861,8 +873,8 @@ __device__ __forceinline__ void velocity_row_unit(const Params<T>& p, int I0, in
 // and pre-phase values and the history (time_loop.F90:133-155,
 // hplane_pmlzh0_velocity.F90:34-63).
 template <class T, bool SI, int MODE>
-__device__ __forceinline__ void velocity_bottom_unit(const Params<T>& p, int I0, int I1) {
-  const int I = I0 + (int)(threadIdx.y * kBX + threadIdx.x);
+__device__ __forceinline__ void velocity_bottom_unit(const Params<T>& p, int I0, int I1, int t) {
+  const int I = I0 + t;
   if (I >= I1) return;
   const int LST = p.PMLZH;
   T old[3][4];  // pre-phase values of rows PMLZH-k of u, w, qx, qz
@@ -897,8 +909,8 @@ __device__ __forceinline__ void velocity_bottom_unit(const Params<T>& p, int I0,
 // bottom three rows.
 template <class T, bool SI, int MODE>
 __device__ __forceinline__ void velocity_frame_unit(const Params<T>& p, const int4 u) {
-  if (u.w == 2) velocity_bottom_unit<T, SI, MODE>(p, u.x, u.y);
-  else velocity_row_unit<T, SI, MODE>(p, u.x, u.y, u.z);
+  if (u.w == 2) velocity_bottom_unit<T, SI, MODE>(p, u.x, u.y, (int)(threadIdx.y * kBX + threadIdx.x));
+  else velocity_row_unit<T, SI, MODE>(p, u.x, u.y, u.z, (int)threadIdx.x, (int)threadIdx.y);
 }
 
 template <class T, bool SI, int MODE>

@@ -87,6 +87,11 @@ class Engine:
         assert tab.ndim == 2 and tab.shape[1] == 24
         self._check(self.lib.fdp_set_medium(self._ctx, _iptr(jm), self.nx, self.nz, tab.shape[0], _ptr(tab)))
 
+    def share_medium(self, other: "Engine") -> None:
+        """Uses ``other``'s device medium instead of a copy of its own
+        (``fdp_share_medium``): same grid, precision and device."""
+        self._check(self.lib.fdp_share_medium(self._ctx, other._ctx))
+
     def set_pml(self, profiles: list[np.ndarray]) -> None:
         arrs = [self._real(p) for p in profiles]
         assert len(arrs) == 24
@@ -117,7 +122,8 @@ class Engine:
 
     def receivers(self, it_first: int, n_levels: int) -> np.ndarray:
         """(n_levels, MR, 10) values in STORE_SEISMOGRAMS column order."""
-        out = np.zeros((n_levels, self.mr, native.FDP_REC_VALUES), dtype=self.dtype)
+        # fdp_get_receivers writes every value (zeros where a flag is off)
+        out = np.empty((n_levels, self.mr, native.FDP_REC_VALUES), dtype=self.dtype)
         self._check(self.lib.fdp_get_receivers(self._ctx, it_first, n_levels, _ptr(out)))
         return out
 

@@ -13,6 +13,7 @@ READ_MODEL (JM expansion), READ_MODEL_PAR (table scaling), OPEN_SR_FILE
 from __future__ import annotations
 
 import ctypes as C
+import dataclasses
 import math
 from dataclasses import dataclass, field
 
@@ -202,22 +203,37 @@ def prepare(cfg: JobConfig, medium: Medium, precision: str = "f32") -> Inputs:
                   np.asarray(cfg.irecz, np.int32), np.asarray(cfg.lrecz, np.int32), cfg.rec_flags)
 
 
-def load_inputs(engine, inp: Inputs) -> None:
-    """Sets the module state of an engine (GPU or oracle) from prepared inputs."""
-    engine.set_medium(inp.jm, inp.table)
+def load_inputs(engine, inp: Inputs, medium_from=None) -> None:
+    """Sets the module state of an engine (GPU or oracle) from prepared
+    inputs; with ``medium_from`` (an engine of the same grid) the medium is
+    shared with that engine instead of uploaded again."""
+    if medium_from is None:
+        engine.set_medium(inp.jm, inp.table)
+    else:
+        engine.share_medium(medium_from)
     engine.set_pml(inp.profiles)
     engine.set_bottom_nr(inp.ab)
     engine.set_source(inp.sourtf)
     engine.set_receivers(inp.irecx, inp.lrecx, inp.irecz, inp.lrecz, inp.rec_flags)
 
 
-def make_engine(inp: Inputs, device: int = 0):
+def make_engine(inp: Inputs, device: int = 0, medium_from=None):
     from .engine import Engine
     e = Engine(inp.mx, inp.mz, inp.tpml, inp.lin_x, inp.lin_z, inp.h, inp.dt,
                precision="f64" if inp.precision == FDP_F64 else "f32",
                stress_imaging=inp.stress_imaging, device=device)
-    load_inputs(e, inp)
+    load_inputs(e, inp, medium_from)
     return e
+
+
+def with_source(inp: Inputs, cfg: JobConfig, x_source: float, z_source: float) -> Inputs:
+    """The same prepared job with the source moved: LIN_X and LIN_Z as
+    READ_OPEN computes them for the new position; the medium, PML profiles,
+    bottom coefficients, source time function and receivers stay (none of
+    them depends on where the source is)."""
+    c = dataclasses.replace(cfg, x_source=x_source, z_source=z_source)
+    lin_x, lin_z = source_cell(c, inp.h)
+    return dataclasses.replace(inp, lin_x=lin_x, lin_z=lin_z)
 
 
 # ---------------------------------------------------------------------------
@@ -271,6 +287,20 @@ def batch_shots(n_shots: int = 64, nsteps: int = 3000, seed: int = 20251, sides=
         out.append((seed * 1000 + k, dict(mx=mx, mz=mz, nsteps=nsteps, tpml=tpml, f0=f0, dt=dt, h=h, n_rec=n_rec,
                                           x_source=xs, z_source=zs)))
     return out
+
+
+def large_shots(n_shots: int = 16, mx: int = 8192, mz: int = 8192, nsteps: int = 10000, seed: int = 20252,
+                tpml: int = 20, n_rec: int = 512) -> tuple[JobConfig, Medium, list[tuple[float, float]]]:
+    """The large survey: one layered random medium of :func:`layered` shared
+    by ``n_shots`` shots whose sources lie uniformly in the upper quarter;
+    returns the first shot's configuration, the medium and every shot's
+    (x_source, z_source)."""
+    cfg, med = layered(mx=mx, mz=mz, nsteps=nsteps, tpml=tpml, n_rec=n_rec, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    pos = [(float(rng.uniform(0.05, 0.95) * mx * cfg.h), float(rng.uniform(0.01, 0.25) * mz * cfg.h))
+           for _ in range(n_shots)]
+    cfg.x_source, cfg.z_source = pos[0]
+    return cfg, med, pos
 
 
 def batch_shot(seed: int, mx: int, mz: int, nsteps: int, tpml: int, f0: float, dt: float, h: float, n_rec: int,

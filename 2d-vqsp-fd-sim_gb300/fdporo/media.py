@@ -136,13 +136,20 @@ def layered_grf(mx: int, n_rows: int, h: float, seed: int, layer_depth: float = 
     depth = np.arange(n_rows, dtype=np.float64)[:, None] * h
     low = depth >= layer_depth
     g = gaussian_random_field((n_rows, mx), corr_len / h, seed)
-    fac = 1.0 + std * g
+    t = np.empty((n_rows, mx, 24), dtype=np.float64)
+    # blocks of rows, so that the element-wise temporaries stay small on
+    # large grids (the values do not depend on the blocking)
+    step = max(1, (1 << 22) // max(mx, 1))
+    for r0 in range(0, n_rows, step):
+        r1 = min(n_rows, r0 + step)
+        fac = 1.0 + std * g[r0:r1]
 
-    def pick(name):
-        a, b = getattr(upper, name), getattr(lower, name)
-        return np.where(low, b, a) * np.ones((n_rows, mx))
+        def pick(name):
+            a, b = getattr(upper, name), getattr(lower, name)
+            return np.where(low[r0:r1], b, a) * np.ones((r1 - r0, mx))
 
-    t = biot_table(pick("rho_s"), pick("rho_f"), pick("phi") * fac, pick("k_s"), pick("k_f"),
-                   pick("k_frame") * fac, pick("mu") * fac, pick("kappa"), pick("eta"), pick("tortuosity"))
+        t[r0:r1] = biot_table(pick("rho_s"), pick("rho_f"), pick("phi") * fac, pick("k_s"), pick("k_f"),
+                              pick("k_frame") * fac, pick("mu") * fac, pick("kappa"), pick("eta"),
+                              pick("tortuosity"))
     jm = (np.arange(n_rows * mx, dtype=np.int32) + 1).reshape(n_rows, mx)
     return Medium(jm, t.reshape(-1, 24))

@@ -11,6 +11,12 @@ from pathlib import Path
 from .build import LIB_PATH, build
 
 FDP_OK = 0
+FDP_ERR_ARG = -1
+FDP_ERR_CUDA = -2
+FDP_ERR_ALLOC = -3
+FDP_ERR_STATE = -4
+FDP_ERR_UNSUPPORTED = -5
+FDP_ERR_DEVICE = -6
 FDP_F32 = 4
 FDP_F64 = 8
 
@@ -59,6 +65,7 @@ _PD = C.POINTER(C.c_double)
 SIGNATURES = {
     "fdp_create": (C.c_int, [C.POINTER(fdp_grid), C.POINTER(_VP)]),
     "fdp_set_medium": (C.c_int, [_VP, _PI32, _I32, _I32, _I32, _VP]),
+    "fdp_share_medium": (C.c_int, [_VP, _VP]),
     "fdp_set_pml": (C.c_int, [_VP, C.POINTER(_VP)]),
     "fdp_set_bottom_nr": (C.c_int, [_VP, _VP]),
     "fdp_set_source": (C.c_int, [_VP, _VP, _I32]),

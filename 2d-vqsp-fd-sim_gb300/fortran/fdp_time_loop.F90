@@ -31,6 +31,10 @@ MODULE FDP_GB300
       TYPE(C_PTR), VALUE :: CTX, JM, TABLE24
       INTEGER(C_INT32_T), VALUE :: NX, NZ, JMNUM
     END FUNCTION FDP_SET_MEDIUM
+    INTEGER(C_INT) FUNCTION FDP_SHARE_MEDIUM(DST, SRC) BIND(C, NAME='fdp_share_medium')
+      IMPORT :: C_INT, C_PTR
+      TYPE(C_PTR), VALUE :: DST, SRC
+    END FUNCTION FDP_SHARE_MEDIUM
     INTEGER(C_INT) FUNCTION FDP_SET_PML(CTX, PROFILES24) BIND(C, NAME='fdp_set_pml')
       IMPORT :: C_INT, C_PTR
       TYPE(C_PTR), VALUE :: CTX

@@ -444,6 +444,105 @@ def run_batch(args) -> None:
         print(json.dumps(line), flush=True)
 
 
+LARGE = dict(shots=16, mx=8192, mz=8192, mt2=10000, seed=20252)
+
+
+def run_large(args) -> None:
+    """Large survey: LARGE['shots'] shots over one 8192^2 layered random
+    medium (per-cell, config-2 generator, free surface on top, 20-cell PML
+    on the other sides), sources uniform in the upper quarter, FP32.  The
+    medium is derived and uploaded once and shared by every shot
+    (fdp_share_medium); all field state stays on the device; the shots are
+    advanced together by fdp_batch.  Compared with the plain single-shot
+    path: the first shot alone through fdp_run."""
+    import torch
+    from fdporo import job
+    from fdporo.engine import Batch
+    ws, rank, local = _dist()
+    dev = local if torch.cuda.is_available() else 0
+    n = args.shots if args.shots != BATCH["shots"] else LARGE["shots"]
+    t0 = time.perf_counter()
+    cfg, med, pos = job.large_shots(n, mx=LARGE["mx"], mz=LARGE["mz"], nsteps=LARGE["mt2"], seed=LARGE["seed"])
+    inp = job.prepare(cfg, med, "f32")
+    del med
+    t_prep = time.perf_counter() - t0
+    free0 = torch.cuda.mem_get_info(dev)[0]
+    t0 = time.perf_counter()
+    owner = job.make_engine(inp, device=dev)
+    engines = [owner] + [job.make_engine(job.with_source(inp, cfg, x, z), device=dev, medium_from=owner)
+                         for x, z in pos[1:]]
+    t_upload = time.perf_counter() - t0
+    used = free0 - torch.cuda.mem_get_info(dev)[0]
+    medium = owner.medium_info()
+    core = owner.core_info()
+    # the planes as the engine pads them: pitch of NX + 8 rounded up to 32, NZ + 4 rows
+    pitch = (inp.nx + 8 + 31) // 32 * 32
+    plane_bytes = (medium["planes_stress"] + medium["planes_velocity"]) * 4 * pitch * (inp.nz + 4)
+    ab = algorithmic_bytes(inp, 4, medium)
+    level_bytes = n * (ab["stress"] + ab["velocity"])
+    cells = n * inp.cells
+    K, W = args.steps, max(args.warmup, 20)  # the batch tunes its shape on its first 18 levels
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b = Batch(engines)
+    ext = torch.cuda.ExternalStream(b.stream(), device=dev)
+    b.time_loop(1, W)
+    b.synchronize()
+    launches0 = b.kernel_launches()
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        e0.record(ext)
+        b.time_loop(W + 1, W + K)
+        e1.record(ext)
+        e1.synchronize()
+    ms_batch = e0.elapsed_time(e1) / K
+    launches = b.kernel_launches() - launches0
+    shape = b.shape()
+    b.synchronize()
+    b.close()
+    for e in engines[1:]:
+        e.close()
+    # the plain single-shot path: the first shot alone
+    lo = W + K + 1
+    owner.time_loop(lo, lo + W - 1)
+    owner.synchronize()
+    lo += W
+    st = torch.cuda.ExternalStream(owner.stream(), device=dev)
+    e0.record(st)
+    owner.time_loop(lo, lo + K - 1)
+    e1.record(st)
+    e1.synchronize()
+    ms_single = e0.elapsed_time(e1) / K
+    owner.close()
+    peak, peak_kind = measured_peak_gbs()
+    gbs = level_bytes / (ms_batch / 1e3) / 1e9
+    shots_h = lambda ms, k: k * 3600.0 / (LARGE["mt2"] * ms / 1e3)
+    line = {
+        "metric": "Gcell-updates/s", "value": cells / (ms_batch / 1e3) / 1e9, "unit": "Gcell-updates/s",
+        "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (one seeded layered medium with a Gaussian random field, shared by every shot)",
+        "config": {"workload": f"large-{LARGE['mx']}-x{n}", "shots": n, "mx": LARGE["mx"], "mz": LARGE["mz"],
+                   "cells_per_shot": inp.cells, "cells_per_level": cells, "tpml": inp.tpml,
+                   "levels_per_shot": LARGE["mt2"], "edge": "20-cell PML (the learned edge's fallback)",
+                   "l2": "inputs larger than L2 (no flush)", "medium": "shared (one copy on the device)"},
+        "shots_per_hour": shots_h(ms_batch, n),
+        "single_shot": {"ms_per_level": ms_single, "shots_per_hour": shots_h(ms_single, 1),
+                        "gcell_updates_per_s": inp.cells / (ms_single / 1e3) / 1e9},
+        "speedup_vs_single_shot_path": shots_h(ms_batch, n) / shots_h(ms_single, 1),
+        "roofline": {"bound": "hbm", "kernel": "whole level (batched phases)", "achieved": gbs, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": gbs / peak, "traffic": None,
+                     "alg_bytes_per_level": level_bytes},
+        "device_memory": {"used_bytes": used, "medium_planes_bytes": plane_bytes,
+                          "without_sharing_bytes": used + (n - 1) * plane_bytes},
+        "setup_s": {"medium_and_prepare": t_prep, "engines": t_upload},
+        "tile_shape": {"units_per_item": shape[0], "waves": shape[1]},
+        "core": core,
+        "gpu_launches": launches, "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 EDGE = dict(n=512, margin=256, depth_margin=512, levels=2000, f0=20.0, seed=40000)
 
 
@@ -539,7 +638,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--workload", choices=["layered", "batch", "edge"], default="layered")
+    ap.add_argument("--workload", choices=["layered", "batch", "edge", "large"], default="layered")
     ap.add_argument("--edge-train", type=int, default=32)
     ap.add_argument("--edge-held", type=int, default=8)
     ap.add_argument("--edge-epochs", type=int, default=1)
@@ -554,6 +653,8 @@ def main() -> None:
         run_batch(args)
     elif args.workload == "edge":
         run_edge(args)
+    elif args.workload == "large":
+        run_large(args)
     else:
         run_gpu(args)
 

@@ -103,7 +103,9 @@ enum fdp_field_id {
  * runs vectorised beside a frame kernel for the PML, free-surface, source
  * and bottom cells on a second stream; "fused" runs frame and core of a
  * phase in one launch; "global" runs one unit kernel per phase over the
- * whole grid; "tma" the TMA-staged variant of the latter. */
+ * whole grid; "tma" the TMA-staged variant of the latter; "coretma" the
+ * default split with TMA-staged persistent core kernels (FP32 contexts with
+ * a Biot-plane medium; others keep the per-thread-load core). */
 int fdp_create(const fdp_grid* grid, fdp_ctx** out);
 
 /* Medium: JM(PMLL:PMLXH, 0:PMLZH) (nx = MX+2*TPML, nz = PMLZH+1) after
@@ -116,6 +118,16 @@ int fdp_create(const fdp_grid* grid, fdp_ctx** out);
  * read_model_par.F90:158-169 does. */
 int fdp_set_medium(fdp_ctx* ctx, const int32_t* jm, int32_t nx, int32_t nz, int32_t jmnum,
                    const void* table24);
+
+/* Makes dst use src's device medium (JM, material table or per-cell planes,
+ * AUXIL) instead of holding its own copy: shots of one survey over the same
+ * model (GRID_MEDIUM is the same module state for all of them in the
+ * reference, read_model.F90 / read_model_par.F90) keep one copy in HBM and
+ * derive it once.  Both contexts need the same grid (MX, MZ, TPML),
+ * precision and device, and src a medium.  dst's own medium is freed; the
+ * shared arrays live until the last context using them is destroyed or
+ * given a medium of its own by fdp_set_medium. */
+int fdp_share_medium(fdp_ctx* dst, fdp_ctx* src);
 
 /* PML damping profiles from PPML (ppml.F90:156-306), 24 arrays in this order:
  *   ODA_XL ODB_XL ODC_XL ODD_XL ODA_XH ODB_XH ODC_XH ODD_XH      (0:TPML,   0:PMLZH)
@@ -252,7 +264,10 @@ typedef struct fdp_batch fdp_batch;
 /* Groups n contexts, each with medium, PML, bottom coefficients and source
  * set.  The contexts stay owned by the caller and must outlive the batch;
  * while it exists, run them only through it.  After fdp_batch_synchronize
- * their receivers, snapshots and fields are read with the fdp_get_* calls. */
+ * their receivers, snapshots and fields are read with the fdp_get_* calls.
+ * The batch copies each context's device parameters: a context given a new
+ * medium, source, receivers or edge afterwards makes fdp_batch_run return
+ * FDP_ERR_STATE (create the batch again). */
 int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out);
 
 /* Advances every shot over levels it_begin..it_end (within every shot's

@@ -55,6 +55,7 @@ def test_create_rejects_bad_geometry(fdp_lib, bad):
 def test_null_context_is_rejected(fdp_lib):
     assert fdp_lib.fdp_run(None, 1, 1) == -1
     assert fdp_lib.fdp_synchronize(None) == -1
+    assert fdp_lib.fdp_share_medium(None, None) == -1
     fdp_lib.fdp_destroy(None)
 
 
