@@ -1089,45 +1089,56 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
     Params<T> p;
     fill_params<T>(c, p);
     const int nedge = edge_threads(c);
-    cudaEvent_t ev[4];
-    for (auto& e : ev) CK(c, cudaEventCreate(&e));
     const bool core[2] = {c->use_core && !c->fused[0] && c->cs[1] > c->cs[0],
                           c->use_core && !c->fused[1] && c->cv[1] > c->cv[0]};
-    for (int k = 0; k < 2; ++k)
-      if (core[k]) for (auto& e : c->core_ev[k]) CK(c, cudaEventCreate(&e));
-    fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
-    for (int it = it_begin; it <= it_end; ++it) {
-      const int off = it - it_begin;
-      CK(c, cudaEventRecord(ev[0], c->stream));
-      launch<T>(c, p, 0, off);
-      CK(c, cudaEventRecord(ev[1], c->stream));
-      launch<T>(c, p, 1, off);
-      CK(c, cudaEventRecord(ev[2], c->stream));
-      if (nedge > 0) launch<T>(c, p, 2, off);
-      c->launches += fdp::edge_launch(c, off);
-      CK(c, cudaEventRecord(ev[3], c->stream));
-      CK(c, cudaEventSynchronize(ev[3]));
-      float t;
-      for (int k = 0; k < 3; ++k) {
-        CK(c, cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
-        ms_out[k] += t;
-      }
-      for (int k = 0; k < 2; ++k)
-        if (core[k]) {
-          CK(c, cudaEventElapsedTime(&t, c->core_ev[k][0], c->core_ev[k][1]));
-          ms_out[3 + k] += t;
-          launches_out[3 + k] += 1;
+    // every level is enqueued before the one synchronisation at the end, so
+    // the device never waits for the host and each window holds device time
+    // only: per level, events around the two phases and the edge, and
+    // around each phase's core kernel
+    const int n = it_end - it_begin + 1;
+    std::vector<cudaEvent_t> ev((size_t)n * 8, nullptr);
+    int rc = FDP_OK;
+    for (auto& e : ev)
+      if (cudaEventCreate(&e) != cudaSuccess) { e = nullptr; rc = fail(c, FDP_ERR_CUDA, "cudaEventCreate failed"); break; }
+    if (rc == FDP_OK) {
+      fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
+      for (int it = it_begin; it <= it_end; ++it) {
+        const int off = it - it_begin;
+        cudaEvent_t* e = &ev[(size_t)off * 8];
+        for (int k = 0; k < 2; ++k) {
+          c->core_ev[k][0] = core[k] ? e[4 + 2 * k] : nullptr;
+          c->core_ev[k][1] = core[k] ? e[5 + 2 * k] : nullptr;
         }
-      launches_out[0] += 1; launches_out[1] += 1; launches_out[2] += nedge > 0 ? 1 : 0;
+        cudaEventRecord(e[0], c->stream);
+        launch<T>(c, p, 0, off);
+        cudaEventRecord(e[1], c->stream);
+        launch<T>(c, p, 1, off);
+        cudaEventRecord(e[2], c->stream);
+        if (nedge > 0) launch<T>(c, p, 2, off);
+        c->launches += fdp::edge_launch(c, off);
+        cudaEventRecord(e[3], c->stream);
+      }
+      fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
+      c->launches += 2;
+      for (auto& pair : c->core_ev) pair[0] = pair[1] = nullptr;
+      cudaError_t err = cudaStreamSynchronize(c->stream);
+      if (err == cudaSuccess) err = cudaGetLastError();
+      if (err != cudaSuccess) rc = fail(c, FDP_ERR_CUDA, "profile run: %s", cudaGetErrorString(err));
+      for (int off = 0; off < n && rc == FDP_OK; ++off) {
+        const cudaEvent_t* e = &ev[(size_t)off * 8];
+        float t;
+        for (int k = 0; k < 3; ++k)
+          if (cudaEventElapsedTime(&t, e[k], e[k + 1]) == cudaSuccess) ms_out[k] += t;
+        for (int k = 0; k < 2; ++k)
+          if (core[k] && cudaEventElapsedTime(&t, e[4 + 2 * k], e[5 + 2 * k]) == cudaSuccess) {
+            ms_out[3 + k] += t;
+            launches_out[3 + k] += 1;
+          }
+        launches_out[0] += 1; launches_out[1] += 1; launches_out[2] += nedge > 0 ? 1 : 0;
+      }
     }
-    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_end - it_begin + 1);
-    c->launches += 2;
-    for (auto& e : ev) cudaEventDestroy(e);
-    for (auto& pair : c->core_ev)
-      for (auto& e : pair)
-        if (e) { cudaEventDestroy(e); e = nullptr; }
-    CK(c, cudaStreamSynchronize(c->stream));
-    CK(c, cudaGetLastError());
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+    if (rc != FDP_OK) return rc;
     if (it_end > c->last_it) c->last_it = it_end;
     return FDP_OK;
   };

@@ -381,6 +381,14 @@ __device__ __forceinline__ T strain_zz_pml(const Params<T>& p, const R& rd, int 
 // Stress update of one cell (I, L): the row routines of hplane_ic_stress,
 // hplane_lin_stress, hplane_0/1_stress (non-imaging), hplane_mz1_stress,
 // hplane_pml_stress and hplane_pmlzh0_stress restricted to that cell.
+//
+// Every value the cell reads is loaded first -- the velocity neighbourhood
+// unconditionally (the neighbours lie in the arrays' padding where they are
+// unused), the PML memory variables and profiles of its region, its
+// coefficients and its old stresses -- then the arithmetic runs, then every
+// store: a frame cell costs one round trip to memory instead of one per
+// strain, whose memory-variable stores would otherwise order the next
+// strain's loads behind them.
 template <class T, bool SI, int MODE, class R>
 __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int I, int L, int it) {
   const int TPML = p.TPML, MX = p.MX, MX1 = p.MX1;
@@ -391,102 +399,169 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
   const bool mz1 = (L == p.MZ - 1);
   const bool r0 = (!SI) && (L == 0);
   const bool r1 = (!SI) && (L == 1);
+  const bool do_xz = I >= 2 - TPML && I <= MX + TPML;            // stress_xz.F90:40
+  const bool do_nn = !last && I >= 2 - TPML && I <= MX1 + TPML;  // stress_nn.F90:49
 
-  // ---------------- EXZ and TXZ: I = 2-TPML .. MX+TPML (stress_xz.F90:40)
-  if (I >= 2 - TPML && I <= MX + TPML) {
-    T exz;
+  // ---- loads
+  // u: column I rows L-2..L+1 and row L columns I-1..I+2; w: row L columns
+  // I-2..I+1 and column I rows L-1..L+2; qx: row L columns I-1..I+2; qz:
+  // column I rows L-1..L+2
+  const T u_m2 = rd(0, I, L - 2), u_m1 = rd(0, I, L - 1), u_0 = rd(0, I, L), u_p1 = rd(0, I, L + 1);
+  const T u_xm1 = rd(0, I - 1, L), u_xp1 = rd(0, I + 1, L), u_xp2 = rd(0, I + 2, L);
+  const T w_xm2 = rd(1, I - 2, L), w_xm1 = rd(1, I - 1, L), w_0 = rd(1, I, L), w_xp1 = rd(1, I + 1, L);
+  const T w_m1 = rd(1, I, L - 1), w_p1 = rd(1, I, L + 1), w_p2 = rd(1, I, L + 2);
+  const T x_m1 = rd(2, I - 1, L), x_0 = rd(2, I, L), x_p1 = rd(2, I + 1, L), x_p2 = rd(2, I + 2, L);
+  const T z_m1 = rd(3, I, L - 1), z_0 = rd(3, I, L), z_p1 = rd(3, I, L + 1), z_p2 = rd(3, I, L + 2);
+  // exz: the z-PML part (strain_uw_xz_2nd_pml.F90) and the x-PML part of
+  // the side strips (strain_uw_xz.F90:181-196, 209-223 and the PML rows)
+  const bool xz_z = do_xz && !r0 && (pml || last);
+  const bool xz_lo = do_xz && !r0 && I <= 2, xz_hi = do_xz && !r0 && I > MX1;
+  const int zi = (I - p.PMLL) + (last ? TPML + 1 : L - p.MZ + 1) * p.NX;
+  T mz = T(0), za = T(0), zd = T(0), zb = T(0), zc = T(0);
+  if (xz_z) { mz = p.PXZH[zi]; za = p.ODA2_ZH[zi]; zd = p.ODD2_ZH[zi]; zb = p.ODB2_ZH[zi]; zc = p.ODC2_ZH[zi]; }
+  const int xz_xi = xz_lo ? (3 - I) + L * (TPML + 2) : (I - MX1) + L * (TPML + 2);
+  const int xz_mi = xz_lo ? (I - p.PMLL) + L * (TPML + 2) : (I - MX) + L * (TPML + 1);
+  T* const xz_m = xz_lo ? p.PZXL : p.PZXH;
+  T mx = T(0), xa = T(0), xd = T(0), xb = T(0), xc = T(0);
+  if (xz_lo || xz_hi) {
+    const T* a_ = xz_lo ? p.ODA2_XL : p.ODA2_XH;
+    const T* d_ = xz_lo ? p.ODD2_XL : p.ODD2_XH;
+    const T* b_ = xz_lo ? p.ODB2_XL : p.ODB2_XH;
+    const T* c_ = xz_lo ? p.ODC2_XL : p.ODC2_XH;
+    mx = xz_m[xz_mi]; xa = a_[xz_xi]; xd = d_[xz_xi]; xb = b_[xz_xi]; xc = c_[xz_xi];
+  }
+  // ezz, qzz in the PML rows and row MZ-1 (strain_*_zz_2nd_pml.F90)
+  const bool zz_pml = do_nn && !r0 && (pml || mz1);
+  const int zj = (I - p.PMLL) + (mz1 ? 0 : L - p.MZ + 1) * p.NX;
+  T me = T(0), mq = T(0), pa = T(0), pd = T(0), pb = T(0), pc = T(0);
+  if (zz_pml) { me = p.PZZH[zj]; mq = p.OZZH[zj]; pa = p.ODA_ZH[zj]; pd = p.ODD_ZH[zj]; pb = p.ODB_ZH[zj]; pc = p.ODC_ZH[zj]; }
+  // exx, qxx in the side strips (strain_uw_xx.F90:51-94, strain_q_xx.F90:50-91)
+  const bool xx_lo = do_nn && I <= 1, xx_hi = do_nn && I >= MX;
+  const int xx_xi = xx_lo ? (2 - I) + L * (TPML + 1) : (I - MX1) + L * (TPML + 1);
+  const int xx_mi = xx_lo ? (I - p.PMLL) + L * (TPML + 1) : (I - MX) + L * (TPML + 1);
+  T* const xx_me = xx_lo ? p.PXXL : p.PXXH;
+  T* const xx_mq = xx_lo ? p.OXXL : p.OXXH;
+  T ne = T(0), nq = T(0), qa = T(0), qd = T(0), qb = T(0), qc = T(0);
+  if (xx_lo || xx_hi) {
+    const T* a_ = xx_lo ? p.ODA_XL : p.ODA_XH;
+    const T* d_ = xx_lo ? p.ODD_XL : p.ODD_XH;
+    const T* b_ = xx_lo ? p.ODB_XL : p.ODB_XH;
+    const T* c_ = xx_lo ? p.ODC_XL : p.ODC_XH;
+    ne = xx_me[xx_mi]; nq = xx_mq[xx_mi]; qa = a_[xx_xi]; qd = d_[xx_xi]; qb = b_[xx_xi]; qc = c_[xx_xi];
+  }
+  T cmu = T(0), txz0 = T(0);
+  if (do_xz) { cmu = FDP_C(C_MU); txz0 = FDP_F(p.TXZ, I, L); }
+  T s1 = T(0), s2 = T(0), s3 = T(0), z1 = T(0), z2 = T(0), z3 = T(0), q1 = T(0), q2 = T(0), q3 = T(0);
+  T txx0 = T(0), tzz0 = T(0), pr0 = T(0);
+  if (do_nn) {
+    s1 = FDP_C(C_SXX1); s2 = FDP_C(C_SXX2); s3 = FDP_C(C_SXX3);
+    z1 = FDP_C(C_SZZ1); z2 = FDP_C(C_SZZ2); z3 = FDP_C(C_SZZ3);
+    q1 = FDP_C(C_P1); q2 = FDP_C(C_P2); q3 = FDP_C(C_P3);
+    txx0 = FDP_F(p.TXX, I, L); tzz0 = FDP_F(p.TZZ, I, L); pr0 = FDP_F(p.PRES, I, L);
+  }
+
+  // ---- arithmetic (the reference's expressions and order)
+  T exz = T(0), mz_new = T(0), mx_new = T(0);
+  if (do_xz) {
     if (r0) {
       exz = T(0);  // hplane_0_stress.F90:58
     } else if (pml || last) {
       // strain_uw_xz_2nd_pml.F90:69-121
-      const int LL = last ? TPML + 1 : L - p.MZ + 1;
-      const T DZXA = p.CH * (rd(1, I, L) - rd(1, I - 1, L));
-      const T DXZA = p.CH * (rd(0, I, L) - rd(0, I, L - 1));
-      const int zi = (I - p.PMLL) + LL * p.NX;
-      const T mz = p.PXZH[zi];
-      const T zpart = p.ODA2_ZH[zi] * (p.ODD2_ZH[zi] * DXZA + mz);
-      if (I <= 2) {
-        const int xi = (3 - I) + L * (TPML + 2);
-        const int mi = (I - p.PMLL) + L * (TPML + 2);
-        const T mx = p.PZXL[mi];
-        exz = zpart + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
-        p.PZXL[mi] = p.ODB2_XL[xi] * mx + p.ODC2_XL[xi] * DZXA;
-      } else if (I <= MX1) {
+      const T DZXA = p.CH * (w_0 - w_xm1);
+      const T DXZA = p.CH * (u_0 - u_m1);
+      const T zpart = za * (zd * DXZA + mz);
+      if (xz_lo || xz_hi) {
+        exz = zpart + xa * (xd * DZXA + mx);
+        mx_new = xb * mx + xc * DZXA;
+      } else {
         exz = zpart + DZXA;
-      } else {
-        const int xi = (I - MX1) + L * (TPML + 2);
-        const int mi = (I - MX) + L * (TPML + 1);
-        const T mx = p.PZXH[mi];
-        exz = zpart + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
-        p.PZXH[mi] = p.ODB2_XH[xi] * mx + p.ODC2_XH[xi] * DZXA;
       }
-      p.PXZH[zi] = p.ODB2_ZH[zi] * mz + p.ODC2_ZH[zi] * DXZA;
-    } else if (I <= 2) {
-      // strain_uw_xz.F90:181-196 (and strain_uw_xz_1.F90:62-76)
-      const T DZXA = p.CH * (rd(1, I, L) - rd(1, I - 1, L));
-      const int xi = (3 - I) + L * (TPML + 2);
-      const int mi = (I - p.PMLL) + L * (TPML + 2);
-      const T mx = p.PZXL[mi];
-      exz = p.CH * (rd(0, I, L) - rd(0, I, L - 1)) + p.ODA2_XL[xi] * (p.ODD2_XL[xi] * DZXA + mx);
-      p.PZXL[mi] = p.ODB2_XL[xi] * mx + p.ODC2_XL[xi] * DZXA;
-    } else if (I <= MX1) {
-      if (r1) {
-        // strain_uw_xz_1.F90:79-97 (AFDA_XZ undefined)
-        exz = p.AH * (rd(1, I + 1, 1) - rd(1, I - 2, 1)) + p.BH * (rd(1, I, 1) - rd(1, I - 1, 1))
-            + p.CH * (rd(0, I, 1) - rd(0, I, 0));
-      } else {
-        // strain_uw_xz.F90:198-206
-        exz = p.AH * (rd(0, I, L + 1) - rd(0, I, L - 2) + rd(1, I + 1, L) - rd(1, I - 2, L))
-            + p.BH * (rd(0, I, L) - rd(0, I, L - 1) + rd(1, I, L) - rd(1, I - 1, L));
-      }
+      mz_new = zb * mz + zc * DXZA;
+    } else if (xz_lo || xz_hi) {
+      // strain_uw_xz.F90:181-196, 209-223 (and strain_uw_xz_1.F90:62-76)
+      const T DZXA = p.CH * (w_0 - w_xm1);
+      exz = p.CH * (u_0 - u_m1) + xa * (xd * DZXA + mx);
+      mx_new = xb * mx + xc * DZXA;
+    } else if (r1) {
+      // strain_uw_xz_1.F90:79-97 (AFDA_XZ undefined)
+      exz = p.AH * (w_xp1 - w_xm2) + p.BH * (w_0 - w_xm1) + p.CH * (u_0 - u_m1);
     } else {
-      // strain_uw_xz.F90:209-223
-      const T DZXA = p.CH * (rd(1, I, L) - rd(1, I - 1, L));
-      const int xi = (I - MX1) + L * (TPML + 2);
-      const int mi = (I - MX) + L * (TPML + 1);
-      const T mx = p.PZXH[mi];
-      exz = p.CH * (rd(0, I, L) - rd(0, I, L - 1)) + p.ODA2_XH[xi] * (p.ODD2_XH[xi] * DZXA + mx);
-      p.PZXH[mi] = p.ODB2_XH[xi] * mx + p.ODC2_XH[xi] * DZXA;
+      // strain_uw_xz.F90:198-206
+      exz = p.AH * (u_p1 - u_m2 + w_xp1 - w_xm2) + p.BH * (u_0 - u_m1 + w_0 - w_xm1);
     }
-    const T TXZv = FDP_C(C_MU) * exz;
-    FDP_F(p.TXZ, I, L) = FDP_F(p.TXZ, I, L) + p.DTE * TXZv;
   }
-  if (last) return;  // hplane_pmlzh0_stress.F90 updates TXZ only
+  // stress_xz.F90:44-46
+  const T TXZv = cmu * exz;
+  const T txz_new = txz0 + p.DTE * TXZv;
 
-  // ---------------- normal stresses: I = 2-TPML .. MX-1+TPML (stress_nn.F90:49)
-  if (I < 2 - TPML || I > MX1 + TPML) return;
-  T ezz, qzz;
-  if (r0) {
-    ezz = (p.CH * (rd(1, I, 1) - rd(1, I, 0)));  // strain_uw_zz_0.F90:45-49
-    qzz = (p.CH * (rd(3, I, 1) - rd(3, I, 0)));  // strain_q_zz_0.F90:40-44
-  } else if (pml || mz1) {
-    const int LL = mz1 ? 0 : L - p.MZ + 1;
-    ezz = strain_zz_pml(p, rd, 1, p.PZZH, I, L, LL);
-    qzz = strain_zz_pml(p, rd, 3, p.OZZH, I, L, LL);
-  } else {
-    ezz = strain_zz(p, rd, 1, I, L);
-    qzz = strain_zz(p, rd, 3, I, L);
+  T txx_new = T(0), tzz_new = T(0), pr_new = T(0), me_new = T(0), mq_new = T(0), ne_new = T(0), nq_new = T(0);
+  if (do_nn) {
+    T ezz, qzz;
+    if (r0) {
+      ezz = (p.CH * (w_p1 - w_0));  // strain_uw_zz_0.F90:45-49
+      qzz = (p.CH * (z_p1 - z_0));  // strain_q_zz_0.F90:40-44
+    } else if (pml || mz1) {
+      // strain_uw_zz_2nd_pml.F90:55-65 / strain_q_zz_2nd_pml.F90:51-64
+      const T De = p.CH * (w_p1 - w_0);
+      ezz = pa * (pd * De + me);
+      me_new = pb * me + pc * De;
+      const T Dq = p.CH * (z_p1 - z_0);
+      qzz = pa * (pd * Dq + mq);
+      mq_new = pb * mq + pc * Dq;
+    } else {
+      // strain_uw_zz.F90:41-51 / strain_q_zz.F90:41-52
+      ezz = (p.CH * (w_p1 - w_0));
+      if (I >= 2 && I <= MX1) ezz = p.AH * (w_p2 - w_m1) + p.BC * ezz;
+      qzz = (p.CH * (z_p1 - z_0));
+      if (I >= 2 && I <= MX1) qzz = p.AH * (z_p2 - z_m1) + p.BC * qzz;
+    }
+    // strain_uw_xx.F90:51-94 / strain_q_xx.F90:50-91
+    T exx, qxx;
+    if (xx_lo || xx_hi) {
+      const T De = p.CH * (u_xp1 - u_0);
+      exx = qa * (qd * De + ne);
+      ne_new = qb * ne + qc * De;
+      const T Dq = p.CH * (x_p1 - x_0);
+      qxx = qa * (qd * Dq + nq);
+      nq_new = qb * nq + qc * Dq;
+    } else if (I == 2 || I == MX1) {
+      exx = p.CH * (u_xp1 - u_0);
+      qxx = p.CH * (x_p1 - x_0);
+    } else {
+      exx = p.AH * (u_xp2 - u_xm1) + p.BH * (u_xp1 - u_0);
+      qxx = p.AH * (x_p2 - x_m1) + p.BH * (x_p1 - x_0);
+    }
+    // stress_nn.F90:53-59
+    const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
+    const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
+    const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
+    if (L == p.LIN_Z && I == p.LIN_X) {
+      // stress_lin_nn.F90:58-63; SOURSP/SOURFP are the previous level's values
+      const T SOURS = p.STF[2 * (it - 1)], SOURF = p.STF[2 * (it - 1) + 1];
+      const T SOURSP = it > 1 ? p.STF[2 * (it - 2)] : T(0);
+      const T SOURFP = it > 1 ? p.STF[2 * (it - 2) + 1] : T(0);
+      txx_new = txx0 + p.DTE * (TXXv - ((SOURS - SOURSP) / p.DT));
+      tzz_new = tzz0 + p.DTE * (TZZv - ((SOURS - SOURSP) / p.DT));
+      pr_new = pr0 + p.DTE * (PRv + ((SOURF - SOURFP) / p.DT));
+    } else {
+      txx_new = txx0 + p.DTE * TXXv;
+      tzz_new = tzz0 + p.DTE * TZZv;
+      pr_new = pr0 + p.DTE * PRv;
+    }
   }
-  const T exx = strain_xx(p, rd, 0, p.PXXL, p.PXXH, I, L);
-  const T qxx = strain_xx(p, rd, 2, p.OXXL, p.OXXH, I, L);
-  const T s1 = FDP_C(C_SXX1), s2 = FDP_C(C_SXX2), s3 = FDP_C(C_SXX3);
-  const T z1 = FDP_C(C_SZZ1), z2 = FDP_C(C_SZZ2), z3 = FDP_C(C_SZZ3);
-  const T q1 = FDP_C(C_P1), q2 = FDP_C(C_P2), q3 = FDP_C(C_P3);
-  const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
-  const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
-  const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
-  if (L == p.LIN_Z && I == p.LIN_X) {
-    // stress_lin_nn.F90:58-63; SOURSP/SOURFP are the previous level's values
-    const T SOURS = p.STF[2 * (it - 1)], SOURF = p.STF[2 * (it - 1) + 1];
-    const T SOURSP = it > 1 ? p.STF[2 * (it - 2)] : T(0);
-    const T SOURFP = it > 1 ? p.STF[2 * (it - 2) + 1] : T(0);
-    FDP_F(p.TXX, I, L) = FDP_F(p.TXX, I, L) + p.DTE * (TXXv - ((SOURS - SOURSP) / p.DT));
-    FDP_F(p.TZZ, I, L) = FDP_F(p.TZZ, I, L) + p.DTE * (TZZv - ((SOURS - SOURSP) / p.DT));
-    FDP_F(p.PRES, I, L) = FDP_F(p.PRES, I, L) + p.DTE * (PRv + ((SOURF - SOURFP) / p.DT));
-  } else {
-    FDP_F(p.TXX, I, L) = FDP_F(p.TXX, I, L) + p.DTE * TXXv;
-    FDP_F(p.TZZ, I, L) = FDP_F(p.TZZ, I, L) + p.DTE * TZZv;
-    FDP_F(p.PRES, I, L) = FDP_F(p.PRES, I, L) + p.DTE * PRv;
+
+  // ---- stores
+  if (do_xz) {
+    if (xz_z) p.PXZH[zi] = mz_new;
+    if (xz_lo || xz_hi) xz_m[xz_mi] = mx_new;
+    FDP_F(p.TXZ, I, L) = txz_new;
+  }
+  if (do_nn) {
+    if (zz_pml) { p.PZZH[zj] = me_new; p.OZZH[zj] = mq_new; }
+    if (xx_lo || xx_hi) { xx_me[xx_mi] = ne_new; xx_mq[xx_mi] = nq_new; }
+    FDP_F(p.TXX, I, L) = txx_new;
+    FDP_F(p.TZZ, I, L) = tzz_new;
+    FDP_F(p.PRES, I, L) = pr_new;
   }
 }
 
@@ -847,9 +922,14 @@ __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity(const __grid_constant__ Params
 // stencils everywhere, no source row), so the core kernels are the interior
 // branches of stress_cell / velocity_cell, same expressions in the same
 // order, for four cells at a time.
-// A frame unit: columns [x, y) (at most kBX), unit row z.
+// A frame unit: columns [x, y) (at most kBX), unit row z.  Resident CTAs
+// per SM the register allocation aims for: the cell code keeps all of a
+// cell's inputs in registers at once.
+#ifndef FDP_STRESS_FRAME_MIN_BLOCKS
+#define FDP_STRESS_FRAME_MIN_BLOCKS 3
+#endif
 template <class T, bool SI, int MODE>
-__global__ void __launch_bounds__(kBX * kBZ) k_stress_frame(const __grid_constant__ Params<T> p,
+__global__ void __launch_bounds__(kBX * kBZ, FDP_STRESS_FRAME_MIN_BLOCKS) k_stress_frame(const __grid_constant__ Params<T> p,
                                                             const int4* __restrict__ units, int it_off) {
   const int4 u = units[blockIdx.x];
   stress_unit<T, SI, MODE>(p, u.x, u.y, u.z, it_off);

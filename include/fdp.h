@@ -180,7 +180,9 @@ int fdp_synchronize(fdp_ctx* ctx);
 int fdp_get_stream(fdp_ctx* ctx, void** stream);
 
 /* Diagnostics: advances levels it_begin..it_end like fdp_run but without
- * graphs, with CUDA events around each part of a level, waits, and returns
+ * graphs, with CUDA events around each part of a level (all levels are
+ * enqueued before one wait, so the windows hold device time, not host
+ * launch latency), and returns
  * the summed device time in milliseconds in ms_out[0..4] and the number of
  * timed launches in launches_out[0..4]: {stress phase, velocity phase,
  * row 1 and receivers (and an attached learned edge), stress core kernel,
