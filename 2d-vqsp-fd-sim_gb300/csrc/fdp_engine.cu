@@ -272,7 +272,13 @@ template <class T, int MODE> bool launch_core_tma(fdp_ctx* c, const Params<T>& p
   return false;
 }
 
-template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
+// Launch modes of the frame/core split (launch_level_any): the stress frame
+// kernel finishes the previous level (row 1, velocity samples), and the
+// velocity frame kernel takes this level's stress samples (k_edge then
+// skips them).
+constexpr int kDeferPrev = 1, kFrameSamples = 2;
+
+template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<T>& p, int kind, int it_off, int mode) {
   const dim3 blk(fdp::kBX, fdp::kBZ, 1);
   const dim3 tblk(fdp::kTX, 4, 1);
   if (kind == 0 && c->use_tma) fdp::k_stress_tma<T, SI, MODE><<<tile_grid(c), tblk, 0, c->stream>>>(p, c->tma_vel, it_off);
@@ -298,8 +304,13 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
       cudaEventRecord(c->fork, c->stream);
       cudaStreamWaitEvent(c->side, c->fork, 0);
     }
-    if (kind == 0) fdp::k_stress_frame<T, SI, MODE><<<c->nframe_s, blk, 0, fs>>>(p, (const int4*)c->frame_s.p, it_off);
-    else fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v, blk, 0, fs>>>(p, (const int4*)c->frame_v.p);
+    const int mr_blocks = (c->mr + fdp::kBX * fdp::kBZ - 1) / (fdp::kBX * fdp::kBZ);
+    if (kind == 0)
+      fdp::k_stress_frame<T, SI, MODE><<<c->nframe_s + ((mode & kDeferPrev) ? mr_blocks : 0), blk, 0, fs>>>(
+          p, (const int4*)c->frame_s.p, c->nframe_s, it_off, (mode & kDeferPrev) ? 1 : 0);
+    else
+      fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v + ((mode & kFrameSamples) ? mr_blocks : 0), blk, 0, fs>>>(
+          p, (const int4*)c->frame_v.p, c->nframe_v, it_off);
     if (core) {
       if (c->core_ev[kind][0]) cudaEventRecord(c->core_ev[kind][0], c->stream);
       if (launch_core_tma<T, MODE>(c, p, kind)) {}
@@ -313,7 +324,8 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
   }
   else if (kind == 0) fdp::k_stress<T, SI, MODE><<<cell_grid(c, 0), blk, 0, c->stream>>>(p, it_off);
   else if (kind == 1) fdp::k_velocity<T, SI, MODE><<<cell_grid(c, 1), blk, 0, c->stream>>>(p, it_off);
-  else fdp::k_edge<T, SI><<<(edge_threads(c) + kBlockX - 1) / kBlockX, kBlockX, 0, c->stream>>>(p, it_off);
+  else fdp::k_edge<T, SI><<<(edge_threads(c) + kBlockX - 1) / kBlockX, kBlockX, 0, c->stream>>>(
+      p, it_off, (mode & kFrameSamples) ? 0 : 1);
   c->launches += 1;
 }
 
@@ -384,31 +396,48 @@ int plan_core(fdp_ctx* c) {
   return copy_sync(c, c->frame_v.p, uv.data(), uv.size() * sizeof(int), cudaMemcpyHostToDevice);
 }
 
-template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_off) {
+template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_off, int mode = 0) {
   const bool si = c->g.stress_imaging != 0;
   switch (c->medium_mode) {
     case fdp::M_TABLE:
-      si ? launch_kind<T, true, fdp::M_TABLE>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_TABLE>(c, p, kind, it_off);
+      si ? launch_kind<T, true, fdp::M_TABLE>(c, p, kind, it_off, mode)
+         : launch_kind<T, false, fdp::M_TABLE>(c, p, kind, it_off, mode);
       break;
     case fdp::M_BIOT:
-      si ? launch_kind<T, true, fdp::M_BIOT>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_BIOT>(c, p, kind, it_off);
+      si ? launch_kind<T, true, fdp::M_BIOT>(c, p, kind, it_off, mode)
+         : launch_kind<T, false, fdp::M_BIOT>(c, p, kind, it_off, mode);
       break;
     default:
-      si ? launch_kind<T, true, fdp::M_PLANES>(c, p, kind, it_off) : launch_kind<T, false, fdp::M_PLANES>(c, p, kind, it_off);
+      si ? launch_kind<T, true, fdp::M_PLANES>(c, p, kind, it_off, mode)
+         : launch_kind<T, false, fdp::M_PLANES>(c, p, kind, it_off, mode);
   }
 }
 
-template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_off) {
-  launch<T>(c, p, 0, it_off);
-  launch<T>(c, p, 1, it_off);
-  if (edge_threads(c) > 0) launch<T>(c, p, 2, it_off);
+// Whether a run of levels folds the row-1/receiver step of each level into
+// the next level's stress frame kernel (and its stress samples into the
+// level's velocity frame kernel), leaving one k_edge at the end of the run:
+// the frame/core split with no learned edge attached (that one reads row 1
+// after every level).
+bool defer_edge(const fdp_ctx* c) {
+  return c->use_core && !c->use_tma && !c->fused[0] && !c->fused[1] && !(c->edge && c->edge_attached) &&
+         edge_threads(c) > 0;
+}
+
+// Level it_off of a run of levels; `first` and `last` mark the run's ends.
+template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_off, bool first, bool last) {
+  const bool defer = defer_edge(c);
+  launch<T>(c, p, 0, it_off, defer && !first ? kDeferPrev : 0);
+  launch<T>(c, p, 1, it_off, defer ? kFrameSamples : 0);
+  if (edge_threads(c) > 0 && (!defer || last)) launch<T>(c, p, 2, it_off, defer ? kFrameSamples : 0);
   c->launches += fdp::edge_launch(c, it_off);  // learned absorbing edge, when attached
   return FDP_OK;
 }
 
-int level_launches(const fdp_ctx* c) {
+// Kernel launches of a run of n levels.
+long long run_launches(const fdp_ctx* c, int n) {
   const int cores = c->use_core ? (!c->fused[0] && c->cs[1] > c->cs[0]) + (!c->fused[1] && c->cv[1] > c->cv[0]) : 0;
-  return 2 + cores + (edge_threads(c) > 0 ? 1 : 0) + (c->edge && c->edge_attached ? 3 : 0);
+  const int edges = edge_threads(c) > 0 ? (defer_edge(c) ? 1 : n) : 0;
+  return (long long)n * (2 + cores + (c->edge && c->edge_attached ? 3 : 0)) + edges;
 }
 
 template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
@@ -429,7 +458,7 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
     cudaGraph_t gr = nullptr;
     CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const long long before = c->launches;
-    for (int k = 0; k < kChunk; ++k) launch_level_any<T>(c, p, k);
+    for (int k = 0; k < kChunk; ++k) launch_level_any<T>(c, p, k, k == 0, k == kChunk - 1);
     fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, kChunk);
     c->launches = before;  // capture only records; replays are counted below
     cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
@@ -438,14 +467,14 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) { c->graph = nullptr; return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
   }
-  const int per_level = level_launches(c);
+  const long long per_chunk = run_launches(c, kChunk);
   while (it_end - it + 1 >= kChunk && c->graph) {
     CK(c, cudaGraphLaunch(c->graph, c->stream));
-    c->launches += (long long)kChunk * per_level + 1;
+    c->launches += per_chunk + 1;
     it += kChunk;
   }
   int k = 0;
-  for (; it <= it_end; ++it, ++k) launch_level_any<T>(c, p, k);
+  for (; it <= it_end; ++it, ++k) launch_level_any<T>(c, p, k, k == 0, it == it_end);
   if (k > 0) {
     fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, k);
     c->launches += 1;

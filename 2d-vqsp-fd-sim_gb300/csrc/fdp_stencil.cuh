@@ -34,6 +34,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace fdp {
 
 // Derived material coefficients (one column per k, indexed by JM).
@@ -331,6 +333,18 @@ template <class T> struct GlobalRd {
   }
 };
 
+// The same through the coherent path, for cells whose inputs the running
+// kernel itself writes first (the stress-imaging row 1 written at the start
+// of a stress phase).
+template <class T> struct GlobalRdC {
+  const T* f[4];
+  long long pitch;
+  int PMLL;
+  __device__ __forceinline__ T operator()(int k, int I, int L) const {
+    return f[k][(long long)L * pitch + (I - PMLL)];
+  }
+};
+
 // ---------------------------------------------------------------------------
 // strain_uw_xx.F90:51-94 / strain_q_xx.F90:50-91 for one cell
 template <class T, class R>
@@ -572,17 +586,18 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
 // per block, the frame and batched kernels the units of their lists.
 // stress_unit's cells of thread (tx, ty) of the unit, without the
 // stress-imaging mirror rows.
-template <class T, bool SI, int MODE>
+template <class T, bool SI, int MODE, bool COH = false>
 __device__ __forceinline__ void stress_unit_cells(const Params<T>& p, int I0, int I1, int by, int it_off, int tx,
                                                   int ty) {
   const int I = I0 + tx;
   const int L0 = (by * kBZ + ty) * kRZS;  // rows L0 .. L0+kRZS-1
   const bool core = p.cs_x1 > p.cs_x0;  // the core kernel updates the core cells
-  if (!core && I1 > p.PMLXH && stress_fast_rows(p, I, L0)) {
+  if (!COH && !core && I1 > p.PMLXH && stress_fast_rows(p, I, L0)) {
     stress_interior_rows<T, MODE>(p, I, L0);
   } else if (I < I1) {
     const int it = *p.it_base + it_off;
-    const GlobalRd<T> rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
+    using Rd = typename std::conditional<COH, GlobalRdC<T>, GlobalRd<T>>::type;
+    const Rd rd{{p.UM, p.WM, p.QX, p.QZ}, p.pitch, p.PMLL};
     const bool incol = I >= p.cs_x0 && I < p.cs_x1;
 #pragma unroll 1
     for (int L = L0; L < L0 + kRZS; ++L)
@@ -604,9 +619,9 @@ __device__ __forceinline__ void stress_mirror(const Params<T>& p, int I) {
   FDP_F(p.TXZ, I, 2) = T(0);
 }
 
-template <class T, bool SI, int MODE>
+template <class T, bool SI, int MODE, bool COH = false>
 __device__ __forceinline__ void stress_unit(const Params<T>& p, int I0, int I1, int by, int it_off) {
-  stress_unit_cells<T, SI, MODE>(p, I0, I1, by, it_off, (int)threadIdx.x, (int)threadIdx.y);
+  stress_unit_cells<T, SI, MODE, COH>(p, I0, I1, by, it_off, (int)threadIdx.x, (int)threadIdx.y);
   if (SI && by == 0) {
     __syncthreads();  // rows 2..4 of this unit are final
     if (I0 + (int)threadIdx.x < I1 && threadIdx.y == 0) stress_mirror(p, I0 + (int)threadIdx.x);
@@ -652,23 +667,23 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
       if (I <= 3 || I >= MX1) {
         int xi, mi;
         const T *xa_, *xd_, *xb_, *xc_;
-        T *G, *H, *R, *S;
+        T *G, *H, *Rm, *S;
         if (I <= 3) {
           xi = (3 - I) + L * (TPML + 2); mi = (I - p.PMLL) + L * (TPML + 3);
           xa_ = p.ODA2_XL; xd_ = p.ODD2_XL; xb_ = p.ODB2_XL; xc_ = p.ODC2_XL;
-          G = p.GXXL; H = p.HXXL; R = p.RXXL; S = p.SXXL;
+          G = p.GXXL; H = p.HXXL; Rm = p.RXXL; S = p.SXXL;
         } else {
           xi = (I - MX1) + L * (TPML + 2); mi = (I - (MX - 1)) + L * (TPML + 2);
           xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
-          G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
+          G = p.GXXH; H = p.HXXH; Rm = p.RXXH; S = p.SXXH;
         }
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
-        const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
+        const T g = G[mi], h = H[mi], r = Rm[mi], s = S[mi];
         qx = E * qx0 - R1 * (xa * (xd * DXXXA + g)) - R1 * (za * (zd * DXZZA + gz)) - R2 * (xa * (xd * PXXXA + h));
         u = u0 + Cu * qx0 + R1u * (xa * (xd * DXXXA + r) + za * (zd * DXZZA + rz)) + R3u * (xa * (xd * PXXXA + s));
         G[mi] = xb * g + xc * DXXXA;
         H[mi] = xb * h + xc * PXXXA;
-        R[mi] = xb * r + xc * DXXXA;
+        Rm[mi] = xb * r + xc * DXXXA;
         S[mi] = xb * s + xc * PXXXA;
       } else {
         qx = E * qx0 - R1 * (za * (zd * DXZZA + gz) + DXXXA) - R2 * (rd(3, I, L) - rd(3, I - 1, L));
@@ -682,26 +697,26 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
         // inh_qx_2nd.F90 / inh_v_u_2nd.F90
         int xi, mi;
         const T *xa_, *xd_, *xb_, *xc_;
-        T *G, *H, *R, *S;
+        T *G, *H, *Rm, *S;
         if (I <= 3) {
           xi = (3 - I) + L * (TPML + 2); mi = (I - p.PMLL) + L * (TPML + 3);
           xa_ = p.ODA2_XL; xd_ = p.ODD2_XL; xb_ = p.ODB2_XL; xc_ = p.ODC2_XL;
-          G = p.GXXL; H = p.HXXL; R = p.RXXL; S = p.SXXL;
+          G = p.GXXL; H = p.HXXL; Rm = p.RXXL; S = p.SXXL;
         } else {
           xi = (I - MX1) + L * (TPML + 2); mi = (I - (MX - 1)) + L * (TPML + 2);
           xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
-          G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
+          G = p.GXXH; H = p.HXXH; Rm = p.RXXH; S = p.SXXH;
         }
         const T DXXXA = rd(0, I, L) - rd(0, I - 1, L);
         const T PXXXA = rd(3, I, L) - rd(3, I - 1, L);
         const T txz1 = rd(2, I, L + 1), txz0 = rd(2, I, L);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
-        const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
+        const T g = G[mi], h = H[mi], r = Rm[mi], s = S[mi];
         qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1 - txz0) - R2 * (xa * (xd * PXXXA + h));
         u = u0 + Cu * qx0 + R1u * (xa * (xd * DXXXA + r) + txz1 - txz0) + R3u * (xa * (xd * PXXXA + s));
         G[mi] = xb * g + xc * DXXXA;
         H[mi] = xb * h + xc * PXXXA;
-        R[mi] = xb * r + xc * DXXXA;
+        Rm[mi] = xb * r + xc * DXXXA;
         S[mi] = xb * s + xc * PXXXA;
       } else {
         // inh_qx_int.F90:40-54 / inh_v_uv_int.F90:41-56
@@ -717,26 +732,26 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
       if (I <= 3 || I >= MX1) {
         int xi, mi;
         const T *xa_, *xd_, *xb_, *xc_;
-        T *G, *H, *R, *S;
+        T *G, *H, *Rm, *S;
         if (I <= 3) {
           xi = (3 - I); mi = (I - p.PMLL);
           xa_ = p.ODA2_XL; xd_ = p.ODD2_XL; xb_ = p.ODB2_XL; xc_ = p.ODC2_XL;
-          G = p.GXXL; H = p.HXXL; R = p.RXXL; S = p.SXXL;
+          G = p.GXXL; H = p.HXXL; Rm = p.RXXL; S = p.SXXL;
         } else {
           xi = (I - MX1); mi = (I - (MX - 1));
           xa_ = p.ODA2_XH; xd_ = p.ODD2_XH; xb_ = p.ODB2_XH; xc_ = p.ODC2_XH;
-          G = p.GXXH; H = p.HXXH; R = p.RXXH; S = p.SXXH;
+          G = p.GXXH; H = p.HXXH; Rm = p.RXXH; S = p.SXXH;
         }
         const T DXXXA = rd(0, I, 0) - rd(0, I - 1, 0);
         const T PXXXA = rd(3, I, 0) - rd(3, I - 1, 0);
         const T txz1 = rd(2, I, 1);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
-        const T g = G[mi], h = H[mi], r = R[mi], s = S[mi];
+        const T g = G[mi], h = H[mi], r = Rm[mi], s = S[mi];
         qx = E * qx0 - R1 * (xa * (xd * DXXXA + g) + txz1) - R2 * (xa * (xd * PXXXA + h));
         u = u0 + Cu * qx0 + R1u * (xa * (xd * DXXXA + r) + txz1) + R3u * (xa * (xd * PXXXA + s));
         G[mi] = xb * g + xc * DXXXA;
         H[mi] = xb * h + xc * PXXXA;
-        R[mi] = xb * r + xc * DXXXA;
+        Rm[mi] = xb * r + xc * DXXXA;
         S[mi] = xb * s + xc * PXXXA;
       } else {
         const T X = A * (rd(0, I + 1, 0) - rd(0, I - 2, 0)) + B * (rd(0, I, 0) - rd(0, I - 1, 0))
@@ -770,20 +785,20 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
       if (I <= 2 || I >= MX1) {
         int xi, mi;
         const T *xa_, *xd_, *xb_, *xc_;
-        T *G, *R;
+        T *G, *Rm;
         if (I <= 2) {
           xi = (2 - I) + L * (TPML + 1); mi = (I - p.PMLL) + L * (TPML + 2);
-          xa_ = p.ODA_XL; xd_ = p.ODD_XL; xb_ = p.ODB_XL; xc_ = p.ODC_XL; G = p.GZXL; R = p.RZXL;
+          xa_ = p.ODA_XL; xd_ = p.ODD_XL; xb_ = p.ODB_XL; xc_ = p.ODC_XL; G = p.GZXL; Rm = p.RZXL;
         } else {
           xi = (I - MX1) + L * (TPML + 1); mi = (I - (MX - 1)) + L * (TPML + 2);
-          xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; R = p.RZXH;
+          xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; Rm = p.RZXH;
         }
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
-        const T g = G[mi], r = R[mi];
+        const T g = G[mi], r = Rm[mi];
         qz = E * qz0 - R1 * (za * (zd * DZZZA + gz)) - R1 * (xa * (xd * DXZXA + g)) - R2 * (za * (zd * PZZZA + hz));
         w = w0 + Cw * qz0 + R1w * (za * (zd * DZZZA + rz) + xa * (xd * DXZXA + r)) + R3w * (za * (zd * PZZZA + sz));
         G[mi] = xb * g + xc * DXZXA;
-        R[mi] = xb * r + xc * DXZXA;
+        Rm[mi] = xb * r + xc * DXZXA;
       } else {
         qz = E * qz0 - R1 * (za * (zd * DZZZA + gz) + DXZXA) - R2 * (za * (zd * PZZZA + hz));
         w = w0 + Cw * qz0 + R1w * (za * (zd * DZZZA + rz) + DXZXA) + R3w * (za * (zd * PZZZA + sz));
@@ -797,23 +812,23 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
         // inh_qz_2nd.F90 / inh_v_w_2nd.F90 (also row 1 without stress imaging)
         int xi, mi;
         const T *xa_, *xd_, *xb_, *xc_;
-        T *G, *R;
+        T *G, *Rm;
         if (I <= 2) {
           xi = (2 - I) + L * (TPML + 1); mi = (I - p.PMLL) + L * (TPML + 2);
-          xa_ = p.ODA_XL; xd_ = p.ODD_XL; xb_ = p.ODB_XL; xc_ = p.ODC_XL; G = p.GZXL; R = p.RZXL;
+          xa_ = p.ODA_XL; xd_ = p.ODD_XL; xb_ = p.ODB_XL; xc_ = p.ODC_XL; G = p.GZXL; Rm = p.RZXL;
         } else {
           xi = (I - MX1) + L * (TPML + 1); mi = (I - (MX - 1)) + L * (TPML + 2);
-          xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; R = p.RZXH;
+          xa_ = p.ODA_XH; xd_ = p.ODD_XH; xb_ = p.ODB_XH; xc_ = p.ODC_XH; G = p.GZXH; Rm = p.RZXH;
         }
         const T DXZXA = rd(2, I + 1, L) - rd(2, I, L);
         const T dzz = rd(1, I, L) - rd(1, I, L - 1);
         const T dp = rd(3, I, L) - rd(3, I, L - 1);
         const T xa = xa_[xi], xd = xd_[xi], xb = xb_[xi], xc = xc_[xi];
-        const T g = G[mi], r = R[mi];
+        const T g = G[mi], r = Rm[mi];
         qz = E * qz0 - R1 * (dzz + xa * (xd * DXZXA + g)) - R2 * dp;
         w = w0 + Cw * qz0 + R1w * (dzz + xa * (xd * DXZXA + r)) + R3w * dp;
         G[mi] = xb * g + xc * DXZXA;
-        R[mi] = xb * r + xc * DXZXA;
+        Rm[mi] = xb * r + xc * DXZXA;
       } else if (SI || L >= 2) {
         // inh_qz_int.F90:41-55 / inh_v_w_int.F90:43-58
         const T X = A * (rd(1, I, L + 1) - rd(1, I, L - 2) + rd(2, I + 2, L) - rd(2, I - 1, L))
@@ -928,11 +943,36 @@ __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity(const __grid_constant__ Params
 #ifndef FDP_STRESS_FRAME_MIN_BLOCKS
 #define FDP_STRESS_FRAME_MIN_BLOCKS 3
 #endif
+template <class T, bool SI>
+__device__ __forceinline__ void edge_thread(const Params<T>& p, int g, int it_off);
+template <class T>
+__device__ __forceinline__ void stress_sample_thread(const Params<T>& p, int g, int it_off);
+
+// Blocks 0..n-1 run the n frame units.  With edge_prev set, the kernel also
+// finishes the previous level: the top units first write the
+// stress-imaging row 1 of their columns from rows 2 and 3 (which the
+// previous velocity phase left final, and which this phase's stresses at
+// rows 2 and 3 read), and blocks n.. take the previous level's velocity
+// samples of the receivers (velocities stay unchanged through a stress
+// phase; row-1 samples are recomputed, not read).
 template <class T, bool SI, int MODE>
 __global__ void __launch_bounds__(kBX * kBZ, FDP_STRESS_FRAME_MIN_BLOCKS) k_stress_frame(const __grid_constant__ Params<T> p,
-                                                            const int4* __restrict__ units, int it_off) {
-  const int4 u = units[blockIdx.x];
-  stress_unit<T, SI, MODE>(p, u.x, u.y, u.z, it_off);
+                                                            const int4* __restrict__ units, int n, int it_off,
+                                                            int edge_prev) {
+  const int b = (int)blockIdx.x;
+  const int tid = (int)(threadIdx.y * kBX + threadIdx.x);
+  if (b >= n) {
+    edge_thread<T, SI>(p, (SI ? p.NX : 0) + (b - n) * kBX * kBZ + tid, it_off - 1);
+    return;
+  }
+  const int4 u = units[b];
+  if (SI && edge_prev && u.z == 0) {
+    if (threadIdx.y == 0 && u.x + (int)threadIdx.x < u.y) edge_thread<T, SI>(p, u.x + (int)threadIdx.x - p.PMLL, it_off - 1);
+    __syncthreads();  // row 1 of these columns is final before rows 2 and 3 read it
+    stress_unit<T, SI, MODE, true>(p, u.x, u.y, u.z, it_off);
+  } else {
+    stress_unit<T, SI, MODE>(p, u.x, u.y, u.z, it_off);
+  }
 }
 
 // Velocity frame cells up to row PMLZH-3, one row per thread: columns
@@ -993,10 +1033,18 @@ __device__ __forceinline__ void velocity_frame_unit(const Params<T>& p, const in
   else velocity_row_unit<T, SI, MODE>(p, u.x, u.y, u.z, (int)threadIdx.x, (int)threadIdx.y);
 }
 
+// Blocks 0..n-1 run the n frame units; blocks n.. take this level's
+// stress samples of the receivers (the velocity phase leaves the stresses
+// alone).
 template <class T, bool SI, int MODE>
 __global__ void __launch_bounds__(kBX * kBZ, 4) k_velocity_frame(const __grid_constant__ Params<T> p,
-                                                              const int4* __restrict__ units) {
-  velocity_frame_unit<T, SI, MODE>(p, units[blockIdx.x]);
+                                                              const int4* __restrict__ units, int n, int it_off) {
+  const int b = (int)blockIdx.x;
+  if (b >= n) {
+    stress_sample_thread<T>(p, (b - n) * kBX * kBZ + (int)(threadIdx.y * kBX + threadIdx.x), it_off);
+    return;
+  }
+  velocity_frame_unit<T, SI, MODE>(p, units[b]);
 }
 
 template <class T> struct V4 { T v[4]; };
@@ -1295,11 +1343,12 @@ __device__ __forceinline__ void stress_sample_thread(const Params<T>& p, int g, 
   out[5] = in ? -FDP_F(p.TXX, IZ, LX) : T(0);
 }
 
+// samples = 0 leaves the stress samples to the velocity frame kernel.
 template <class T, bool SI>
-__global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> p, int it_off) {
+__global__ void __launch_bounds__(128) k_edge(const __grid_constant__ Params<T> p, int it_off, int samples) {
   const int g = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   edge_thread<T, SI>(p, g, it_off);
-  stress_sample_thread<T>(p, g - (SI ? p.NX : 0), it_off);
+  if (samples) stress_sample_thread<T>(p, g - (SI ? p.NX : 0), it_off);
 }
 
 // ---------------------------------------------------------------------------
