@@ -1227,9 +1227,11 @@ struct fdp_batch {
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   int m = 0, waves = 0;          // units per item; persistent CTAs per resident slot (0: one CTA per item)
+                                 // m = FDP_BATCH_SHOTS: every shot's own kernels on its own stream
   bool tuned = false;            // shape fixed (by the caller or by tuning)
   int sms = 0;
   cudaGraphExec_t graph = nullptr;
+  std::vector<cudaEvent_t> shot_ev;  // per shot: the end of its levels, joined into `stream`
   long long launches = 0;
   std::string err;
 };
@@ -1414,7 +1416,76 @@ int batch_set_shape(fdp_batch* b, int m, int waves) {
   if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
   b->m = m;
   b->waves = waves;
-  return batch_queue(b);
+  return m == FDP_BATCH_SHOTS ? FDP_OK : batch_queue(b);
+}
+
+// The shots mode: n levels of every shot with the shot's own kernels (the
+// level sequence fdp_run launches: frame/core split, folded row-1 and
+// receiver step, one k_edge at the end), each shot on its own stream,
+// forked from and joined back to the batch stream, so that the shots run
+// side by side.  Each shot's level counter starts where the batch set it
+// and advances by n at the end.
+template <class T> void shots_levels(fdp_batch* b, int n) {
+  cudaEventRecord(b->fork, b->stream);
+  for (size_t s = 0; s < b->shots.size(); ++s) {
+    fdp_ctx* c = b->shots[s];
+    Params<T> p;
+    fill_params<T>(c, p);
+    cudaStreamWaitEvent(c->stream, b->fork, 0);
+    for (int k = 0; k < n; ++k) launch_level_any<T>(c, p, k, k == 0, k == n - 1);
+    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
+    cudaEventRecord(b->shot_ev[s], c->stream);
+    cudaStreamWaitEvent(b->stream, b->shot_ev[s], 0);
+  }
+}
+
+long long shots_launches(const fdp_batch* b, int n) {
+  long long total = 0;
+  for (const fdp_ctx* c : b->shots) total += run_launches(c, n) + 1;
+  return total;
+}
+
+// Sets every shot's level counter to `it` (on the batch stream).
+void shots_set_base(fdp_batch* b, int it) {
+  for (fdp_ctx* c : b->shots) fdp::k_set_base<<<1, 1, 0, b->stream>>>((int*)c->itbase.p, it);
+  b->launches += (long long)b->shots.size();
+}
+
+// The shots mode's graph of kChunk levels of every shot.
+template <class T> int shots_graph(fdp_batch* b) {
+  if (b->graph) return FDP_OK;
+  cudaGraph_t gr = nullptr;
+  BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  std::vector<long long> before;
+  for (const fdp_ctx* c : b->shots) before.push_back(c->launches);
+  shots_levels<T>(b, kChunk);
+  for (size_t s = 0; s < b->shots.size(); ++s) b->shots[s]->launches = before[s];  // capture only records
+  cudaError_t e = cudaStreamEndCapture(b->stream, &gr);
+  if (e != cudaSuccess) return bfail(b, FDP_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->graph, gr, 0);
+  cudaGraphDestroy(gr);
+  if (e != cudaSuccess) { b->graph = nullptr; return bfail(b, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+  return FDP_OK;
+}
+
+// Runs levels [it, it_end] in the shots mode: graph replays of kChunk
+// levels, then the rest launched directly.
+template <class T> int shots_run(fdp_batch* b, int it, int it_end) {
+  shots_set_base(b, it);
+  int rc;
+  if (it_end - it + 1 >= kChunk && (rc = shots_graph<T>(b)) != FDP_OK) return rc;
+  while (it_end - it + 1 >= kChunk) {
+    BCK(b, cudaGraphLaunch(b->graph, b->stream));
+    b->launches += shots_launches(b, kChunk);
+    it += kChunk;
+  }
+  if (it <= it_end) {
+    const long long before = b->launches;
+    shots_levels<T>(b, it_end - it + 1);
+    b->launches = before + shots_launches(b, it_end - it + 1);
+  }
+  BCK(b, cudaGetLastError());
+  return FDP_OK;
 }
 
 // Shape tuning on real levels: every candidate computes the same values bit
@@ -1447,10 +1518,30 @@ template <class T> int batch_tune(fdp_batch* b, int it_begin, int it_end, int* u
     }
     if (rc != FDP_OK) break;
   }
+  // the shots mode, timed over one graph replay of kChunk levels when the
+  // run still has them (its direct launches are host-bound)
+  if (rc == FDP_OK && it_end - it + 1 >= kChunk) {
+    // the graph is built before the clock starts: the device would
+    // otherwise wait for its capture and instantiation
+    if ((rc = batch_set_shape(b, FDP_BATCH_SHOTS, 0)) == FDP_OK && (rc = shots_graph<T>(b)) == FDP_OK) {
+      cudaEventRecord(e0, b->stream);
+      rc = shots_run<T>(b, it, it + kChunk - 1);
+      cudaEventRecord(e1, b->stream);
+      float ms = 0.f;
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (rc == FDP_OK && e != cudaSuccess) rc = bfail(b, FDP_ERR_CUDA, "shape tuning: %s", cudaGetErrorString(e));
+      if (rc == FDP_OK) {
+        if (ms * per / kChunk < best) { best = ms * per / kChunk; bm = FDP_BATCH_SHOTS; bw = 0; }
+        it += kChunk;
+      }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != FDP_OK) return rc;
   *used = it - it_begin;
+  if (bm == b->m && bw == b->waves) return FDP_OK;  // keeps the shots mode's graph
   return batch_set_shape(b, bm, bw);
 }
 
@@ -1463,6 +1554,7 @@ template <class T> int batch_run_t(fdp_batch* b, int it_begin, int it_end) {
     b->tuned = used > 0;
   }
   if (it > it_end) return FDP_OK;
+  if (b->m == FDP_BATCH_SHOTS) return shots_run<T>(b, it, it_end);
   fdp::k_set_base<<<1, 1, 0, b->stream>>>((int*)b->itbase.p, it);
   b->launches += 1;
   if (it_end - it + 1 >= kChunk && !b->graph) {
@@ -1537,10 +1629,14 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
   // every cell); the frame kernels run on a side stream beside the cores
   b->framed = true;
   for (const fdp_ctx* c : b->shots) b->framed = b->framed && c->use_core;
+  e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+  b->shot_ev.assign(b->shots.size(), nullptr);
+  for (auto& ev : b->shot_ev)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return bail(bfail(b, FDP_ERR_CUDA, "batch events: %s", cudaGetErrorString(e)));
   if (b->framed) {
     e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
     if (e != cudaSuccess) return bail(bfail(b, FDP_ERR_CUDA, "batch side stream: %s", cudaGetErrorString(e)));
     if ((rc = batch_units(b)) != FDP_OK) return bail(rc);
   }
@@ -1588,8 +1684,9 @@ int fdp_batch_set_shape(fdp_batch* b, int32_t units_per_item, int32_t waves) {
     b->tuned = false;
     return FDP_OK;
   }
-  if (units_per_item < 1 || units_per_item > 64 || waves < 0 || waves > 64)
-    return bfail(b, FDP_ERR_ARG, "units per item must be 1..64 and waves 0..64");
+  if (units_per_item == FDP_BATCH_SHOTS) waves = 0;
+  else if (units_per_item < 1 || units_per_item > 64 || waves < 0 || waves > 64)
+    return bfail(b, FDP_ERR_ARG, "units per item must be 1..64 (or FDP_BATCH_SHOTS) and waves 0..64");
   BCK(b, cudaSetDevice(b->device));
   BCK(b, cudaStreamSynchronize(b->stream));
   b->tuned = true;
@@ -1646,6 +1743,7 @@ void fdp_batch_destroy(fdp_batch* b) {
   for (DevArr* a : {&b->params, &b->first, &b->itbase, &b->units, &b->ubase}) if (a->p) cudaFree(a->p);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
+  for (cudaEvent_t ev : b->shot_ev) if (ev) cudaEventDestroy(ev);
   if (b->side) cudaStreamDestroy(b->side);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;

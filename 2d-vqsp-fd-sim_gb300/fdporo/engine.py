@@ -235,7 +235,8 @@ class Batch:
         self._check(self.lib.fdp_batch_synchronize(self._b))
 
     def set_shape(self, units_per_item: int, waves: int) -> None:
-        """Fixes the tile shape (``units_per_item = 0``: tune on the next run)."""
+        """Fixes the tile shape (``units_per_item = 0``: tune on the next run;
+        ``native.FDP_BATCH_SHOTS``: every shot's own kernels side by side)."""
         self._check(self.lib.fdp_batch_set_shape(self._b, units_per_item, waves))
 
     def shape(self) -> tuple[int, int]:

@@ -17,6 +17,7 @@ FDP_ERR_ALLOC = -3
 FDP_ERR_STATE = -4
 FDP_ERR_UNSUPPORTED = -5
 FDP_ERR_DEVICE = -6
+FDP_BATCH_SHOTS = -1
 FDP_F32 = 4
 FDP_F64 = 8
 

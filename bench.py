@@ -388,7 +388,9 @@ def run_batch(args) -> None:
             cells.append(inp.cells)
     setup_s = time.perf_counter() - t0
     total = sum(cells)
-    K, W = args.steps, max(args.warmup, 20)  # the batch tunes its shape on its first 18 levels
+    # the batch tunes its shape on its first 50 levels (9 queue shapes x 2,
+    # then one 32-level graph of the shots mode)
+    K, W = args.steps, max(args.warmup, 50)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     b = Batch(engines)
@@ -481,7 +483,9 @@ def run_large(args) -> None:
     ab = algorithmic_bytes(inp, 4, medium)
     level_bytes = n * (ab["stress"] + ab["velocity"])
     cells = n * inp.cells
-    K, W = args.steps, max(args.warmup, 20)  # the batch tunes its shape on its first 18 levels
+    # the batch tunes its shape on its first 50 levels (9 queue shapes x 2,
+    # then one 32-level graph of the shots mode)
+    K, W = args.steps, max(args.warmup, 50)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     b = Batch(engines)
     ext = torch.cuda.ExternalStream(b.stream(), device=dev)

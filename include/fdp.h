@@ -275,13 +275,19 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out);
 /* Advances every shot over levels it_begin..it_end (within every shot's
  * MT2).  Asynchronous.  Unless a shape was set, the first run tunes the
  * tile shape on its own first levels (each candidate computes the same
- * values, so no level is wasted or altered) and keeps the fastest. */
+ * values, so no level is wasted or altered) and keeps the fastest.  While
+ * a batch runs, its shots' own streams carry work (the shots mode). */
 int fdp_batch_run(fdp_batch* b, int32_t it_begin, int32_t it_end);
 
 /* Tile shape of the work queue: units_per_item vertically adjacent units
  * (32 columns by 8 or 32 rows each) per item, and `waves` persistent CTAs
  * per resident CTA slot of the GPU (0: one CTA per item).  units_per_item
- * = 0 asks the next run to tune again. */
+ * = FDP_BATCH_SHOTS runs instead every shot's own kernels (those fdp_run
+ * launches) on the shot's own stream, all shots side by side in one CUDA
+ * graph per 32 levels.  units_per_item = 0 asks the next run to tune again
+ * (the tuner times the nine queue shapes on two levels each and, when the
+ * run has 32 more levels, the shots mode on one graph of them). */
+#define FDP_BATCH_SHOTS (-1)
 int fdp_batch_set_shape(fdp_batch* b, int32_t units_per_item, int32_t waves);
 int fdp_batch_get_shape(fdp_batch* b, int32_t* units_per_item, int32_t* waves);
 
