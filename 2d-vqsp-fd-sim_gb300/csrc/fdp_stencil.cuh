@@ -938,8 +938,8 @@ __global__ void FDP_VELOCITY_BOUNDS(T) k_velocity(const __grid_constant__ Params
 // branches of stress_cell / velocity_cell, same expressions in the same
 // order, for four cells at a time.
 // A frame unit: columns [x, y) (at most kBX), unit row z.  Resident CTAs
-// per SM the register allocation aims for: the cell code keeps all of a
-// cell's inputs in registers at once.
+// per SM the register allocation aims for (FP32; two in FP64): the cell
+// code keeps all of a cell's inputs in registers at once.
 #ifndef FDP_STRESS_FRAME_MIN_BLOCKS
 #define FDP_STRESS_FRAME_MIN_BLOCKS 3
 #endif
@@ -956,7 +956,7 @@ __device__ __forceinline__ void stress_sample_thread(const Params<T>& p, int g, 
 // samples of the receivers (velocities stay unchanged through a stress
 // phase; row-1 samples are recomputed, not read).
 template <class T, bool SI, int MODE>
-__global__ void __launch_bounds__(kBX * kBZ, FDP_STRESS_FRAME_MIN_BLOCKS) k_stress_frame(const __grid_constant__ Params<T> p,
+__global__ void __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? FDP_STRESS_FRAME_MIN_BLOCKS : 2) k_stress_frame(const __grid_constant__ Params<T> p,
                                                             const int4* __restrict__ units, int n, int it_off,
                                                             int edge_prev) {
   const int b = (int)blockIdx.x;
@@ -1037,7 +1037,7 @@ __device__ __forceinline__ void velocity_frame_unit(const Params<T>& p, const in
 // stress samples of the receivers (the velocity phase leaves the stresses
 // alone).
 template <class T, bool SI, int MODE>
-__global__ void __launch_bounds__(kBX * kBZ, 4) k_velocity_frame(const __grid_constant__ Params<T> p,
+__global__ void __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? 4 : 2) k_velocity_frame(const __grid_constant__ Params<T> p,
                                                               const int4* __restrict__ units, int n, int it_off) {
   const int b = (int)blockIdx.x;
   if (b >= n) {
