@@ -43,6 +43,7 @@ struct fdp_ctx {
   // device memory
   DevArr fields[8];
   DevArr jm, coef, planes, aux, prof[24], mem[27], ab, hist, stf, rec, raw, itbase, errbuf;
+  DevArr diag_flag;  // fdp_diag_wait_timeout: a word nothing sets
   // TMA descriptors of the input fields of each phase; use_tma selects the
   // TMA-staged kernels (FDP_KERNEL_VARIANT=tma; the global-load kernels are
   // the default)

@@ -183,7 +183,12 @@ int device_status(fdp_ctx* c) {
   int v = 0;
   CK(c, cudaMemcpyAsync(&v, c->errbuf.p, sizeof v, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
-  if (v) return fail(c, FDP_ERR_DEVICE, "a kernel gave up waiting for its tile copy (status %d)", v);
+  if (v) {
+    // reported once: the word is cleared, and the context stays usable
+    CK(c, cudaMemsetAsync(c->errbuf.p, 0, sizeof v, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return fail(c, FDP_ERR_DEVICE, "a kernel gave up waiting (status %d)", v);
+  }
   return FDP_OK;
 }
 
@@ -1071,6 +1076,16 @@ int fdp_synchronize(fdp_ctx* c) {
   return device_status(c);
 }
 
+int fdp_diag_wait_timeout(fdp_ctx* c, int32_t polls) {
+  if (!c || polls < 1 || polls > (1 << 20)) return fail(c, FDP_ERR_ARG, "need a context and 1..2^20 polls");
+  int rc;
+  if (!c->diag_flag.p && (rc = dev_alloc(c, c->diag_flag, sizeof(int))) != FDP_OK) return rc;
+  fdp::k_wait_flag<<<1, 1, 0, c->stream>>>((const int*)c->diag_flag.p, (unsigned)polls, (int*)c->errbuf.p);
+  c->launches += 1;
+  CK(c, cudaGetLastError());
+  return FDP_OK;
+}
+
 int64_t fdp_kernel_launches(fdp_ctx* c) { return c ? c->launches : 0; }
 
 int fdp_medium_info(fdp_ctx* c, int32_t* mode, int32_t* planes_stress, int32_t* planes_velocity) {
@@ -1183,7 +1198,7 @@ void fdp_destroy(fdp_ctx* c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
   unshare_medium(c);
   DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase,
-                   &c->errbuf, &c->frame_s, &c->frame_v};
+                   &c->errbuf, &c->frame_s, &c->frame_v, &c->diag_flag};
   for (auto* a : all) if (a->p) cudaFree(a->p);
   for (auto& a : c->fields) if (a.p) cudaFree(a.p);
   for (auto& a : c->prof) if (a.p) cudaFree(a.p);

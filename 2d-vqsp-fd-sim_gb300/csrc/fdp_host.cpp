@@ -239,6 +239,16 @@ template <class T> int run(const Opts& o) {
     sf.push_back(D + "REC_STRESS_" + std::to_string(j) + ".asc");
   }
   for (int it0 = 1; it0 <= MT2;) {
+    // time_loop.F90:79-86: a file STOP in the job directory ends the run
+    // before level it0 (looked for before every chunk of levels); the level
+    // is written into it, list-directed, and the files written so far stay
+    if (exists(D + "STOP")) {
+      if (FILE* sf = std::fopen((D + "STOP").c_str(), "w")) {
+        std::fprintf(sf, "%12d\n", it0);
+        std::fclose(sf);
+      }
+      break;
+    }
     int it1 = std::min(MT2, it0 + chunk - 1);
     if (SNV) it1 = std::min(it1, (it0 / IPAS2 + 1) * IPAS2);
     ck(fdp_run(ctx, it0, it1), "fdp_run");

@@ -1526,6 +1526,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
+// The failure path of the bounded waits, on its own: polls a word that
+// nothing sets, `polls` times about 100 ns apart, then records the expired
+// wait in the status word the host reads, as a kernel whose tile copy does
+// not arrive does.
+static __global__ void k_wait_flag(const int* flag, unsigned polls, int* err) {
+  for (unsigned i = 0; i < polls; ++i) {
+    if (*(const volatile int*)flag) return;
+    __nanosleep(100);
+  }
+  atomicOr(err, 4);
+}
+
 // Waits for the tile's copies with an iteration limit (far above any real
 // latency); false means the copies did not complete in time.
 constexpr unsigned kWaitLimit = 1u << 22;

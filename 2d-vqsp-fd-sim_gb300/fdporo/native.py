@@ -67,6 +67,7 @@ SIGNATURES = {
     "fdp_create": (C.c_int, [C.POINTER(fdp_grid), C.POINTER(_VP)]),
     "fdp_set_medium": (C.c_int, [_VP, _PI32, _I32, _I32, _I32, _VP]),
     "fdp_share_medium": (C.c_int, [_VP, _VP]),
+    "fdp_diag_wait_timeout": (C.c_int, [_VP, _I32]),
     "fdp_set_pml": (C.c_int, [_VP, C.POINTER(_VP)]),
     "fdp_set_bottom_nr": (C.c_int, [_VP, _VP]),
     "fdp_set_source": (C.c_int, [_VP, _VP, _I32]),

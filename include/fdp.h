@@ -172,6 +172,14 @@ int fdp_field_bounds(fdp_ctx* ctx, int32_t id, int32_t* bounds4);
 int fdp_get_field(fdp_ctx* ctx, int32_t id, void* host);
 int fdp_set_field(fdp_ctx* ctx, int32_t id, const void* host);
 
+/* Diagnostics of the failure path: enqueues a kernel that waits, at most
+ * `polls` polls about 100 ns apart (1..2^20), for a device word nothing
+ * sets, and then records the expired wait in the context's status word, as
+ * a TMA-staged kernel does when its tile copy never arrives.  The next
+ * fdp_synchronize (or fdp_get_*) returns FDP_ERR_DEVICE once; the status
+ * word is then cleared and the context stays usable. */
+int fdp_diag_wait_timeout(fdp_ctx* ctx, int32_t polls);
+
 /* Waits for all work of the context. */
 int fdp_synchronize(fdp_ctx* ctx);
 

@@ -56,6 +56,7 @@ def test_null_context_is_rejected(fdp_lib):
     assert fdp_lib.fdp_run(None, 1, 1) == -1
     assert fdp_lib.fdp_synchronize(None) == -1
     assert fdp_lib.fdp_share_medium(None, None) == -1
+    assert fdp_lib.fdp_diag_wait_timeout(None, 10) == -1
     fdp_lib.fdp_destroy(None)
 
 

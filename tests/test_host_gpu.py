@@ -42,3 +42,19 @@ def test_fdp_host_reports_missing_input(tmp_path):
     r = subprocess.run([str(build.HOST_EXE), "--dir", str(tmp_path)], capture_output=True, text=True)
     assert r.returncode != 0
     assert "NOPE.IN NOT FOUND" in r.stderr
+
+
+@pytest.mark.gpu
+def test_fdp_host_stops_on_a_stop_file(tmp_path):
+    """time_loop.F90:79-86: a file named STOP ends the run before the next
+    level and receives that level's number; nothing is written for the
+    levels not run."""
+    cfg, med = job.small_homogeneous(mx=40, mz=30, nsteps=60, tpml=6, f0=250.0, n_rec=3)
+    med = type(med)(np.ones((cfg.n_model_rows, cfg.mx), np.int32), med.table)
+    d = formats.write_job(tmp_path / "job", "JOB", cfg, med, "f32")
+    (d / "STOP").write_text("")
+    build.build()
+    r = subprocess.run([str(build.HOST_EXE), "--dir", str(d)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert (d / "STOP").read_text().split() == ["1"]
+    assert not (d / "REC_UW_1.asc").exists() or (d / "REC_UW_1.asc").read_text() == ""
