@@ -98,3 +98,26 @@ def test_bounds_checked_build_catches_bad_jm():
     o = Oracle(inp.mx, inp.mz, inp.tpml, inp.lin_x, inp.lin_z, inp.h, inp.dt)
     with pytest.raises(RuntimeError):
         o.set_medium(bad, inp.table)
+
+
+def test_fast_p_wave_travels_at_the_biot_speed():
+    # homogeneous sandstone, explosive source: the fast P pulse's peak moves
+    # along the source row at CALCUL_VELOCITY's fast-P speed (calcul_velocity.F90)
+    from oracle import setup_ref
+    n, f0, levels = 240, 300.0, 420
+    cfg, med = job.small_homogeneous(mx=n, mz=n, nsteps=levels, tpml=20, f0=f0, n_rec=2, key_tlp=False)
+    src_x = n // 2
+    ir = np.array([src_x + 30, src_x + 90], np.int32)
+    _, lin_z = job.source_cell(cfg, cfg.h)
+    lr = np.full(2, lin_z, np.int32)
+    cfg.irecx, cfg.lrecx, cfg.irecz, cfg.lrecz = ir, lr, ir, lr
+    inp, o = _run(cfg, med, "f64", levels)
+    t = inp.table[0]
+    C = setup_ref.COL
+    vpf = setup_ref.calcul_velocity(t[C["SXX1"]], -t[C["P1"]], -t[C["P3"]], t[C["MU"]],
+                                    inp.h * t[C["R1U"]] / inp.dt, inp.h * t[C["R2QX"]] / inp.dt,
+                                    inp.h * t[C["R3U"]] / inp.dt, np.float64)[0]
+    u = o.receivers(1, levels)[:, :, 0]
+    peaks = np.argmax(np.abs(u), axis=0) * inp.dt
+    speed = 60.0 * cfg.h / (peaks[1] - peaks[0])
+    assert abs(speed / vpf - 1) < 0.03, (speed, vpf)
