@@ -356,13 +356,57 @@ def run_gpu(args) -> None:
 BATCH = dict(shots=64, mt2=3000, seed=20251)
 
 
-def _prepare_batch_shot(item):
-    """Prepared FP32 inputs of one shot of the batched workload (runs in a
-    worker process; the result is uploaded by the parent)."""
+def _prepare_batch_shot(item, precision: str = "f32"):
+    """Prepared inputs of one shot of the batched workload (runs in a worker
+    process; the result is uploaded by the parent)."""
     from fdporo import job
     seed, kw = item
     cfg, med = job.batch_shot(seed, **kw)
-    return job.prepare(cfg, med, "f32")
+    return job.prepare(cfg, med, precision)
+
+
+def _prepare_batch_shot_f64(item):
+    return _prepare_batch_shot(item, "f64")
+
+
+def plain_fp64_comparison(shots, dev: int, levels: int = 10) -> dict:
+    """The plain single-shot path in the reference's working precision
+    (REAL(8)): every shot of the batch alone through fdp_run in FP64, timed
+    over `levels` levels each; and the FP32 seismogram error against FP64
+    over the whole run of the smallest shot."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    import torch
+    from fdporo import job
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ms, cells, small = 0.0, [], None
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as pool:
+        for item, inp in zip(shots, pool.map(_prepare_batch_shot_f64, shots)):
+            e = job.make_engine(inp, device=dev)
+            e.time_loop(1, 3)
+            s = torch.cuda.ExternalStream(e.stream(), device=dev)
+            e0.record(s)
+            e.time_loop(4, 3 + levels)
+            e1.record(s)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1) / levels
+            e.close()
+            cells.append(inp.cells)
+            if small is None or inp.cells < small[1]:
+                small = (item, inp.cells)
+    # FP32 against FP64 over a whole run of the smallest shot
+    item = small[0]
+    recs = []
+    for prec in ("f32", "f64"):
+        inp = _prepare_batch_shot(item, prec)
+        e = job.make_engine(inp, device=dev)
+        e.time_loop(1, inp.mt2)
+        recs.append(e.receivers(1, inp.mt2)[:, :, [0, 1, 8, 9]].astype(np.float64))
+        e.close()
+    err = float(np.linalg.norm(recs[0] - recs[1]) / max(np.linalg.norm(recs[1]), 1e-300))
+    return {"ms_per_level": ms, "levels_timed_per_shot": levels, "cells_per_level": sum(cells),
+            "fp32_seismogram_rel_l2_vs_fp64": err, "error_shot_cells": small[1]}
 
 
 def run_batch(args) -> None:
@@ -428,6 +472,7 @@ def run_batch(args) -> None:
     for e in engines:
         e.close()
     per_shot = lambda ms: args.shots * 3600.0 / (BATCH["mt2"] * ms / 1e3)
+    fp64 = plain_fp64_comparison(shots, dev)
     line = {
         "metric": "shots/hour", "value": per_shot(ms_batch), "unit": "shots/hour", "n_gpus": 1, "steps": K,
         "warmup": W, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -439,6 +484,9 @@ def run_batch(args) -> None:
         "sequential": {"ms_per_level": ms_seq, "shots_per_hour": per_shot(ms_seq),
                        "gcell_updates_per_s": total / (ms_seq / 1e3) / 1e9},
         "speedup_vs_sequential": ms_seq / ms_batch,
+        # the plain single-shot path in the reference's working precision
+        "plain_fp64_single_shot": dict(fp64, shots_per_hour=per_shot(fp64["ms_per_level"])),
+        "speedup_vs_plain_fp64_single_shot": fp64["ms_per_level"] / ms_batch,
         "tile_shape": {"units_per_item": shape[0], "waves": shape[1]},
         "gpu_launches": launches, "clocks": clk.summary(),
     }
