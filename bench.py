@@ -19,6 +19,11 @@ Arms:
                      of the dominant kernel, CPU baseline on a sample)
   --impl reference   the CPU restatement of the reference's time loop
                      (OpenMP over rows, all host threads), same workload
+
+Other workloads (--workload): batch (64 shots of uneven sizes, shots/hour
+against the same shots one after another, and against the plain FP64
+single-shot path), large (16 shots of 8192^2 over one shared medium) and
+edge (the learned absorbing edge against the strip alone and the PMLs).
 """
 from __future__ import annotations
 
