@@ -9,7 +9,9 @@
 // FP32 accumulators starting from the bias), tanh on the hidden layers.
 // Training continues in the same CTA: one thread per sample back-propagates
 // in FP32 from the bf16 activations and weights, then the CTA reduces every
-// parameter's gradient over its samples and adds it to the global gradient.
+// parameter's gradient over its samples into its own partial, and a second
+// kernel adds the tiles' partials to the gradient in tile order (no atomics:
+// training is bit-reproducible).
 // Adam updates FP32 master weights and refreshes their bf16 copies.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -90,6 +92,8 @@ struct NetArgs {
   const int4* tiles;   // (set, first, count, out_base)
   float* grad;         // training: gradient accumulator, kSets * kSetP
   double* loss;        // training: sum of squared errors
+  float* part;         // training: each tile's gradient of its set, [tiles][kSetP]
+  double* tloss;       // training: each tile's sum of squared errors
   float gscale;        // training: d loss / d y factor, 2 / (outputs in the batch)
   int damping;         // band source: outputs are damping factors, not corrections
   // array source
@@ -280,13 +284,21 @@ __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a
     const float h = __bfloat162float(H1[tid * sH + k]);
     DZ1[tid * sD + k] = s * (1.f - h * h);
   }
-  // sum of squared errors
+  // sum of squared errors: warps in order, then the tile's partial (the
+  // partials of all tiles are added in tile order by k_grad_reduce, so a
+  // training step is bit-reproducible)
+  __shared__ double wloss[kTile / 32];
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) se += __shfl_xor_sync(0xffffffffu, se, off);
-  if ((tid & 31) == 0) atomicAdd(a.loss, (double)se);
+  if ((tid & 31) == 0) wloss[tid >> 5] = (double)se;
   __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kTile / 32; ++w) t += wloss[w];
+    a.tloss[blockIdx.x] = t;
+  }
   // parameter gradients, summed over the tile's samples
-  float* grad = a.grad + (size_t)set * kSetP;
+  float* grad = a.part + (size_t)blockIdx.x * kSetP;
   const int n = min(count, kTile);
   for (int e = tid; e < kSetP; e += kTile) {
     float s = 0.f;
@@ -306,8 +318,26 @@ __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a
     } else {
       for (int q = 0; q < n; ++q) s += DY[q * sY + (e - oB3)];
     }
-    atomicAdd(grad + e, s);
+    grad[e] = s;
   }
+}
+
+// Adds the tiles' partial gradients to the gradient of their sets, each
+// parameter's partials in tile order, and their losses to the loss.
+__global__ void k_grad_reduce(const int4* __restrict__ tiles, int ntiles, const float* __restrict__ part,
+                              const double* __restrict__ tloss, float* grad, double* loss) {
+  const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (k == 0) {
+    double t = *loss;
+    for (int q = 0; q < ntiles; ++q) t += tloss[q];
+    *loss = t;
+  }
+  if (k >= kSets * kSetP) return;
+  const int set = k / kSetP, e = k % kSetP;
+  float g = grad[k];
+  for (int q = 0; q < ntiles; ++q)
+    if (tiles[q].x == set) g += part[(size_t)q * kSetP + e];
+  grad[k] = g;
 }
 
 // Adam on every parameter; zeroes the gradient and refreshes the bf16 copy.
@@ -395,6 +425,7 @@ struct fdp_edge {
   int device = 0;
   cudaStream_t stream = nullptr;
   DevArr w, wb, m, v, g, scale, loss;
+  DevArr part, tloss;         // training: per-tile partial gradients and losses
   DevArr ax, at, ay, atiles;  // array-source scratch
   float hscale[8] = {1, 1, 1, 1, 1, 1, 1, 1};
   int damping = 0;  // band outputs: damping factors instead of corrections
@@ -520,6 +551,8 @@ int edge_state(fdp_edge* e, fdp_ctx* c, EdgeState** res) {
   return FDP_OK;
 }
 
+template <int SRC> int train_tiles(fdp_edge* e, NetArgs a, int ntiles, cudaStream_t st);
+
 NetArgs net_args(fdp_edge* e) {
   NetArgs a{};
   a.wb = (const bf16*)e->wb.p;
@@ -575,7 +608,7 @@ int run_array(fdp_edge* e, int32_t n, const int32_t* set, const float* x, const 
   a.gscale = 2.f / ((float)n * kOut);
   if (train) {
     ECK(e, cudaMemsetAsync(e->loss.p, 0, sizeof(double), e->stream));
-    k_net<SRC_ARRAY, true><<<(unsigned)tiles.size(), kTile, kSmTrain, e->stream>>>(a);
+    if ((rc = train_tiles<SRC_ARRAY>(e, a, (int)tiles.size(), e->stream)) != FDP_OK) return rc;
   } else {
     k_net<SRC_ARRAY, false><<<(unsigned)tiles.size(), kTile, kSmInfer, e->stream>>>(a);
     std::vector<float> ys((size_t)n * kOut);
@@ -583,6 +616,22 @@ int run_array(fdp_edge* e, int32_t n, const int32_t* set, const float* x, const 
     ECK(e, cudaStreamSynchronize(e->stream));
     for (int k = 0; k < n; ++k) std::memcpy(y + (size_t)order[k] * kOut, &ys[(size_t)k * kOut], kOut * sizeof(float));
   }
+  ECK(e, cudaGetLastError());
+  return FDP_OK;
+}
+
+// A training launch of the network over `ntiles` tiles and the reduction
+// of their partial gradients and losses (in tile order) into the
+// gradient and the loss.
+template <int SRC> int train_tiles(fdp_edge* e, NetArgs a, int ntiles, cudaStream_t st) {
+  int rc;
+  if ((rc = ealloc(e, e->part, (size_t)ntiles * kSetP * sizeof(float))) != FDP_OK ||
+      (rc = ealloc(e, e->tloss, (size_t)ntiles * sizeof(double))) != FDP_OK)
+    return rc;
+  a.part = (float*)e->part.p;
+  a.tloss = (double*)e->tloss.p;
+  k_net<SRC, true><<<(unsigned)ntiles, kTile, kSmTrain, st>>>(a);
+  k_grad_reduce<<<(unsigned)((kAll + 255) / 256), 256, 0, st>>>(a.tiles, ntiles, a.part, a.tloss, a.grad, a.loss);
   ECK(e, cudaGetLastError());
   return FDP_OK;
 }
@@ -781,7 +830,7 @@ int fdp_edge_train_level(fdp_edge* e, fdp_ctx* trunc, fdp_ctx* ext, int32_t ox, 
   a.gscale = 2.f / ((float)s->nsamples * kOut);
   a.y = teacher ? nullptr : (float*)s->corr.p;
   ECK(e, cudaMemsetAsync(e->loss.p, 0, sizeof(double), trunc->stream));
-  k_net<SRC_BAND, true><<<s->ntiles, kTile, kSmTrain, trunc->stream>>>(a);
+  if ((rc = train_tiles<SRC_BAND>(e, a, s->ntiles, trunc->stream)) != FDP_OK) return rc;
   if ((rc = adam_step(e, lr, trunc->stream)) != FDP_OK) return rc;
   if (teacher) {
     k_edge_teacher<<<dim3((trunc->NX + 127) / 128, trunc->NZ, 1), 128, 0, trunc->stream>>>(a.t, a.e, ox, s->geo,
@@ -830,7 +879,8 @@ const char* fdp_edge_last_error(const fdp_edge* e) { return e ? e->err.c_str() :
 void fdp_edge_destroy(fdp_edge* e) {
   if (!e) return;
   if (e->stream) cudaStreamSynchronize(e->stream);
-  for (DevArr* a : {&e->w, &e->wb, &e->m, &e->v, &e->g, &e->scale, &e->loss, &e->ax, &e->at, &e->ay, &e->atiles})
+  for (DevArr* a : {&e->w, &e->wb, &e->m, &e->v, &e->g, &e->scale, &e->loss, &e->ax, &e->at, &e->ay, &e->atiles,
+                    &e->part, &e->tloss})
     if (a->p) cudaFree(a->p);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;

@@ -119,3 +119,20 @@ def test_training_lowers_reflection():
         print(kind, "reflected energy: strip alone", plain, "with the network", learned)
         assert learned["reflected_energy"] < 0.3 * plain["reflected_energy"]
         assert learned["seismogram_rel_l2"] < 0.5 * plain["seismogram_rel_l2"]
+
+
+def test_training_is_bit_reproducible():
+    """Each tile's gradient is a partial of its own, added to the gradient in
+    tile order: two trainings from the same seed on the same levels end
+    with the same parameters, bit for bit."""
+    from fdporo import edge as E
+    pair = E.make_pair(21, n=96, margin=160, depth_margin=200, nsteps=200, f0=100.0, strip="plain")
+    scale = E.field_scales(pair, levels=150, every=25)
+    params = []
+    for _ in range(2):
+        ed = E.Edge(scale=scale, seed=3)
+        ed.set_output("correct")
+        E.train_pair(ed, pair, levels=200, lr=3e-4, free_every=50, free_run=25)
+        params.append(ed.params())
+    assert np.any(params[0] != 0)
+    np.testing.assert_array_equal(params[0], params[1])
