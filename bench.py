@@ -637,8 +637,9 @@ def run_edge(args) -> None:
             for k, pair in enumerate(pool.map(_make_edge_pair, train_seeds)):
                 if ed is None:
                     ed = E.Edge(scale=E.field_scales(pair, levels=L, every=50), seed=EDGE["seed"])
-                    ed.set_output("correct")
-                losses += E.train_pair(ed, pair, levels=L, lr=3e-4, report_every=L, free_every=50, free_run=25)
+                    ed.set_output(args.edge_output)
+                lr = 1e-3 if args.edge_output == "damp" else 3e-4
+                losses += E.train_pair(ed, pair, levels=L, lr=lr, report_every=L, free_every=50, free_run=25)
         train_s = time.perf_counter() - t0
         res = {"strip_alone": [], "learned_edge": [], "pml4": [], "pml20": []}
         for pair in pool.map(_make_edge_pair, held_seeds):
@@ -677,7 +678,8 @@ def run_edge(args) -> None:
         "config": {"workload": "learned-edge", "region": EDGE["n"], "target_grid":
                    [EDGE["n"] + 2 * EDGE["margin"], EDGE["n"] + EDGE["depth_margin"]], "levels": L,
                    "train_media": args.edge_train, "held_out_media": args.edge_held, "epochs": args.edge_epochs,
-                   "strip_cells": 4, "network": "96-64-64-8 tanh, one per side and depth"},
+                   "strip_cells": 4, "network": "96-64-64-8 tanh, one per side and depth",
+                   "output": args.edge_output},
         "held_out_mean": summary, "train_seconds": train_s, "final_train_loss": losses[-1] if losses else None,
         "level_ms": {"learned_edge_4_cells": ms_edge, "pml_20_cells": ms_pml},
         "region_speedup_vs_pml20": ms_pml / ms_edge,
@@ -698,7 +700,8 @@ def main() -> None:
     ap.add_argument("--workload", choices=["layered", "batch", "edge", "large"], default="layered")
     ap.add_argument("--edge-train", type=int, default=32)
     ap.add_argument("--edge-held", type=int, default=8)
-    ap.add_argument("--edge-epochs", type=int, default=1)
+    ap.add_argument("--edge-epochs", type=int, default=2)
+    ap.add_argument("--edge-output", choices=["damp", "correct"], default="damp")
     ap.add_argument("--shots", type=int, default=BATCH["shots"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
