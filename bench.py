@@ -478,6 +478,24 @@ def run_batch(args) -> None:
         e.close()
     per_shot = lambda ms: args.shots * 3600.0 / (BATCH["mt2"] * ms / 1e3)
     fp64 = plain_fp64_comparison(shots, dev)
+    # the same shots with a 4-cell PML (the width of the learned edge's
+    # strip; on the learned-edge media it absorbs as well as the 20-cell
+    # one), batched the same way
+    thin = job.batch_shots(args.shots, nsteps=BATCH["mt2"], seed=BATCH["seed"], tpml=4)
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as pool:
+        engines = [job.make_engine(inp, device=dev) for inp in pool.map(_prepare_batch_shot, thin)]
+    b = Batch(engines)
+    ext = torch.cuda.ExternalStream(b.stream(), device=dev)
+    b.time_loop(1, W)
+    b.synchronize()
+    e0.record(ext)
+    b.time_loop(W + 1, W + K)
+    e1.record(ext)
+    e1.synchronize()
+    ms_thin = e0.elapsed_time(e1) / K
+    b.close()
+    for e in engines:
+        e.close()
     line = {
         "metric": "shots/hour", "value": per_shot(ms_batch), "unit": "shots/hour", "n_gpus": 1, "steps": K,
         "warmup": W, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -492,6 +510,9 @@ def run_batch(args) -> None:
         # the plain single-shot path in the reference's working precision
         "plain_fp64_single_shot": dict(fp64, shots_per_hour=per_shot(fp64["ms_per_level"])),
         "speedup_vs_plain_fp64_single_shot": fp64["ms_per_level"] / ms_batch,
+        "batch_4_cell_pml": {"ms_per_level": ms_thin, "shots_per_hour": per_shot(ms_thin),
+                             "speedup_vs_20_cell_batch": ms_batch / ms_thin,
+                             "speedup_vs_plain_fp64_single_shot": fp64["ms_per_level"] / ms_thin},
         "tile_shape": {"units_per_item": shape[0], "waves": shape[1]},
         "gpu_launches": launches, "clocks": clk.summary(),
     }
