@@ -112,6 +112,34 @@ struct NetArgs {
 
 __device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
+// out[(o0 + i) * ldo + k0 + j] = sum over samples q < n, in order, of
+// A[q * sA + o0 + i] * B[q * sB + k0 + j] (i < MO, j < MK): one thread's
+// block of a weight gradient.
+template <int MO, int MK>
+__device__ __forceinline__ void grad_block(const float* A, int sA, const bf16* B, int sB, int n, int o0, int k0,
+                                           float* out, int ldo) {
+  float acc[MO][MK];
+#pragma unroll
+  for (int i = 0; i < MO; ++i)
+#pragma unroll
+    for (int j = 0; j < MK; ++j) acc[i][j] = 0.f;
+  for (int q = 0; q < n; ++q) {
+    float d[MO], x[MK];
+#pragma unroll
+    for (int i = 0; i < MO; ++i) d[i] = A[q * sA + o0 + i];
+#pragma unroll
+    for (int j = 0; j < MK; ++j) x[j] = __bfloat162float(B[q * sB + k0 + j]);
+#pragma unroll
+    for (int i = 0; i < MO; ++i)
+#pragma unroll
+      for (int j = 0; j < MK; ++j) acc[i][j] += d[i] * x[j];
+  }
+#pragma unroll
+  for (int i = 0; i < MO; ++i)
+#pragma unroll
+    for (int j = 0; j < MK; ++j) out[(o0 + i) * ldo + k0 + j] = acc[i][j];
+}
+
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -297,28 +325,27 @@ __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a
     for (int w = 0; w < kTile / 32; ++w) t += wloss[w];
     a.tloss[blockIdx.x] = t;
   }
-  // parameter gradients, summed over the tile's samples
+  // parameter gradients, summed over the tile's samples in sample order:
+  // each thread a block of every weight matrix's gradient, its operands
+  // loaded once per sample for the whole block
+  static_assert(kTile == 128 && kHid == 64 && kIn == 96 && kOut == 8, "gradient blocks of the thread mapping");
   float* grad = a.part + (size_t)blockIdx.x * kSetP;
   const int n = min(count, kTile);
-  for (int e = tid; e < kSetP; e += kTile) {
+  grad_block<4, 12>(DZ1, sD, X, sX, n, (tid >> 3) * 4, (tid & 7) * 12, grad + oW1, kIn);
+  grad_block<4, 8>(DZ2, sD, H1, sH, n, (tid >> 3) * 4, (tid & 7) * 8, grad + oW2, kHid);
+  grad_block<1, 4>(DY, sY, H2, sH, n, tid >> 4, (tid & 15) * 4, grad + oW3, kHid);
+  for (int e = tid; e < 2 * kHid + kOut; e += kTile) {
     float s = 0.f;
-    if (e < oB1) {
-      const int o = e / kIn, k = e % kIn;
-      for (int q = 0; q < n; ++q) s += DZ1[q * sD + o] * __bfloat162float(X[q * sX + k]);
-    } else if (e < oW2) {
-      for (int q = 0; q < n; ++q) s += DZ1[q * sD + (e - oB1)];
-    } else if (e < oB2) {
-      const int o = (e - oW2) / kHid, k = (e - oW2) % kHid;
-      for (int q = 0; q < n; ++q) s += DZ2[q * sD + o] * __bfloat162float(H1[q * sH + k]);
-    } else if (e < oW3) {
-      for (int q = 0; q < n; ++q) s += DZ2[q * sD + (e - oB2)];
-    } else if (e < oB3) {
-      const int o = (e - oW3) / kHid, k = (e - oW3) % kHid;
-      for (int q = 0; q < n; ++q) s += DY[q * sY + o] * __bfloat162float(H2[q * sH + k]);
+    if (e < kHid) {
+      for (int q = 0; q < n; ++q) s += DZ1[q * sD + e];
+      grad[oB1 + e] = s;
+    } else if (e < 2 * kHid) {
+      for (int q = 0; q < n; ++q) s += DZ2[q * sD + (e - kHid)];
+      grad[oB2 + e - kHid] = s;
     } else {
-      for (int q = 0; q < n; ++q) s += DY[q * sY + (e - oB3)];
+      for (int q = 0; q < n; ++q) s += DY[q * sY + (e - 2 * kHid)];
+      grad[oB3 + e - 2 * kHid] = s;
     }
-    grad[e] = s;
   }
 }
 

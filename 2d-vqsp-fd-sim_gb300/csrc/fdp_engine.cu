@@ -529,12 +529,14 @@ void derive_table(const int32_t jmnum, const T* tab, HostBuf<T>& out) {
     put(fdp::C_SZZ1, r[SZZ1]); put(fdp::C_SZZ2, r[SZZ2]); put(fdp::C_SZZ3, r[SZZ3]);
     put(fdp::C_P1, r[P1]); put(fdp::C_P2, r[P2]); put(fdp::C_P3, r[P3]);
     // inh_qx_int.F90:44 and inh_v_uv_int.F90:46, evaluated per material
-    put(fdp::C_EQX, std::exp(-r[R3QX]));
-    put(fdp::C_CU, (r[R2U] / r[R3QX]) * (T(1) - std::exp(-r[R3QX])));
+    // each exponential evaluated once (the same call gives the same value)
+    const T eqx = std::exp(-r[R3QX]), eqz = std::exp(-r[R3QZ]);
+    put(fdp::C_EQX, eqx);
+    put(fdp::C_CU, (r[R2U] / r[R3QX]) * (T(1) - eqx));
     put(fdp::C_R1QX, r[R1QX]); put(fdp::C_R2QX, r[R2QX]);
     put(fdp::C_R1U, r[R1U]); put(fdp::C_R3U, r[R3U]);
-    put(fdp::C_EQZ, std::exp(-r[R3QZ]));
-    put(fdp::C_CW, (r[R2W] / r[R3QZ]) * (T(1) - std::exp(-r[R3QZ])));
+    put(fdp::C_EQZ, eqz);
+    put(fdp::C_CW, (r[R2W] / r[R3QZ]) * (T(1) - eqz));
     put(fdp::C_R1QZ, r[R1QZ]); put(fdp::C_R2QZ, r[R2QZ]);
     put(fdp::C_R1W, r[R1W]); put(fdp::C_R3W, r[R3W]);
     put(fdp::C_AUXW, r[AUXW]); put(fdp::C_AUXQZ, r[AUXQZ]);
