@@ -7,6 +7,8 @@
 #include <memory>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "fdp.h"
 #include "fdp_core_tma.cuh"
 
@@ -92,6 +94,15 @@ struct fdp_ctx {
   // trained or carried an edge; applied after every level while attached
   EdgeState* edge = nullptr;
   bool edge_attached = false;
+};
+
+// An NVTX range around an entry point, for profilers' timelines (nvtx3 is
+// header-only: nothing is loaded unless a profiler is attached).
+struct TraceRange {
+  explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange&) = delete;
+  TraceRange& operator=(const TraceRange&) = delete;
 };
 
 // Marks the context's device parameters changed: its captured graph is

@@ -828,6 +828,7 @@ int fdp_edge_train_batch(fdp_edge* e, int32_t n, const int32_t* set, const float
 
 int fdp_edge_train_level(fdp_edge* e, fdp_ctx* trunc, fdp_ctx* ext, int32_t ox, int32_t level, float lr,
                          int32_t teacher, double* loss) {
+  const TraceRange trace("fdp_edge_train_level");
   if (!e || !trunc || !ext) return efail(e, FDP_ERR_ARG, "null argument");
   if (trunc->prec != 4 || ext->prec != 4) return efail(e, FDP_ERR_UNSUPPORTED, "the learned edge runs on FP32 contexts");
   if ((trunc->g.stress_imaging != 0) != (ext->g.stress_imaging != 0))

@@ -736,6 +736,7 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
 extern "C" {
 
 int fdp_create(const fdp_grid* g, fdp_ctx** out) {
+  const TraceRange trace("fdp_create");
   if (!g || !out) return fail(nullptr, FDP_ERR_ARG, "null argument");
   *out = nullptr;
   if (g->precision != FDP_F32 && g->precision != FDP_F64)
@@ -828,6 +829,7 @@ void unshare_medium(fdp_ctx* c) {
 }
 
 int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_t jmnum, const void* table24) {
+  const TraceRange trace("fdp_set_medium");
   if (!c || !jm || !table24) return fail(c, FDP_ERR_ARG, "null argument");
   if (nx != c->NX || nz != c->NZ) return fail(c, FDP_ERR_ARG, "JM is %dx%d, grid is %dx%d", nx, nz, c->NX, c->NZ);
   if (jmnum < 1) return fail(c, FDP_ERR_ARG, "JMNUM must be >= 1");
@@ -859,6 +861,7 @@ int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_
 }
 
 int fdp_share_medium(fdp_ctx* dst, fdp_ctx* src) {
+  const TraceRange trace("fdp_share_medium");
   if (!dst || !src) return fail(dst, FDP_ERR_ARG, "null argument");
   if (dst == src) return FDP_OK;
   if (!src->have_medium) return fail(dst, FDP_ERR_STATE, "the source context has no medium yet");
@@ -962,6 +965,7 @@ int fdp_set_receivers(fdp_ctx* c, const int32_t* irecx, const int32_t* lrecx, co
 }
 
 int fdp_run(fdp_ctx* c, int32_t it_begin, int32_t it_end) {
+  const TraceRange trace("fdp_run");
   if (!c) return fail(c, FDP_ERR_ARG, "null context");
   if (!c->have_medium || !c->have_pml || !c->have_nr || !c->have_source)
     return fail(c, FDP_ERR_STATE, "set medium, PML profiles, bottom coefficients and source before fdp_run");
@@ -976,6 +980,7 @@ int fdp_run(fdp_ctx* c, int32_t it_begin, int32_t it_end) {
 }
 
 int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host) {
+  const TraceRange trace("fdp_get_receivers");
   if (!c || (!host && n_levels > 0)) return fail(c, FDP_ERR_ARG, "null argument");
   if (n_levels <= 0 || c->mr == 0) return FDP_OK;
   if (it_first < 1 || it_first + n_levels - 1 > c->mt2) return fail(c, FDP_ERR_ARG, "levels outside 1..MT2");
@@ -1123,6 +1128,7 @@ int fdp_get_stream(fdp_ctx* c, void** stream) {
 }
 
 int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out, int64_t* launches_out) {
+  const TraceRange trace("fdp_profile_run");
   if (!c || !ms_out || !launches_out) return fail(c, FDP_ERR_ARG, "null argument");
   if (!c->have_medium || !c->have_pml || !c->have_nr || !c->have_source)
     return fail(c, FDP_ERR_STATE, "set medium, PML profiles, bottom coefficients and source before profiling");
@@ -1718,6 +1724,7 @@ int fdp_batch_get_shape(fdp_batch* b, int32_t* units_per_item, int32_t* waves) {
 }
 
 int fdp_batch_run(fdp_batch* b, int32_t it_begin, int32_t it_end) {
+  const TraceRange trace("fdp_batch_run");
   if (!b) return bfail(b, FDP_ERR_ARG, "null batch");
   if (it_end < it_begin) return FDP_OK;
   for (size_t s = 0; s < b->shots.size(); ++s) {
