@@ -1088,7 +1088,9 @@ __device__ __forceinline__ T core_coef(const Params<T>& p, int k, long long cell
   }
 }
 
-#define FDP_CORE_BOUNDS(T) __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? 2 : 1)
+// Two CTAs per SM in both precisions (FP64: 128 registers, no spills; 4.50
+// instead of 4.20 Gcell-updates/s with one CTA of up to 252 registers).
+#define FDP_CORE_BOUNDS(T) __launch_bounds__(kBX * kBZ, 2)
 
 // core block (bx, by) of a phase: 4*kBX columns by kBZ rows of its core
 template <class T, int MODE>
