@@ -3,8 +3,13 @@
 // A context holds one shot's grid resident in HBM: the eight wavefield
 // arrays, the medium, the PML profiles and memory variables, the bottom
 // history, the source time function and the receiver samples.  fdp_run
-// enqueues three kernels per time level on the context's stream; runs of
-// kChunk levels are captured once into a CUDA graph and replayed.
+// enqueues each time level's kernels on the context's stream (with the
+// frame/core split: each phase's frame kernel on a side stream beside its
+// core kernel, the row-1/receiver step folded into the next level's stress
+// frame kernel, one k_edge at the end of a run); runs of kChunk levels are
+// captured once into a CUDA graph and replayed.  Batches (fdp_batch_*)
+// advance many contexts together: work-queue kernels over all shots, or
+// every shot's own level sequence side by side in one graph.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>

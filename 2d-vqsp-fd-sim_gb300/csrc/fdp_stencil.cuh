@@ -5,7 +5,9 @@
 // (time_loop.F90:133-179) likewise with k_velocity; k_edge is the one step
 // with a cross-column dependency (the stress-imaging row 1,
 // hplane_1_velocity.F90:61-76) plus receiver sampling
-// (store_seismograms.F90:47-104, store_seismograms_pressure.F90:45-58).
+// (store_seismograms.F90:47-104, store_seismograms_pressure.F90:45-58);
+// inside a run of levels the split does that step in the next level's
+// k_stress_frame (and the stress samples in k_velocity_frame).
 //
 // Every row routine of the reference (strain_*, stress_*, inh_*, sto_*)
 // becomes a branch on the cell's row and column class inside these kernels;
