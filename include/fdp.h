@@ -20,8 +20,10 @@
  *     (FDP_F32 = REAL(4), FDP_F64 = REAL(8)); that is the reference's
  *     working precision PP (mod_precision.F90:7,10).
  *   - The context owns all device memory; the caller owns all host memory.
- *   - One host thread per context; one CUDA stream per context.  fdp_run
- *     only enqueues work; fdp_get_* and fdp_synchronize wait for it.
+ *   - One host thread per context; one CUDA stream per context (its frame
+ *     kernels run on a second stream forked from and joined back into it;
+ *     fdp_get_stream returns the first).  fdp_run only enqueues work;
+ *     fdp_get_* and fdp_synchronize wait for it.
  */
 #ifndef FDP_H
 #define FDP_H
