@@ -147,15 +147,15 @@ __global__ void __launch_bounds__(kBX * kBZ, 1) k_core_tma(const __grid_constant
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           auto C = [&](int k) { return core_coef<float, M_BIOT>(p, k, 0, 0, bio, 0, j); };
-          // strain_uw_xz.F90:201-204
+          // strain_uw_xz.F90:81-84
           const float exz = p.AH * (up1.v[j] - um2.v[j] + at(wr, j, 1) - at(wr, j, -2))
                           + p.BH * (ur[1].v[j] - um1.v[j] + wr[1].v[j] - at(wr, j, -1));
-          // strain_uw_zz.F90:43,49 and strain_q_zz.F90:43,49
+          // strain_uw_zz.F90:51,58-59 and strain_q_zz.F90:48,55-56
           float ezz = (p.CH * (wp1.v[j] - wr[1].v[j]));
           ezz = p.AH * (wp2.v[j] - wm1.v[j]) + p.BC * ezz;
           float qzz = (p.CH * (zp1.v[j] - z0.v[j]));
           qzz = p.AH * (zp2.v[j] - zm1.v[j]) + p.BC * qzz;
-          // strain_uw_xx.F90:71-72 and strain_q_xx.F90:70-71
+          // strain_uw_xx.F90:82-83 and strain_q_xx.F90:77-78
           const float exx = p.AH * (at(ur, j, 2) - at(ur, j, -1)) + p.BH * (at(ur, j, 1) - ur[1].v[j]);
           const float qxx = p.AH * (at(xr, j, 2) - at(xr, j, -1)) + p.BH * (at(xr, j, 1) - xr[1].v[j]);
           // stress_xz.F90:44-46 and stress_nn.F90:53-59

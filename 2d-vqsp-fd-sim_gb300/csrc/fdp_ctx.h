@@ -81,8 +81,10 @@ struct fdp_ctx {
   // set while jm, coef, planes and aux belong to a share with other
   // contexts (the share frees them, not this context)
   std::shared_ptr<MediumShare> medium_share;
-  // graph of kChunk levels
-  cudaGraphExec_t graph = nullptr;
+  // captured runs of levels, indexed by their length (1..kRunGraphs); the
+  // longest is replayed over and over, a shorter one ends a run
+  static constexpr int kRunGraphs = 32;
+  cudaGraphExec_t graph[kRunGraphs + 1] = {};
   bool params_dirty = true;
   // bumped by every change of the device parameters (set_*, a shared
   // medium, an attached edge); a batch refuses to run a shot whose count

@@ -39,7 +39,9 @@ namespace {
 constexpr int kChunk = 32;       // time levels per captured graph
 constexpr int kBlockX = 128;     // threads per block (x)
 
-std::string g_create_error;
+// Message of the last failed call that has no context, per host thread, so
+// concurrent callers neither race on it nor see each other's messages.
+thread_local std::string g_create_error;
 
 }  // namespace
 
@@ -209,7 +211,7 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   p.A = (T)(-1.0f / 24.0f);
   p.B = (T)(9.0f / 8.0f);
   p.AH = p.A / H; p.BH = p.B / H; p.CH = T(1) / H;
-  p.BC = p.BH / p.CH;  // strain_uw_zz.F90:39
+  p.BC = p.BH / p.CH;  // strain_uw_zz.F90:45
   p.DT = (T)c->g.dt;
   p.DTE = p.DT + (T)c->g.tau_eps;
   const size_t off = (size_t)kPadZ * c->pitch + kPadX;
@@ -450,47 +452,72 @@ long long run_launches(const fdp_ctx* c, int n) {
   return (long long)n * (2 + cores + (c->edge && c->edge_attached ? 3 : 0)) + edges;
 }
 
-template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
-  Params<T> p;
-  fill_params<T>(c, p);
-  // levels per graph replay = kChunk; the graph reads the level from
-  // *it_base and advances it by kChunk at its end.
-  if (c->params_dirty && c->graph) {
-    cudaGraphExecDestroy(c->graph);
-    c->graph = nullptr;
+// Frees every captured run of levels (their kernels' parameters changed).
+void drop_graphs(fdp_ctx* c) {
+  for (auto& g : c->graph)
+    if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+// The captured graph of a run of n levels (1 <= n <= kChunk), captured on
+// first use: the run's kernels as launch_level_any enqueues them, then the
+// level counter advanced by n, so a replay continues from whatever level
+// *it_base holds.
+template <class T> int run_graph(fdp_ctx* c, const Params<T>& p, int n, cudaGraphExec_t* out) {
+  if (c->params_dirty) {
+    drop_graphs(c);
+    c->params_dirty = false;
   }
-  c->params_dirty = false;
-  fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
-  c->launches += 1;
-  int it = it_begin;
-  const int nlev = it_end - it_begin + 1;
-  if (nlev >= kChunk && !c->graph) {
+  if (!c->graph[n]) {
     cudaGraph_t gr = nullptr;
     CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const long long before = c->launches;
-    for (int k = 0; k < kChunk; ++k) launch_level_any<T>(c, p, k, k == 0, k == kChunk - 1);
-    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, kChunk);
-    c->launches = before;  // capture only records; replays are counted below
+    for (int k = 0; k < n; ++k) launch_level_any<T>(c, p, k, k == 0, k == n - 1);
+    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
+    c->launches = before;  // capture only records; replays are counted by the caller
     cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
     if (e != cudaSuccess) return fail(c, FDP_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&c->graph, gr, 0);
+    e = cudaGraphInstantiate(&c->graph[n], gr, 0);
     cudaGraphDestroy(gr);
-    if (e != cudaSuccess) { c->graph = nullptr; return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+    if (e != cudaSuccess) {
+      c->graph[n] = nullptr;
+      return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
   }
-  const long long per_chunk = run_launches(c, kChunk);
-  while (it_end - it + 1 >= kChunk && c->graph) {
-    CK(c, cudaGraphLaunch(c->graph, c->stream));
-    c->launches += per_chunk + 1;
-    it += kChunk;
-  }
-  int k = 0;
-  for (; it <= it_end; ++it, ++k) launch_level_any<T>(c, p, k, k == 0, it == it_end);
-  if (k > 0) {
-    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, k);
-    c->launches += 1;
+  *out = c->graph[n];
+  return FDP_OK;
+}
+
+// Levels it_begin..it_end: replays of the kChunk-level graph, then one
+// graph of the remaining levels.  Every run length has its own graph, so a
+// short run costs one graph launch, not its levels' launches one by one.
+template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
+  Params<T> p;
+  fill_params<T>(c, p);
+  fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
+  c->launches += 1;
+  int it = it_begin;
+  while (it <= it_end) {
+    const int n = std::min(kChunk, it_end - it + 1);
+    cudaGraphExec_t g = nullptr;
+    int rc = run_graph<T>(c, p, n, &g);
+    if (rc != FDP_OK) return rc;
+    CK(c, cudaGraphLaunch(g, c->stream));
+    c->launches += run_launches(c, n) + 1;
+    it += n;
   }
   CK(c, cudaGetLastError());
   return FDP_OK;
+}
+
+// Captures the graphs a run of n_levels levels replays (fdp_prepare_run).
+template <class T> int prepare_t(fdp_ctx* c, int n_levels) {
+  Params<T> p;
+  fill_params<T>(c, p);
+  cudaGraphExec_t g = nullptr;
+  int rc = FDP_OK;
+  if (n_levels >= kChunk) rc = run_graph<T>(c, p, kChunk, &g);
+  if (rc == FDP_OK && n_levels % kChunk) rc = run_graph<T>(c, p, n_levels % kChunk, &g);
+  return rc;
 }
 
 // Runs fn(begin, end) over [0, n) split across the host's cores, at least
@@ -519,7 +546,7 @@ template <class T> struct HostBuf {
 
 template <class T>
 void derive_table(const int32_t jmnum, const T* tab, HostBuf<T>& out) {
-  // table24 columns (.MO record order, read_model_par.F90:147-155)
+  // table24 columns (.MO record order, read_model_par.F90:52-60)
   enum { MU, SXX1, SXX2, SXX3, SZZ1, SZZ2, SZZ3, P1, P2, P3, R1U, R1W, R2U, R2W, R3U, R3W,
          R1QX, R1QZ, R2QX, R2QZ, R3QX, R3QZ, AUXW, AUXQZ };
   const size_t ld = (size_t)jmnum + 1;
@@ -923,6 +950,18 @@ int fdp_set_pml(fdp_ctx* c, const void* const* prof) {
   return FDP_OK;
 }
 
+int fdp_set_pml_arrays(fdp_ctx* c, const void* oda_xl, const void* odb_xl, const void* odc_xl, const void* odd_xl,
+                       const void* oda_xh, const void* odb_xh, const void* odc_xh, const void* odd_xh,
+                       const void* oda_zh, const void* odb_zh, const void* odc_zh, const void* odd_zh,
+                       const void* oda2_xl, const void* odb2_xl, const void* odc2_xl, const void* odd2_xl,
+                       const void* oda2_xh, const void* odb2_xh, const void* odc2_xh, const void* odd2_xh,
+                       const void* oda2_zh, const void* odb2_zh, const void* odc2_zh, const void* odd2_zh) {
+  const void* const prof[24] = {oda_xl,  odb_xl,  odc_xl,  odd_xl,  oda_xh,  odb_xh,  odc_xh,  odd_xh,
+                                oda_zh,  odb_zh,  odc_zh,  odd_zh,  oda2_xl, odb2_xl, odc2_xl, odd2_xl,
+                                oda2_xh, odb2_xh, odc2_xh, odd2_xh, oda2_zh, odb2_zh, odc2_zh, odd2_zh};
+  return fdp_set_pml(c, prof);
+}
+
 int fdp_set_bottom_nr(fdp_ctx* c, const void* ab16) {
   if (!c || !ab16) return fail(c, FDP_ERR_ARG, "null argument");
   int rc;
@@ -982,6 +1021,18 @@ int fdp_run(fdp_ctx* c, int32_t it_begin, int32_t it_end) {
   int rc = (c->prec == 8) ? run_t<double>(c, it_begin, it_end) : run_t<float>(c, it_begin, it_end);
   if (rc == FDP_OK && it_end > c->last_it) c->last_it = it_end;
   return rc;
+}
+
+int fdp_prepare_run(fdp_ctx* c, int32_t n_levels) {
+  const TraceRange trace("fdp_prepare_run");
+  if (!c) return fail(c, FDP_ERR_ARG, "null context");
+  if (!c->have_medium || !c->have_pml || !c->have_nr || !c->have_source)
+    return fail(c, FDP_ERR_STATE, "set medium, PML profiles, bottom coefficients and source before fdp_prepare_run");
+  if (n_levels < 0) return fail(c, FDP_ERR_ARG, "negative number of levels");
+  if (c->mr > 0 && !c->raw.p) return fail(c, FDP_ERR_STATE, "receiver buffer missing");
+  if (n_levels == 0) return FDP_OK;
+  CK(c, cudaSetDevice(c->g.device));
+  return (c->prec == 8) ? prepare_t<double>(c, n_levels) : prepare_t<float>(c, n_levels);
 }
 
 int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host) {
@@ -1208,7 +1259,7 @@ void fdp_destroy(fdp_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   fdp::edge_release(c);
-  if (c->graph) cudaGraphExecDestroy(c->graph);
+  drop_graphs(c);
   unshare_medium(c);
   DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase,
                    &c->errbuf, &c->frame_s, &c->frame_v, &c->diag_flag};

@@ -92,7 +92,7 @@ template <class T> int run(const Opts& o) {
   }
   FILE* log = std::fopen((D + job + ".LOG").c_str(), "w");
   if (log) std::fprintf(log, " LOG_FILE: JOB_NAME =%s\n", job.c_str());
-  // read_open.F90:184-196
+  // read_open.F90:83-95
   if (!exists(D + job + ".IN")) die(job + ".IN NOT FOUND", log);
   const std::string IN = slurp(D + job + ".IN"), INM = slurp(D + job + ".INM");
   if (INM.empty()) die(job + ".INM NOT FOUND", log);
@@ -100,13 +100,13 @@ template <class T> int run(const Opts& o) {
     const std::string v = nml(text, g, n);
     return v.empty() ? dflt : v;
   };
-  // CONTROLDATA (read_open.F90:208-214)
+  // CONTROLDATA (read_open.F90:107-113)
   const int TPML = std::atoi(get(IN, "CONTROLDATA", "TPML", "0").c_str());
   const bool SI = to_logical(get(IN, "CONTROLDATA", "STRESS_IMAGING", "T"));
-  // NAMES (read_open.F90:203-217)
+  // NAMES (read_open.F90:102-116)
   const std::string MO = trim(get(INM, "NAMES", "MO_FILE_NAME", job + ".MO"));
   const std::string JMH = trim(get(INM, "NAMES", "JMH_FILE_NAME", job + ".JMH"));
-  // CONTROLDATA1 (read_open.F90:219-229); default-real literals
+  // CONTROLDATA1 (read_open.F90:118-128); default-real literals
   const std::string mt_s = nml(IN, "CONTROLDATA1", "MT");
   if (mt_s.empty()) die("CONTROLDATA1 lacks MT", log);
   const float MT = (float)to_real(mt_s);
@@ -123,8 +123,8 @@ template <class T> int run(const Opts& o) {
   const bool SNV = to_logical(get(IN, "KEYS", "KEY_SNV", "F"));
   const bool TLQ = to_logical(get(IN, "KEYS", "KEY_TLQ", "F"));
   const bool TLP = to_logical(get(IN, "KEYS", "KEY_TLP", "F"));
-  if (!(TLV || SNV)) die("NONE OF TL_ AND SN_ OUTPUT FILES IS REQUIRED", log);  // read_open.F90:240-243
-  // CONTROLDATA2 (read_open.F90:245-254)
+  if (!(TLV || SNV)) die("NONE OF TL_ AND SN_ OUTPUT FILES IS REQUIRED", log);  // read_open.F90:139-142
+  // CONTROLDATA2 (read_open.F90:144-153)
   const int MX = std::atoi(nml(INM, "CONTROLDATA2", "MX").c_str());
   int MZ = std::atoi(nml(INM, "CONTROLDATA2", "MZ").c_str());
   const T H = (T)to_real(nml(INM, "CONTROLDATA2", "H"));
@@ -133,7 +133,7 @@ template <class T> int run(const Opts& o) {
   if (MX <= 0 || MZ <= 0 || !(H > 0) || !(DT > 0)) die("CONTROLDATA2 incomplete", log);
   if (SI) MZ += 2;
   const int MT2 = (int)((T)MT / DT) + 1;
-  // SOURCE (read_open.F90:262-270)
+  // SOURCE (read_open.F90:161-169)
   float XS = std::fabs((float)to_real(get(IN, "SOURCE", "X_SOURCE", "0")));
   float ZS = std::fabs((float)to_real(get(IN, "SOURCE", "Z_SOURCE", "0")));
   const int KEY_SOUR = std::atoi(get(IN, "SOURCE", "KEY_SOUR", "0").c_str());
@@ -141,13 +141,13 @@ template <class T> int run(const Opts& o) {
   if (SI) ZS = (float)((T)ZS + (T)2 * H);
   const int LIN_X = nint((double)((T)(XS - XBMIN) / H));
   const int LIN_Z = nint((double)((T)ZS / H));
-  // NONREF (read_open.F90:275-289)
+  // NONREF (read_open.F90:174-188)
   const T WB = (T)to_real(get(IN, "NONREF", "WB", "0.4"));
   const int KTBO = std::atoi(get(IN, "NONREF", "KTBO", "0").c_str());
   const T THPP = (T)to_real(get(IN, "NONREF", "THPPBO", "0.19757"));
   const T THSS = (T)to_real(get(IN, "NONREF", "THSSBO", "0.70511"));
   const T OMG = (T)to_real(get(IN, "NONREF", "OMG", "0")) / (T)6.283185307179586476925286766559;
-  // REC (read_open.F90:314-341)
+  // REC (read_open.F90:213-240)
   std::vector<int32_t> IRX, LRX, IRZ, LRZ;
   int MR = 0;
   if (TLV) {
@@ -176,7 +176,7 @@ template <class T> int run(const Opts& o) {
       die("bad JM record " + std::to_string(r + 1) + " in " + JMH, log);
   }
   if (fdp_prep_expand_jm(MX, MZ, TPML, SI, rows.data(), jm.data()) != FDP_OK) die("READ_MODEL failed", log);
-  // READ_MODEL_PAR (read_model_par.F90:132-169)
+  // READ_MODEL_PAR (read_model_par.F90:37-74)
   int32_t jmnumr = 0;
   int64_t nb = 0;
   if (fdp_io_read_record((D + MO).c_str(), 0, &jmnumr, 4, &nb) != FDP_OK) die("bad JMNUM record in " + MO, log);

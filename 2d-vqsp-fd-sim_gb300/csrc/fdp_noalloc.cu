@@ -2,13 +2,15 @@
 // in include/fdp.h).
 //
 // Some hosts cannot call cudaMalloc: a Fortran or C driver whose device
-// arrays live in a memory pool it manages itself, code that runs inside
-// CUDA stream capture (where allocation would break the capture), or a
-// runtime that forbids allocation after start-up.  For them this entry point
-// takes every input and output as caller-owned device memory and keeps its
-// only state -- each receiver's previous sample, which the time derivative
-// of STORE_SEISMOGRAMS needs (store_seismograms.F90:65-66, 92-93) -- in a
-// fixed static device array instead of allocating one.
+// arrays live in a memory pool it manages itself (a second allocator would
+// fragment or overcommit the memory that pool has reserved), or a runtime
+// that forbids allocation once it is running (allocation synchronises the
+// device and may fail late, in the middle of a survey).  For them this entry
+// point takes every input and output as caller-owned device memory and keeps
+// its only state -- each receiver's previous sample, which the time
+// derivative of STORE_SEISMOGRAMS needs (store_seismograms.F90:65-66,
+// 92-93) -- in a fixed static device array instead of allocating one.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -26,7 +28,11 @@ static __device__ __align__(256) unsigned char g_prev_samples[(size_t)FDP_NOALLO
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void* g_prev_ptr[kMaxDevices] = {};  // device address of g_prev_samples, per device
+// device address of g_prev_samples per device, and the id of the context it
+// was looked up in: a device reset makes a new context, in which the array
+// may sit elsewhere, so the address is looked up again there
+void* g_prev_ptr[kMaxDevices] = {};
+unsigned long long g_prev_ctx[kMaxDevices] = {};
 
 }  // namespace
 
@@ -75,24 +81,55 @@ __global__ void k_receivers_noalloc(const T* um, const T* wm, const T* qx, const
   p[0] = s[0]; p[1] = s[1]; p[2] = s[2]; p[3] = s[3];
 }
 
-// Device address of the static state on the current device, looked up on
-// the first call per device.
+// Id of the current device's primary context (made current first), through
+// the driver entry points the runtime exposes.
+int current_context_id(int dev, unsigned long long* id) {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return fail(FDP_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId not found");
+    get_current = (GetCurrent)f1;
+    get_id = (GetId)f2;
+  }
+  // cudaSetDevice makes the device's primary context current (creating it
+  // when the device has none yet)
+  cudaError_t e = cudaSetDevice(dev);
+  if (e != cudaSuccess) return fail(FDP_ERR_CUDA, cudaGetErrorString(e));
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, id) != CUDA_SUCCESS)
+    return fail(FDP_ERR_CUDA, "no current CUDA context");
+  return FDP_OK;
+}
+
+// Device address of the static state on the current device: looked up with
+// cudaGetSymbolAddress on the first call on the device, and again only when
+// the device's context has changed since (a cudaDeviceReset in between).
 int prev_samples_ptr(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(FDP_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return fail(FDP_ERR_ARG, "device ordinal beyond the supported range");
-  void* p = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_prev_ptr[dev]) {
-      e = cudaGetSymbolAddress(&p, g_prev_samples);
-      if (e == cudaSuccess) g_prev_ptr[dev] = p;
-    }
-    p = g_prev_ptr[dev];
+  std::lock_guard<std::mutex> lk(g_mu);
+  unsigned long long id = 0;
+  int rc = current_context_id(dev, &id);
+  if (rc != FDP_OK) return rc;
+  if (!g_prev_ptr[dev] || g_prev_ctx[dev] != id) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_prev_samples);
+    if (e != cudaSuccess || !p)
+      return fail(FDP_ERR_CUDA, (std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
+    g_prev_ptr[dev] = p;
+    g_prev_ctx[dev] = id;
   }
-  if (!p) return fail(FDP_ERR_CUDA, (std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
-  *out = p;
+  *out = g_prev_ptr[dev];
   return FDP_OK;
 }
 
@@ -111,12 +148,14 @@ int fdp_receivers_noalloc(int32_t precision, const void* um, const void* wm, con
              FDP_NOALLOC_MAX_RECEIVERS);
     return fail(FDP_ERR_ARG, buf);
   }
-  if (mr == 0) return FDP_OK;
-  if (!um || !wm || !qx || !qz || !pres || !txx || !rec || !out) return fail(FDP_ERR_ARG, "null device pointer");
-  if (nx < 1 || nz < 1 || ld < nx || level < 1 || !(dt > 0)) return fail(FDP_ERR_ARG, "bad grid, level or DT");
+  // the address look-up comes first, so that a call with no receivers sets
+  // the device up without launching anything
   void* prev = nullptr;
   int rc = prev_samples_ptr(&prev);
   if (rc != FDP_OK) return rc;
+  if (mr == 0) return FDP_OK;
+  if (!um || !wm || !qx || !qz || !pres || !txx || !rec || !out) return fail(FDP_ERR_ARG, "null device pointer");
+  if (nx < 1 || nz < 1 || ld < nx || level < 1 || !(dt > 0)) return fail(FDP_ERR_ARG, "bad grid, level or DT");
   cudaStream_t s = (cudaStream_t)stream;
   const int threads = 128, blocks = (mr + threads - 1) / threads;
   if (precision == FDP_F64)

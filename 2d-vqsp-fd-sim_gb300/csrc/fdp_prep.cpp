@@ -16,7 +16,7 @@
 
 namespace {
 
-// .MO record column order (read_model_par.F90:147-155)
+// .MO record column order (read_model_par.F90:52-60)
 enum { MU, SXX1, SXX2, SXX3, SZZ1, SZZ2, SZZ3, P1, P2, P3, R1U, R1W, R2U, R2W, R3U, R3W,
        R1QX, R1QZ, R2QX, R2QZ, R3QX, R3QZ, AUXW, AUXQZ };
 
@@ -436,7 +436,7 @@ int fdp_prep_scale_table(int32_t prec, int32_t jmnum, double dt, double h, void*
   auto body = [&](auto* t, auto DT, auto H) {
     for (int j = 0; j < jmnum; ++j) {
       auto* r = t + (size_t)j * 24;
-      // read_model_par.F90:158-169
+      // read_model_par.F90:63-74
       r[R1U] = DT * r[R1U] / H; r[R2U] = DT * r[R2U]; r[R3U] = DT * r[R3U] / H;
       r[R1W] = DT * r[R1W] / H; r[R2W] = DT * r[R2W]; r[R3W] = DT * r[R3W] / H;
       r[R1QX] = DT * r[R1QX] / H; r[R2QX] = DT * r[R2QX] / H; r[R3QX] = DT * r[R3QX];

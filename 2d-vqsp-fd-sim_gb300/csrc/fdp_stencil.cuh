@@ -179,7 +179,7 @@ __device__ __forceinline__ T coef(const Params<T>& p, int k, long long cell, int
 // tests.  The column's values that the z stencils of those rows share are
 // loaded once, into a window of kRZS + 3 (kRZV + 3) registers per field.
 
-// stress: EXX needs 3 <= I <= MX-2 (strain_uw_xx.F90:69); EXZ, EZZ, the
+// stress: EXX needs 3 <= I <= MX-2 (strain_uw_xx.F90:80); EXZ, EZZ, the
 // stresses cover that range
 template <class T>
 __device__ __forceinline__ bool stress_fast_rows(const Params<T>& p, int I, int L0) {
@@ -218,15 +218,15 @@ __device__ __forceinline__ void stress_interior_rows(const Params<T>& p, int I, 
     const T* Ur = U + r * P;
     const T* Wr = W + r * P;
     const T* Xr = X + r * P;
-    // strain_uw_xz.F90:201-204
+    // strain_uw_xz.F90:81-84
     const T exz = p.AH * (u[r + 3] - u[r] + __ldg(Wr + 1) - __ldg(Wr - 2))
                 + p.BH * (u[r + 2] - u[r + 1] + w[r + 1] - __ldg(Wr - 1));
-    // strain_uw_zz.F90:43,49 and strain_q_zz.F90:43,49
+    // strain_uw_zz.F90:51,58-59 and strain_q_zz.F90:48,55-56
     T ezz = (p.CH * (w[r + 2] - w[r + 1]));
     ezz = p.AH * (w[r + 3] - w[r]) + p.BC * ezz;
     T qzz = (p.CH * (z[r + 2] - z[r + 1]));
     qzz = p.AH * (z[r + 3] - z[r]) + p.BC * qzz;
-    // strain_uw_xx.F90:71-72 and strain_q_xx.F90:70-71
+    // strain_uw_xx.F90:82-83 and strain_q_xx.F90:77-78
     const T exx = p.AH * (__ldg(Ur + 2) - __ldg(Ur - 1)) + p.BH * (__ldg(Ur + 1) - u[r + 2]);
     const T qxx = p.AH * (__ldg(Xr + 2) - __ldg(Xr - 1)) + p.BH * (__ldg(Xr + 1) - __ldg(Xr));
     // stress_xz.F90:44-46 and stress_nn.F90:53-59
@@ -348,7 +348,7 @@ template <class T> struct GlobalRdC {
 };
 
 // ---------------------------------------------------------------------------
-// strain_uw_xx.F90:51-94 / strain_q_xx.F90:50-91 for one cell
+// strain_uw_xx.F90:59-107 / strain_q_xx.F90:54-100 for one cell
 template <class T, class R>
 __device__ __forceinline__ T strain_xx(const Params<T>& p, const R& rd, int f, T* ML, T* MH, int I, int L) {
   const int TPML = p.TPML;
@@ -374,7 +374,7 @@ __device__ __forceinline__ T strain_xx(const Params<T>& p, const R& rd, int f, T
   return e;
 }
 
-// strain_uw_zz.F90:41-51 / strain_q_zz.F90:41-52 (interior and non-imaging row 1)
+// strain_uw_zz.F90:48-60 / strain_q_zz.F90:45-58 (interior and non-imaging row 1)
 template <class T, class R>
 __device__ __forceinline__ T strain_zz(const Params<T>& p, const R& rd, int f, int I, int L) {
   T e = (p.CH * (rd(f, I, L + 1) - rd(f, I, L)));
@@ -429,7 +429,7 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
   const T x_m1 = rd(2, I - 1, L), x_0 = rd(2, I, L), x_p1 = rd(2, I + 1, L), x_p2 = rd(2, I + 2, L);
   const T z_m1 = rd(3, I, L - 1), z_0 = rd(3, I, L), z_p1 = rd(3, I, L + 1), z_p2 = rd(3, I, L + 2);
   // exz: the z-PML part (strain_uw_xz_2nd_pml.F90) and the x-PML part of
-  // the side strips (strain_uw_xz.F90:181-196, 209-223 and the PML rows)
+  // the side strips (strain_uw_xz.F90:61-76, 209-223 and the PML rows)
   const bool xz_z = do_xz && !r0 && (pml || last);
   const bool xz_lo = do_xz && !r0 && I <= 2, xz_hi = do_xz && !r0 && I > MX1;
   const int zi = (I - p.PMLL) + (last ? TPML + 1 : L - p.MZ + 1) * p.NX;
@@ -451,7 +451,7 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
   const int zj = (I - p.PMLL) + (mz1 ? 0 : L - p.MZ + 1) * p.NX;
   T me = T(0), mq = T(0), pa = T(0), pd = T(0), pb = T(0), pc = T(0);
   if (zz_pml) { me = p.PZZH[zj]; mq = p.OZZH[zj]; pa = p.ODA_ZH[zj]; pd = p.ODD_ZH[zj]; pb = p.ODB_ZH[zj]; pc = p.ODC_ZH[zj]; }
-  // exx, qxx in the side strips (strain_uw_xx.F90:51-94, strain_q_xx.F90:50-91)
+  // exx, qxx in the side strips (strain_uw_xx.F90:59-107, strain_q_xx.F90:54-100)
   const bool xx_lo = do_nn && I <= 1, xx_hi = do_nn && I >= MX;
   const int xx_xi = xx_lo ? (2 - I) + L * (TPML + 1) : (I - MX1) + L * (TPML + 1);
   const int xx_mi = xx_lo ? (I - p.PMLL) + L * (TPML + 1) : (I - MX) + L * (TPML + 1);
@@ -494,7 +494,7 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
       }
       mz_new = zb * mz + zc * DXZA;
     } else if (xz_lo || xz_hi) {
-      // strain_uw_xz.F90:181-196, 209-223 (and strain_uw_xz_1.F90:62-76)
+      // strain_uw_xz.F90:61-76, 209-223 (and strain_uw_xz_1.F90:62-76)
       const T DZXA = p.CH * (w_0 - w_xm1);
       exz = p.CH * (u_0 - u_m1) + xa * (xd * DZXA + mx);
       mx_new = xb * mx + xc * DZXA;
@@ -502,7 +502,7 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
       // strain_uw_xz_1.F90:79-97 (AFDA_XZ undefined)
       exz = p.AH * (w_xp1 - w_xm2) + p.BH * (w_0 - w_xm1) + p.CH * (u_0 - u_m1);
     } else {
-      // strain_uw_xz.F90:198-206
+      // strain_uw_xz.F90:78-86
       exz = p.AH * (u_p1 - u_m2 + w_xp1 - w_xm2) + p.BH * (u_0 - u_m1 + w_0 - w_xm1);
     }
   }
@@ -525,13 +525,13 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
       qzz = pa * (pd * Dq + mq);
       mq_new = pb * mq + pc * Dq;
     } else {
-      // strain_uw_zz.F90:41-51 / strain_q_zz.F90:41-52
+      // strain_uw_zz.F90:48-60 / strain_q_zz.F90:45-58
       ezz = (p.CH * (w_p1 - w_0));
       if (I >= 2 && I <= MX1) ezz = p.AH * (w_p2 - w_m1) + p.BC * ezz;
       qzz = (p.CH * (z_p1 - z_0));
       if (I >= 2 && I <= MX1) qzz = p.AH * (z_p2 - z_m1) + p.BC * qzz;
     }
-    // strain_uw_xx.F90:51-94 / strain_q_xx.F90:50-91
+    // strain_uw_xx.F90:59-107 / strain_q_xx.F90:54-100
     T exx, qxx;
     if (xx_lo || xx_hi) {
       const T De = p.CH * (u_xp1 - u_0);
@@ -1127,15 +1127,15 @@ __device__ __forceinline__ void stress_core_block(const Params<T>& p, int bx, in
     const long long cell_ = c0 + j;
     const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
     auto C = [&](int k) { return core_coef<T, MODE>(p, k, cell_, J_, bio, 0, j); };
-    // strain_uw_xz.F90:201-204
+    // strain_uw_xz.F90:81-84
     const T exz = p.AH * (up1.v[j] - um2.v[j] + at(wr, j, 1) - at(wr, j, -2))
                 + p.BH * (ur[1].v[j] - um1.v[j] + wr[1].v[j] - at(wr, j, -1));
-    // strain_uw_zz.F90:43,49 and strain_q_zz.F90:43,49
+    // strain_uw_zz.F90:51,58-59 and strain_q_zz.F90:48,55-56
     T ezz = (p.CH * (wp1.v[j] - wr[1].v[j]));
     ezz = p.AH * (wp2.v[j] - wm1.v[j]) + p.BC * ezz;
     T qzz = (p.CH * (zp1.v[j] - z0.v[j]));
     qzz = p.AH * (zp2.v[j] - zm1.v[j]) + p.BC * qzz;
-    // strain_uw_xx.F90:71-72 and strain_q_xx.F90:70-71
+    // strain_uw_xx.F90:82-83 and strain_q_xx.F90:77-78
     const T exx = p.AH * (at(ur, j, 2) - at(ur, j, -1)) + p.BH * (at(ur, j, 1) - ur[1].v[j]);
     const T qxx = p.AH * (at(xr, j, 2) - at(xr, j, -1)) + p.BH * (at(xr, j, 1) - xr[1].v[j]);
     // stress_xz.F90:44-46 and stress_nn.F90:53-59

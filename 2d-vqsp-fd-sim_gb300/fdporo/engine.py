@@ -98,6 +98,13 @@ class Engine:
         ptrs = (C.c_void_p * 24)(*[a.ctypes.data for a in arrs])
         self._check(self.lib.fdp_set_pml(self._ctx, ptrs))
 
+    def set_pml_arrays(self, profiles: list[np.ndarray]) -> None:
+        """The 24 profiles as separate arguments (fdp_set_pml_arrays, the
+        form the Fortran binding uses)."""
+        arrs = [self._real(p) for p in profiles]
+        assert len(arrs) == 24
+        self._check(self.lib.fdp_set_pml_arrays(self._ctx, *[C.c_void_p(a.ctypes.data) for a in arrs]))
+
     def set_bottom_nr(self, ab16: np.ndarray) -> None:
         ab = self._real(ab16).reshape(16)
         self._check(self.lib.fdp_set_bottom_nr(self._ctx, _ptr(ab)))
@@ -116,6 +123,10 @@ class Engine:
     # -- time stepping --------------------------------------------------------
     def time_loop(self, it_begin: int, it_end: int) -> None:
         self._check(self.lib.fdp_run(self._ctx, it_begin, it_end))
+
+    def prepare_run(self, n_levels: int) -> None:
+        """Captures the graphs a run of ``n_levels`` levels replays (fdp_prepare_run)."""
+        self._check(self.lib.fdp_prepare_run(self._ctx, n_levels))
 
     def synchronize(self) -> None:
         self._check(self.lib.fdp_synchronize(self._ctx))

@@ -1,6 +1,6 @@
 """The reference's file formats: writing job directories and reading output.
 
-A job directory as the reference's driver reads it (read_open.F90:48-341,
+A job directory as the reference's driver reads it (read_open.F90:-53-178,
 read_model.F90, read_model_par.F90, open_sr_file.F90):
 ``HF_2DFD_VS_PORO`` (the job name), ``<JOB>.IN`` and ``<JOB>.INM``
 (namelists), ``<JOB>.JMH`` and ``<JOB>.MO`` (gfortran unformatted sequential

@@ -53,13 +53,13 @@ class JobConfig:
     xbmin: float = 0.0
     key_sour: int = 1
     qr: float = 0.0
-    # CONTROLDATA1 defaults (read_open.F90:219-227): default-real literals
+    # CONTROLDATA1 defaults (read_open.F90:118-126): default-real literals
     r: float = _f32(0.001)
     tau: float = 1.5
     pow_: float = 2.0
     sf: float = 0.0
     wc: float = 0.0
-    # NONREF defaults (read_open.F90:275-285)
+    # NONREF defaults (read_open.F90:174-184)
     ktbo: int = 0
     omg: float = 0.0        # NONREF OMG before the division by 2*pi
     wb: float = 0.4
@@ -139,7 +139,7 @@ class Inputs:
 
 
 def source_cell(cfg: JobConfig, h_pp: float) -> tuple[int, int]:
-    """LIN_X, LIN_Z as READ_OPEN computes them (read_open.F90:264-270);
+    """LIN_X, LIN_Z as READ_OPEN computes them (read_open.F90:163-169);
     X_SOURCE, Z_SOURCE and XBMIN are default-real variables there."""
     xs = np.float32(abs(cfg.x_source))
     zs = np.float32(abs(cfg.z_source))
@@ -181,7 +181,7 @@ def prepare(cfg: JobConfig, medium: Medium, precision: str = "f32") -> Inputs:
                              dt, h, cfg.key_sour, pp(cfg.qr), sourtf.ctypes.data_as(C.c_void_p))
     if rc:
         raise FdpError(rc, "fdp_prep_source")
-    # PRE_NR_COEF1 (bottom); OMG = OMG/(2 pi) as read_open.F90:289 does
+    # PRE_NR_COEF1 (bottom); OMG = OMG/(2 pi) as read_open.F90:188 does
     ab = np.zeros(16, dtype=dt_)
     omg = pp(pp(cfg.omg) / 6.283185307179586476925286766559)
     rc = lib.fdp_prep_bottom_nr(prec, mx, mz, tpml, cfg.ktbo, dt, h, omg, pp(cfg.wb), pp(cfg.thpple), pp(cfg.thssle),

@@ -14,8 +14,8 @@ them:
   b = eta / kappa: REL1_U = m/D, REL2_U = rho_f b/D, REL3_U = rho_f/D,
   REL1_Q = rho_f/D, REL2_Q = rho/D, REL3_Q = rho b/D (unscaled; the
   reference multiplies by DT and divides by H after reading,
-  read_model_par.F90:158-169);
-* free-surface row (read_model_par.F90:173-182, the commented derivation):
+  read_model_par.F90:63-74);
+* free-surface row (read_model_par.F90:78-87, the commented derivation):
   AUXIL_W = (lambda_c - (alpha M)**2/M) / (lambda_c + 2 mu - (alpha M)**2/M),
   AUXIL_QZ = 2 mu (alpha M / M) / (lambda_c + 2 mu - (alpha M)**2/M).
 
@@ -28,7 +28,7 @@ from dataclasses import dataclass, replace
 
 import numpy as np
 
-# column order of a .MO record (read_model_par.F90:147-155)
+# column order of a .MO record (read_model_par.F90:52-60)
 MO_COLUMNS = ["MU", "SIG_XX_1", "SIG_XX_2", "SIG_XX_3", "SIG_ZZ_1", "SIG_ZZ_2", "SIG_ZZ_3",
               "PRES_1", "PRES_2", "PRES_3", "REL1_U", "REL1_W", "REL2_U", "REL2_W", "REL3_U", "REL3_W",
               "REL1_QX", "REL1_QZ", "REL2_QX", "REL2_QZ", "REL3_QX", "REL3_QZ", "AUXIL_W", "AUXIL_QZ"]

@@ -69,10 +69,12 @@ SIGNATURES = {
     "fdp_share_medium": (C.c_int, [_VP, _VP]),
     "fdp_diag_wait_timeout": (C.c_int, [_VP, _I32]),
     "fdp_set_pml": (C.c_int, [_VP, C.POINTER(_VP)]),
+    "fdp_set_pml_arrays": (C.c_int, [_VP] + [_VP] * 24),
     "fdp_set_bottom_nr": (C.c_int, [_VP, _VP]),
     "fdp_set_source": (C.c_int, [_VP, _VP, _I32]),
     "fdp_set_receivers": (C.c_int, [_VP, _PI32, _PI32, _PI32, _PI32, _I32, _I32]),
     "fdp_run": (C.c_int, [_VP, _I32, _I32]),
+    "fdp_prepare_run": (C.c_int, [_VP, _I32]),
     "fdp_get_receivers": (C.c_int, [_VP, _I32, _I32, _VP]),
     "fdp_get_snapshot": (C.c_int, [_VP, _I32, _VP]),
     "fdp_field_bounds": (C.c_int, [_VP, _I32, _PI32]),

@@ -2,14 +2,21 @@
 ! Drop-in replacement of SUBROUTINE TIME_LOOP (time_loop.F90:3-209) that
 ! runs the time stepping on a GB300 through the C ABI of include/fdp.h.
 !
-! Build (where gfortran exists; this repository's build does not compile
-! it): add this file to the reference's serial build after mod_*.F90 and
-! link libfdp.so, then call TIME_LOOP_GB300 instead of TIME_LOOP in
-! main.F90:84.  The reference's set-up (READ_OPEN .. PPML) runs unchanged
-! and fills the modules this routine reads.
+! Build (where a Fortran compiler exists; none is installed where this
+! library is built and tested, so this file has not been compiled): add it
+! to the reference's serial build after mod_*.F90 and link libfdp.so, then
+! call TIME_LOOP_GB300 instead of TIME_LOOP in main.F90:84.  The
+! reference's set-up (READ_OPEN .. PPML) runs unchanged and fills the
+! modules this routine reads.
 !=======================================================================
 MODULE FDP_GB300
+  ! Host arrays cross the ABI as assumed-size dummies of the reference's own
+  ! kinds, passed by reference: the module arrays (ALLOCATABLE without
+  ! TARGET, mod_wavefield.F90:19-20, mod_pml.F90:7,17, mod_auxil.F90:33) are
+  ! contiguous, so they are handed over as they are, with no address taken
+  ! and no copy.  Only the context handle is a C_PTR.
   USE ISO_C_BINDING
+  USE PRECISION, ONLY: PP
   IMPLICIT NONE
 
   TYPE, BIND(C) :: FDP_GRID_T
@@ -27,32 +34,37 @@ MODULE FDP_GB300
       TYPE(C_PTR), INTENT(OUT) :: CTX
     END FUNCTION FDP_CREATE
     INTEGER(C_INT) FUNCTION FDP_SET_MEDIUM(CTX, JM, NX, NZ, JMNUM, TABLE24) BIND(C, NAME='fdp_set_medium')
-      IMPORT :: C_INT, C_INT32_T, C_PTR
-      TYPE(C_PTR), VALUE :: CTX, JM, TABLE24
-      INTEGER(C_INT32_T), VALUE :: NX, NZ, JMNUM
-    END FUNCTION FDP_SET_MEDIUM
-    INTEGER(C_INT) FUNCTION FDP_SHARE_MEDIUM(DST, SRC) BIND(C, NAME='fdp_share_medium')
-      IMPORT :: C_INT, C_PTR
-      TYPE(C_PTR), VALUE :: DST, SRC
-    END FUNCTION FDP_SHARE_MEDIUM
-    INTEGER(C_INT) FUNCTION FDP_SET_PML(CTX, PROFILES24) BIND(C, NAME='fdp_set_pml')
-      IMPORT :: C_INT, C_PTR
+      IMPORT :: C_INT, C_INT32_T, C_PTR, PP
       TYPE(C_PTR), VALUE :: CTX
-      TYPE(C_PTR), INTENT(IN) :: PROFILES24(24)
-    END FUNCTION FDP_SET_PML
+      INTEGER(C_INT32_T), DIMENSION(*), INTENT(IN) :: JM
+      INTEGER(C_INT32_T), VALUE :: NX, NZ, JMNUM
+      REAL(PP), DIMENSION(*), INTENT(IN) :: TABLE24
+    END FUNCTION FDP_SET_MEDIUM
+    INTEGER(C_INT) FUNCTION FDP_SET_PML_ARRAYS(CTX, ODA_XL, ODB_XL, ODC_XL, ODD_XL, ODA_XH, ODB_XH, ODC_XH, ODD_XH, &
+        ODA_ZH, ODB_ZH, ODC_ZH, ODD_ZH, ODA2_XL, ODB2_XL, ODC2_XL, ODD2_XL, ODA2_XH, ODB2_XH, ODC2_XH, ODD2_XH, &
+        ODA2_ZH, ODB2_ZH, ODC2_ZH, ODD2_ZH) BIND(C, NAME='fdp_set_pml_arrays')
+      IMPORT :: C_INT, C_PTR, PP
+      TYPE(C_PTR), VALUE :: CTX
+      REAL(PP), DIMENSION(*), INTENT(IN) :: ODA_XL, ODB_XL, ODC_XL, ODD_XL, ODA_XH, ODB_XH, ODC_XH, ODD_XH, &
+        ODA_ZH, ODB_ZH, ODC_ZH, ODD_ZH, ODA2_XL, ODB2_XL, ODC2_XL, ODD2_XL, ODA2_XH, ODB2_XH, ODC2_XH, ODD2_XH, &
+        ODA2_ZH, ODB2_ZH, ODC2_ZH, ODD2_ZH
+    END FUNCTION FDP_SET_PML_ARRAYS
     INTEGER(C_INT) FUNCTION FDP_SET_BOTTOM_NR(CTX, AB16) BIND(C, NAME='fdp_set_bottom_nr')
-      IMPORT :: C_INT, C_PTR
-      TYPE(C_PTR), VALUE :: CTX, AB16
+      IMPORT :: C_INT, C_PTR, PP
+      TYPE(C_PTR), VALUE :: CTX
+      REAL(PP), DIMENSION(16), INTENT(IN) :: AB16
     END FUNCTION FDP_SET_BOTTOM_NR
     INTEGER(C_INT) FUNCTION FDP_SET_SOURCE(CTX, SOURTF, MT2) BIND(C, NAME='fdp_set_source')
-      IMPORT :: C_INT, C_INT32_T, C_PTR
-      TYPE(C_PTR), VALUE :: CTX, SOURTF
+      IMPORT :: C_INT, C_INT32_T, C_PTR, PP
+      TYPE(C_PTR), VALUE :: CTX
+      REAL(PP), DIMENSION(*), INTENT(IN) :: SOURTF
       INTEGER(C_INT32_T), VALUE :: MT2
     END FUNCTION FDP_SET_SOURCE
     INTEGER(C_INT) FUNCTION FDP_SET_RECEIVERS(CTX, IRECX, LRECX, IRECZ, LRECZ, MR, FLAGS) &
         BIND(C, NAME='fdp_set_receivers')
       IMPORT :: C_INT, C_INT32_T, C_PTR
-      TYPE(C_PTR), VALUE :: CTX, IRECX, LRECX, IRECZ, LRECZ
+      TYPE(C_PTR), VALUE :: CTX
+      INTEGER(C_INT32_T), DIMENSION(*), INTENT(IN) :: IRECX, LRECX, IRECZ, LRECZ
       INTEGER(C_INT32_T), VALUE :: MR, FLAGS
     END FUNCTION FDP_SET_RECEIVERS
     INTEGER(C_INT) FUNCTION FDP_RUN(CTX, IT_BEGIN, IT_END) BIND(C, NAME='fdp_run')
@@ -61,14 +73,16 @@ MODULE FDP_GB300
       INTEGER(C_INT32_T), VALUE :: IT_BEGIN, IT_END
     END FUNCTION FDP_RUN
     INTEGER(C_INT) FUNCTION FDP_GET_RECEIVERS(CTX, IT_FIRST, N_LEVELS, HOST) BIND(C, NAME='fdp_get_receivers')
-      IMPORT :: C_INT, C_INT32_T, C_PTR
-      TYPE(C_PTR), VALUE :: CTX, HOST
+      IMPORT :: C_INT, C_INT32_T, C_PTR, PP
+      TYPE(C_PTR), VALUE :: CTX
       INTEGER(C_INT32_T), VALUE :: IT_FIRST, N_LEVELS
+      REAL(PP), DIMENSION(*), INTENT(OUT) :: HOST
     END FUNCTION FDP_GET_RECEIVERS
     INTEGER(C_INT) FUNCTION FDP_GET_SNAPSHOT(CTX, MASK, HOST) BIND(C, NAME='fdp_get_snapshot')
-      IMPORT :: C_INT, C_INT32_T, C_PTR
-      TYPE(C_PTR), VALUE :: CTX, HOST
+      IMPORT :: C_INT, C_INT32_T, C_PTR, PP
+      TYPE(C_PTR), VALUE :: CTX
       INTEGER(C_INT32_T), VALUE :: MASK
+      REAL(PP), DIMENSION(*), INTENT(OUT) :: HOST
     END FUNCTION FDP_GET_SNAPSHOT
     TYPE(C_PTR) FUNCTION FDP_LAST_ERROR(CTX) BIND(C, NAME='fdp_last_error')
       IMPORT :: C_PTR
@@ -120,10 +134,9 @@ CONTAINS
     INTEGER, PARAMETER :: NCHUNK = 500
     TYPE(FDP_GRID_T) :: G
     TYPE(C_PTR) :: CTX
-    TYPE(C_PTR), TARGET :: PROF(24)
-    REAL(PP), ALLOCATABLE, TARGET :: TAB(:,:), REC(:,:,:)
-    REAL(PP), TARGET :: AB(16)
-    INTEGER(C_INT32_T), ALLOCATABLE, TARGET :: JMC(:,:), IRX(:), LRX(:), IRZ(:), LRZ(:)
+    REAL(PP), ALLOCATABLE :: TAB(:,:), REC(:,:,:)
+    REAL(PP) :: AB(16)
+    INTEGER(C_INT32_T), ALLOCATABLE :: JMC(:,:), IRX(:), LRX(:), IRZ(:), LRZ(:)
     INTEGER :: IT0, IT1, N, K, J, FLAGS
     LOGICAL :: EX
 
@@ -134,30 +147,27 @@ CONTAINS
     G%H = H; G%DT = DT; G%TAU_EPS = TAU_EPS
     CALL FDP_CHECK(FDP_CREATE(G, CTX), C_NULL_PTR, 'fdp_create')
 
-    ! medium (read_model.F90, read_model_par.F90): JM and the table in .MO record order
+    ! medium (read_model.F90, read_model_par.F90): JM as 32-bit integers and
+    ! the table in .MO record order
     ALLOCATE (JMC(PMLL:PMLXH, 0:PMLZH), TAB(24, JMNUM))
-    JMC = JM
+    JMC = INT(JM, C_INT32_T)
     TAB( 1,:) = MU;       TAB( 2,:) = SIG_XX_1; TAB( 3,:) = SIG_XX_2; TAB( 4,:) = SIG_XX_3
     TAB( 5,:) = SIG_ZZ_1; TAB( 6,:) = SIG_ZZ_2; TAB( 7,:) = SIG_ZZ_3; TAB( 8,:) = PRES_1
     TAB( 9,:) = PRES_2;   TAB(10,:) = PRES_3;   TAB(11,:) = REL1_U;   TAB(12,:) = REL1_W
     TAB(13,:) = REL2_U;   TAB(14,:) = REL2_W;   TAB(15,:) = REL3_U;   TAB(16,:) = REL3_W
     TAB(17,:) = REL1_QX;  TAB(18,:) = REL1_QZ;  TAB(19,:) = REL2_QX;  TAB(20,:) = REL2_QZ
     TAB(21,:) = REL3_QX;  TAB(22,:) = REL3_QZ;  TAB(23,:) = AUXIL_W;  TAB(24,:) = AUXIL_QZ
-    CALL FDP_CHECK(FDP_SET_MEDIUM(CTX, C_LOC(JMC), PMLXH-PMLL+1, PMLZH+1, JMNUM, C_LOC(TAB)), CTX, 'fdp_set_medium')
+    CALL FDP_CHECK(FDP_SET_MEDIUM(CTX, JMC, PMLXH-PMLL+1, PMLZH+1, JMNUM, TAB), CTX, 'fdp_set_medium')
 
-    ! PPML profiles (ppml.F90:60-83), in the ABI's order
-    PROF = [C_LOC(ODA_XL), C_LOC(ODB_XL), C_LOC(ODC_XL), C_LOC(ODD_XL), &
-            C_LOC(ODA_XH), C_LOC(ODB_XH), C_LOC(ODC_XH), C_LOC(ODD_XH), &
-            C_LOC(ODA_ZH), C_LOC(ODB_ZH), C_LOC(ODC_ZH), C_LOC(ODD_ZH), &
-            C_LOC(ODA2_XL), C_LOC(ODB2_XL), C_LOC(ODC2_XL), C_LOC(ODD2_XL), &
-            C_LOC(ODA2_XH), C_LOC(ODB2_XH), C_LOC(ODC2_XH), C_LOC(ODD2_XH), &
-            C_LOC(ODA2_ZH), C_LOC(ODB2_ZH), C_LOC(ODC2_ZH), C_LOC(ODD2_ZH)]
-    CALL FDP_CHECK(FDP_SET_PML(CTX, PROF), CTX, 'fdp_set_pml')
+    ! PPML profiles (ppml.F90:60-83): the module arrays themselves
+    CALL FDP_CHECK(FDP_SET_PML_ARRAYS(CTX, ODA_XL, ODB_XL, ODC_XL, ODD_XL, ODA_XH, ODB_XH, ODC_XH, ODD_XH, &
+                   ODA_ZH, ODB_ZH, ODC_ZH, ODD_ZH, ODA2_XL, ODB2_XL, ODC2_XL, ODD2_XL, &
+                   ODA2_XH, ODB2_XH, ODC2_XH, ODD2_XH, ODA2_ZH, ODB2_ZH, ODC2_ZH, ODD2_ZH), CTX, 'fdp_set_pml_arrays')
 
     AB = [ABW01, ABW02, ABW10, ABW11, ABW12, ABW20, ABW21, ABW22, &
           ABH01, ABH02, ABH10, ABH11, ABH12, ABH20, ABH21, ABH22]
-    CALL FDP_CHECK(FDP_SET_BOTTOM_NR(CTX, C_LOC(AB)), CTX, 'fdp_set_bottom_nr')
-    CALL FDP_CHECK(FDP_SET_SOURCE(CTX, C_LOC(SOURTF_A), MT2), CTX, 'fdp_set_source')
+    CALL FDP_CHECK(FDP_SET_BOTTOM_NR(CTX, AB), CTX, 'fdp_set_bottom_nr')
+    CALL FDP_CHECK(FDP_SET_SOURCE(CTX, SOURTF_A, MT2), CTX, 'fdp_set_source')
 
     FLAGS = 0
     IF (KEY_TLV) FLAGS = IOR(FLAGS, FDP_REC_TLV)
@@ -166,7 +176,7 @@ CONTAINS
     IF (KEY_TLV .OR. KEY_TLP) THEN
       ALLOCATE (IRX(MR), LRX(MR), IRZ(MR), LRZ(MR), REC(10, MR, NCHUNK))
       IRX = IRECX; LRX = LRECX; IRZ = IRECZ; LRZ = LRECZ
-      CALL FDP_CHECK(FDP_SET_RECEIVERS(CTX, C_LOC(IRX), C_LOC(LRX), C_LOC(IRZ), C_LOC(LRZ), MR, FLAGS), &
+      CALL FDP_CHECK(FDP_SET_RECEIVERS(CTX, IRX, LRX, IRZ, LRZ, MR, FLAGS), &
                      CTX, 'fdp_set_receivers')
     END IF
 
@@ -184,7 +194,7 @@ CONTAINS
       CALL FDP_CHECK(FDP_RUN(CTX, IT0, IT1), CTX, 'fdp_run')
       N = IT1 - IT0 + 1
       IF (KEY_TLV .OR. KEY_TLP) THEN
-        CALL FDP_CHECK(FDP_GET_RECEIVERS(CTX, IT0, N, C_LOC(REC)), CTX, 'fdp_get_receivers')
+        CALL FDP_CHECK(FDP_GET_RECEIVERS(CTX, IT0, N, REC), CTX, 'fdp_get_receivers')
         DO K = 1, N
           DO J = 1, MR                              ! store_seismograms.F90:140-154
             IF (KEY_TLV) THEN
@@ -207,11 +217,11 @@ CONTAINS
       END IF
       IF (KEY_SNV .AND. MOD(IT1, IPAS2) == 0) THEN
         ! copy the wavefield into the module arrays and let the reference write it
-        CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_UM, C_LOC(UM)), CTX, 'fdp_get_snapshot')
-        CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_WM, C_LOC(WM)), CTX, 'fdp_get_snapshot')
+        CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_UM, UM), CTX, 'fdp_get_snapshot')
+        CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_WM, WM), CTX, 'fdp_get_snapshot')
         IF (KEY_TLQ) THEN
-          CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_QX, C_LOC(QX)), CTX, 'fdp_get_snapshot')
-          CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_QZ, C_LOC(QZ)), CTX, 'fdp_get_snapshot')
+          CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_QX, QX), CTX, 'fdp_get_snapshot')
+          CALL FDP_CHECK(FDP_GET_SNAPSHOT(CTX, FDP_SNAP_QZ, QZ), CTX, 'fdp_get_snapshot')
         END IF
         ITILE = IT1
         CALL STORE_SNAPSHOTS(IT1)

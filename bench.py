@@ -191,17 +191,48 @@ def ncu_traffic(kernel: str) -> float | None:
         return None
 
 
-def cpu_time_levels(inp, levels: int, warmup: int, threads: int) -> float:
-    """Seconds for ``levels`` time levels of the oracle (after ``warmup``)."""
+def cpu_time_levels(inp, levels: int, warmup: int, threads: int, ascii_io: bool = False) -> tuple[float, int]:
+    """Seconds for ``levels`` time levels of the oracle (after ``warmup``),
+    and the receiver files opened.  With ``ascii_io`` every level is followed
+    by the reference's receiver output (store_seismograms.F90:140-154,
+    store_seismograms_pressure.F90:76-83): per receiver an OPEN with
+    POSITION='APPEND', one E13.6 line and a CLOSE of each of its two or three
+    files, here into a temporary directory."""
+    import tempfile
+
     from oracle.oracle import make_oracle
     o = make_oracle(inp, threads=threads)
     if warmup:
         o.time_loop(1, warmup)
-    t = time.perf_counter()
-    o.time_loop(warmup + 1, warmup + levels)
-    el = time.perf_counter() - t
+    opened = 0
+    with tempfile.TemporaryDirectory() as d:
+        t = time.perf_counter()
+        if ascii_io:
+            opened = o.time_loop_ascii(warmup + 1, warmup + levels, d)
+        else:
+            o.time_loop(warmup + 1, warmup + levels)
+        el = time.perf_counter() - t
     o.close()
-    return el
+    return el, opened
+
+
+def cpu_baseline_sample(inp, threads: int, seconds: float) -> dict:
+    """The oracle on a bounded sample of the workload: kernel-only levels from
+    rest (about ``seconds`` of work), and fewer levels with the reference's
+    per-level ASCII receiver output."""
+    t1, _ = cpu_time_levels(inp, 2, 0, threads)
+    lv = int(max(2, min(200, seconds / max(t1 / 2, 1e-6))))
+    el, _ = cpu_time_levels(inp, lv, 0, threads)
+    lv_io = max(2, lv // 4)
+    el_io, opened = cpu_time_levels(inp, lv_io, 0, threads, ascii_io=True)
+    return {"value": inp.cells * lv / el / 1e9, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{lv} full-grid time levels from rest ({el:.1f} s; C++ restatement of the reference "
+                      "time loop, OpenMP over rows)",
+            "with_ascii_io": {"value": inp.cells * lv_io / el_io / 1e9, "unit": METRIC, "levels": lv_io,
+                              "seconds": el_io, "files_per_level": opened // lv_io,
+                              "pattern": "after each level, per receiver OPEN(POSITION='APPEND')/WRITE one "
+                                         "E13.6 line/CLOSE of REC_UW_<j>.asc, REC_Q_<j>.asc (KEY_TLQ) and "
+                                         "REC_STRESS_<j>.asc (KEY_TLP), as store_seismograms(_pressure).F90"}}
 
 
 def run_reference(args) -> None:
@@ -210,8 +241,10 @@ def run_reference(args) -> None:
         return
     threads = os.cpu_count() or 1
     inp = prepare_inputs(args.precision, max(WORKLOAD["mt2"], args.warmup + args.steps))
-    el = cpu_time_levels(inp, args.steps, args.warmup, threads)
+    el, _ = cpu_time_levels(inp, args.steps, args.warmup, threads)
     value = inp.cells * args.steps / el / 1e9
+    lv_io = max(2, args.steps // 4)
+    el_io, opened = cpu_time_levels(inp, lv_io, args.warmup, threads, ascii_io=True)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
@@ -221,7 +254,11 @@ def run_reference(args) -> None:
                    "tpml": WORKLOAD["tpml"], "levels_per_shot": WORKLOAD["mt2"], "media": "per-cell"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full-grid time levels after {args.warmup} warm-up levels "
-                                   "(C++ restatement of the reference time loop, OpenMP over rows)"},
+                                   "(C++ restatement of the reference time loop, OpenMP over rows)",
+                         "with_ascii_io": {"value": inp.cells * lv_io / el_io / 1e9, "unit": METRIC,
+                                           "levels": lv_io, "files_per_level": opened // lv_io,
+                                           "pattern": "per level and receiver OPEN(APPEND)/WRITE/CLOSE of its "
+                                                      "seismogram files, as store_seismograms(_pressure).F90"}},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -244,8 +281,10 @@ def run_gpu(args) -> None:
     eng = job.make_engine(inp, device=dev)
     ext = torch.cuda.ExternalStream(eng.stream(), device=dev)
 
-    # ---- warm-up
+    # ---- warm-up; the CUDA graphs of a run of args.steps levels are captured
+    # here, before the clock starts (fdp_run replays them)
     eng.time_loop(1, args.warmup)
+    eng.prepare_run(args.steps)
     eng.synchronize()
     # ---- timed region
     n0 = eng.kernel_launches()
@@ -322,13 +361,7 @@ def run_gpu(args) -> None:
     # ---- CPU baseline on a bounded sample (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        t1 = cpu_time_levels(inp, 2, 0, threads)
-        lv = int(max(2, min(200, args.cpu_seconds / max(t1 / 2, 1e-6))))
-        el = cpu_time_levels(inp, lv, 0, threads)
-        cpu = {"value": inp.cells * lv / el / 1e9, "unit": METRIC, "cores": threads, "kind": "port",
-               "sample": f"{lv} full-grid time levels from rest ({el:.1f} s; C++ restatement of the reference "
-                         "time loop, OpenMP over rows)"}
+        cpu = cpu_baseline_sample(inp, os.cpu_count() or 1, args.cpu_seconds)
 
     if rank != 0:
         return
@@ -341,6 +374,7 @@ def run_gpu(args) -> None:
         "config": {"workload": "layered-grf-2048", "cells": inp.cells, "mx": WORKLOAD["mx"], "mz": WORKLOAD["mz"],
                    "tpml": WORKLOAD["tpml"], "media": "per-cell", "levels_per_shot": WORKLOAD["mt2"],
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"shot replicas x{ws}",
+                   "graphs": "the timed levels replay CUDA graphs captured before the timed region",
                    "shots_per_hour_device": 3600.0 / (step_s * WORKLOAD["mt2"])},
         "gpu_launches": launches,
         "clocks": clk.summary(),

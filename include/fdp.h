@@ -46,9 +46,9 @@ extern "C" {
 #define FDP_F64 8
 
 /* Grid and control data.  Mirrors CONTROL_DATA/AUXIL after READ_OPEN and
- * AUX1 (read_open.F90:245-272, aux1.F90:36-46): mz is the value after the
- * stress-imaging shift MZ=MZ+2 (read_open.F90:250-252) and lin_z the source
- * row after the +2H shift (read_open.F90:266-270). */
+ * AUX1 (read_open.F90:144-171, aux1.F90:36-46): mz is the value after the
+ * stress-imaging shift MZ=MZ+2 (read_open.F90:149-151) and lin_z the source
+ * row after the +2H shift (read_open.F90:165-169). */
 typedef struct fdp_grid {
   int32_t mx, mz;          /* MX, MZ                                          */
   int32_t tpml;            /* TPML, PML thickness in cells                    */
@@ -63,7 +63,7 @@ typedef struct fdp_ctx fdp_ctx;
 
 /* Field identifiers for fdp_get_field / fdp_set_field / fdp_field_bounds.
  * Bounds are those of the reference's arrays (ppml.F90:85-112,
- * tl_alloc.F90:233-245, alloc_nr.F90:33-40). */
+ * tl_alloc.F90:24-36, alloc_nr.F90:33-40). */
 enum fdp_field_id {
   FDP_UM = 0, FDP_WM, FDP_QX, FDP_QZ, FDP_TXX, FDP_TZZ, FDP_TXZ, FDP_PRES,
   FDP_PZXL, FDP_PZXH, FDP_PXXL, FDP_PXXH, FDP_OXXL, FDP_OXXH, FDP_PXZH, FDP_PZZH, FDP_OZZH,
@@ -85,7 +85,7 @@ enum fdp_field_id {
 #define FDP_SNAP_QX (1 << 2)
 #define FDP_SNAP_QZ (1 << 3)
 
-/* Receiver flags for fdp_set_receivers (KEYS namelist, read_open.F90:153). */
+/* Receiver flags for fdp_set_receivers (KEYS namelist, read_open.F90:52). */
 #define FDP_REC_TLV (1 << 0) /* KEY_TLV: u, -w (store_seismograms.F90)        */
 #define FDP_REC_TLQ (1 << 1) /* KEY_TLQ: qx, -qz                              */
 #define FDP_REC_TLP (1 << 2) /* KEY_TLP: p, -txx (store_seismograms_pressure) */
@@ -98,7 +98,7 @@ enum fdp_field_id {
 #define FDP_REC_VALUES 10
 
 /* Creates a context and allocates the device state, zeroed as TL_ALLOC,
- * PPML and ALLOC_NR do (tl_alloc.F90:253-265, ppml.F90:115-153,
+ * PPML and ALLOC_NR do (tl_alloc.F90:44-56, ppml.F90:115-153,
  * alloc_nr.F90:42-54).  Replaces the allocations of TL_ALLOC/PPML/ALLOC_NR.
  * The environment variable FDP_KERNEL_VARIANT, read here, selects the
  * kernels, all bit-identical: unset, the interior ("core") of each phase
@@ -113,11 +113,11 @@ int fdp_create(const fdp_grid* grid, fdp_ctx** out);
 /* Medium: JM(PMLL:PMLXH, 0:PMLZH) (nx = MX+2*TPML, nz = PMLZH+1) after
  * READ_MODEL's row/column replication (read_model.F90:57-89), and the
  * material table as READ_MODEL_PAR holds it after scaling
- * (read_model_par.F90:147-169): table24[(jm-1)*24 + k], k in the .MO record
+ * (read_model_par.F90:52-74): table24[(jm-1)*24 + k], k in the .MO record
  * order MU SIG_XX_1..3 SIG_ZZ_1..3 PRES_1..3 REL1_U REL1_W REL2_U REL2_W
  * REL3_U REL3_W REL1_QX REL1_QZ REL2_QX REL2_QZ REL3_QX REL3_QZ AUXIL_W
  * AUXIL_QZ, REL* already multiplied by DT and divided by H as
- * read_model_par.F90:158-169 does. */
+ * read_model_par.F90:63-74 does. */
 int fdp_set_medium(fdp_ctx* ctx, const int32_t* jm, int32_t nx, int32_t nz, int32_t jmnum,
                    const void* table24);
 
@@ -138,6 +138,18 @@ int fdp_share_medium(fdp_ctx* dst, fdp_ctx* src);
  *   ODA2_ZH ODB2_ZH ODC2_ZH ODD2_ZH                              (0:TPML+1, PMLL:PMLXH) */
 int fdp_set_pml(fdp_ctx* ctx, const void* const* profiles24);
 
+/* The same 24 profiles as separate arguments, in the same order: the form a
+ * Fortran caller binds, passing the PML module's arrays (ALLOCATABLE,
+ * mod_pml.F90:7-15) by reference as assumed-size dummies, since taking
+ * their C address would need the TARGET attribute they lack. */
+int fdp_set_pml_arrays(fdp_ctx* ctx, const void* oda_xl, const void* odb_xl, const void* odc_xl,
+                       const void* odd_xl, const void* oda_xh, const void* odb_xh, const void* odc_xh,
+                       const void* odd_xh, const void* oda_zh, const void* odb_zh, const void* odc_zh,
+                       const void* odd_zh, const void* oda2_xl, const void* odb2_xl, const void* odc2_xl,
+                       const void* odd2_xl, const void* oda2_xh, const void* odb2_xh, const void* odc2_xh,
+                       const void* odd2_xh, const void* oda2_zh, const void* odb2_zh, const void* odc2_zh,
+                       const void* odd2_zh);
+
 /* Bottom non-reflecting coefficients from PRE_NR_COEF1 (pre_nr_coef1.F90:187-202):
  * ABW01 ABW02 ABW10 ABW11 ABW12 ABW20 ABW21 ABW22 ABH01 ... ABH22. */
 int fdp_set_bottom_nr(fdp_ctx* ctx, const void* ab16);
@@ -146,7 +158,7 @@ int fdp_set_bottom_nr(fdp_ctx* ctx, const void* ab16);
  * sourtf[2*(it-1)] = solid part, sourtf[2*(it-1)+1] = fluid part. */
 int fdp_set_source(fdp_ctx* ctx, const void* sourtf, int32_t mt2);
 
-/* Receivers IRECX, LRECX, IRECZ, LRECZ (read_open.F90:326-337) and the
+/* Receivers IRECX, LRECX, IRECZ, LRECZ (read_open.F90:225-236) and the
  * FDP_REC_* flags (KEY_TLV/KEY_TLQ/KEY_TLP).  Replaces the sampling part of
  * STORE_SEISMOGRAMS / STORE_SEISMOGRAMS_PRESSURE. */
 int fdp_set_receivers(fdp_ctx* ctx, const int32_t* irecx, const int32_t* lrecx, const int32_t* irecz,
@@ -154,8 +166,17 @@ int fdp_set_receivers(fdp_ctx* ctx, const int32_t* irecx, const int32_t* lrecx, 
 
 /* Advances time levels it_begin..it_end (1-based, inclusive, it_end <= MT2):
  * the body of DO ITILE = MT1, MT2 (time_loop.F90:65-206) without its file
- * output.  Asynchronous. */
+ * output.  Asynchronous: the levels are replayed from captured CUDA graphs
+ * (see fdp_prepare_run). */
 int fdp_run(fdp_ctx* ctx, int32_t it_begin, int32_t it_end);
+
+/* Captures, without running anything, the CUDA graphs that a run of
+ * n_levels levels replays: fdp_run replays one graph of 32 levels per 32
+ * levels and one graph of the remaining levels, each captured on its first
+ * use (and again after a set_* call changes the device parameters).  A
+ * caller that times its runs, or whose first run must not pay for the
+ * capture, calls this beforehand.  No counterpart in the reference. */
+int fdp_prepare_run(fdp_ctx* ctx, int32_t n_levels);
 
 /* Copies receiver values of levels it_first..it_first+n_levels-1 (already
  * run) to host: n_levels * MR * FDP_REC_VALUES values, level-major.  The
@@ -231,10 +252,9 @@ const char* fdp_last_error(const fdp_ctx* ctx);
 
 /* Receiver sampling that allocates no device memory.  It has no
  * counterpart in the reference.  It serves callers that cannot call
- * cudaMalloc -- a host whose device arrays come from its own memory pool,
- * work recorded inside a CUDA stream capture, or a runtime that forbids
- * allocation once running.  All inputs and outputs are the caller's device
- * memory:
+ * cudaMalloc: a host whose device arrays come from a memory pool it manages
+ * itself, or a runtime that forbids allocation once it is running.  All
+ * inputs and outputs are the caller's device memory:
  *   um wm qx qz pres txx  the wavefield after a completed level, each
  *                         (pmll:pmll+nx-1, 0:nz-1) column-major with leading
  *                         dimension ld elements, in precision `precision`;
@@ -244,13 +264,19 @@ const char* fdp_last_error(const fdp_ctx* ctx);
  * The previous sample of each receiver, which the time derivative needs
  * (store_seismograms.F90:65-66), is kept between calls in one static device
  * array of FDP_NOALLOC_MAX_RECEIVERS entries that every GPU loading the
- * library holds until exit; larger mr is rejected with FDP_ERR_ARG.  A call
- * with level == 1 clears that state (the reference starts it at zero);
- * later levels must follow in order, one call per level.  All calls share
- * the array, so calls that overlap on the GPU race.  The first call on a
- * device looks up the array's device address; make it before any stream
- * capture.  The kernel is enqueued on `stream` (a cudaStream_t, may be 0);
- * errors are returned and described by fdp_last_error(NULL). */
+ * library holds until exit; larger mr is rejected with FDP_ERR_ARG.  The
+ * derivative columns of a call are taken against the samples the previous
+ * call stored.  A call with level == 1 starts from zero samples, as the
+ * reference does; later levels must follow in order, one call per level.  To
+ * start at a level k > 1 (a resumed run), first call it with the wavefield
+ * of level k-1 and discard that call's output: otherwise the first call's
+ * derivative columns use whatever an earlier call left in the array.  All
+ * calls share the array, so calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's device address (and again after a
+ * reset of the device's context); make it before any stream capture.  A
+ * call with mr == 0 only does that look-up and launches nothing.  The
+ * kernel is enqueued on `stream` (a cudaStream_t, may be 0); errors are
+ * returned and described by fdp_last_error(NULL). */
 int fdp_receivers_noalloc(int32_t precision, const void* um, const void* wm, const void* qx, const void* qz,
                           const void* pres, const void* txx, int32_t nx, int32_t nz, int32_t ld, int32_t pmll,
                           const int32_t* rec, int32_t mr, int32_t flags, double dt, int32_t level, void* out,

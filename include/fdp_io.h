@@ -2,9 +2,9 @@
  * fdp_io.h -- the reference's file formats, for hosts without the Fortran
  * driver (the C++ drop-in host fdp_host uses them).
  *
- *   - Fortran namelist input (<JOB>.IN, <JOB>.INM; read_open.F90:149-170)
+ *   - Fortran namelist input (<JOB>.IN, <JOB>.INM; read_open.F90:48-69)
  *   - gfortran unformatted sequential records with 4-byte length markers
- *     (.JMH and .MO, read_model.F90:62, read_model_par.F90:132-155;
+ *     (.JMH and .MO, read_model.F90:62, read_model_par.F90:37-60;
  *     SNAP.V######, store_snapshots.F90:173-190)
  *   - the Ew.d edit descriptor of the seismogram files
  *     ('(5(1X,E13.6))', store_seismograms.F90:144)

@@ -24,7 +24,7 @@ extern "C" {
 int fdp_prep_velocities(int32_t prec, double sig1, double p, double ainv, double mu, double rel1,
                         double rel2, double rel3, double* vpf, double* vps, double* vs);
 
-/* READ_MODEL_PAR scaling (read_model_par.F90:158-169) of a .MO table
+/* READ_MODEL_PAR scaling (read_model_par.F90:63-74) of a .MO table
  * table24[(jm-1)*24+k] in place. */
 int fdp_prep_scale_table(int32_t prec, int32_t jmnum, double dt, double h, void* table24);
 
@@ -35,7 +35,7 @@ int fdp_prep_expand_jm(int32_t mx, int32_t mz, int32_t tpml, int32_t stress_imag
                        int32_t* jm_out);
 
 /* PPML (ppml.F90:156-306): the 24 damping profiles in fdp_set_pml order.
- * r, tau, pow, sf, wc are CONTROLDATA1 values (read_open.F90:155,219-227),
+ * r, tau, pow, sf, wc are CONTROLDATA1 values (read_open.F90:54,118-126),
  * ktbo the bottom condition key. */
 int fdp_prep_pml(int32_t prec, int32_t mx, int32_t mz, int32_t tpml, int32_t ktbo, double r, double tau,
                  double pow_, double sf, double wc, double dt, double h, const int32_t* jm, int32_t jmnum,
@@ -44,7 +44,7 @@ int fdp_prep_pml(int32_t prec, int32_t mx, int32_t mz, int32_t tpml, int32_t ktb
 /* PRE_NR_COEF1 bottom part (pre_nr_coef1.F90:187-202) with NONREF
  * (nonref.F90:69-204), HIGDON_FD, HIGCE_FD, HIGCE2_FD and OptAbsBc:
  * the 16 coefficients ABW01..ABW22, ABH01..ABH22.  omg is the NONREF
- * namelist OMG already divided by 2*pi (read_open.F90:289). */
+ * namelist OMG already divided by 2*pi (read_open.F90:188). */
 int fdp_prep_bottom_nr(int32_t prec, int32_t mx, int32_t mz, int32_t tpml, int32_t ktbo, double dt, double h,
                        double omg, double wb, double thpple, double thssle, const int32_t* jm, int32_t jmnum,
                        const void* table24, void* ab16);

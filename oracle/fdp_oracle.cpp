@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <cstdio>
 #include <stdexcept>
@@ -165,7 +166,7 @@ template <class T> struct Sim {
     PMLL = 1 - TPML; PMLXH = MX + TPML;
     PMLZH = MZ + TPML; PMLZH1 = MZ + TPML - 1; PMLZH2 = MZ + TPML - 2;
     AH = A / H; BH = B / H; CH = T(1) / H;
-    // tl_alloc.F90:233-265
+    // tl_alloc.F90:24-56
     FA2<T>* f[] = {&UM, &WM, &QX, &QZ, &QXP, &QZP, &TXX, &TZZ, &TXZ, &PRES};
     for (auto* a : f) a->alloc(PMLL, PMLXH, 0, PMLZH);
     JM.alloc(PMLL, PMLXH, 0, PMLZH);
@@ -201,7 +202,7 @@ template <class T> struct Sim {
 
   // ================= stress-phase row kernels =========================
 
-  // strain_uw_xz.F90:181-223
+  // strain_uw_xz.F90:61-103
   void strain_uw_xz(Strain<T>& s, int L) {
     const int L1 = L - 1, L2 = L - 2, LP1 = L + 1;
     for (int I = 2 - TPML; I <= 2; ++I) {
@@ -238,7 +239,7 @@ template <class T> struct Sim {
     }
   }
 
-  // strain_uw_zz.F90:33-51 and strain_q_zz.F90:33-52
+  // strain_uw_zz.F90:48-60 and strain_q_zz.F90:45-58
   void strain_zz(FA1<T>& E, FA2<T>& W, int L) {
     const T BC = BH / CH;
     for (int I = 2 - TPML; I <= MX1 + TPML; ++I) E(I) = (CH * (W(I, L + 1) - W(I, L)));
@@ -259,7 +260,7 @@ template <class T> struct Sim {
     }
   }
 
-  // strain_uw_xx.F90:48-94 and strain_q_xx.F90:47-91
+  // strain_uw_xx.F90:59-107 and strain_q_xx.F90:54-100
   void strain_xx(FA1<T>& E, FA2<T>& U, FA2<T>& ML, FA2<T>& MH, int L) {
     for (int I = 2 - TPML; I <= 1; ++I) {
       T DXXA = CH * (U(I + 1, L) - U(I, L));
@@ -443,10 +444,18 @@ template <class T> struct Sim {
   // inh_v_uv_int.F90:36-56
   void inh_v_uv_int(int L) {
     const int IN1 = L - 1, IN2 = L, IN3 = L + 1, IN4 = L + 2;
+#ifdef ORACLE_PLANT_X_SLIP
+    // a deliberate staggered-index slip (the outer x-pair of d(txx)/dx one
+    // cell to the right), built only by the test that checks that the
+    // known-answer tests catch such a mistake
+    const int S = 1;
+#else
+    const int S = 0;
+#endif
     for (int I = 4; I <= MX - 2; ++I) {
       int J = JM(I, L);
       UM(I, L) = UM(I, L) + (REL2_U[J] / REL3_QX[J]) * (T(1) - fexp(-REL3_QX[J])) * QXP(I, L)
-                 + REL1_U[J] * (A * (TXX(I + 1, L) - TXX(I - 2, L) + TXZ(I, IN4) - TXZ(I, IN1))
+                 + REL1_U[J] * (A * (TXX(I + 1 + S, L) - TXX(I - 2 + S, L) + TXZ(I, IN4) - TXZ(I, IN1))
                               + B * (TXX(I, L) - TXX(I - 1, L) + TXZ(I, IN3) - TXZ(I, IN2)))
                  + REL3_U[J] * (A * (PRES(I + 1, L) - PRES(I - 2, L)) + B * (PRES(I, L) - PRES(I - 1, L)));
     }
@@ -1055,7 +1064,7 @@ template <class T> static void set_medium(Sim<T>* s, const int32_t* jm, int jmnu
                               &s->SIG_ZZ_3, &s->PRES_1, &s->PRES_2, &s->PRES_3, &s->REL1_U, &s->REL1_W,
                               &s->REL2_U, &s->REL2_W, &s->REL3_U, &s->REL3_W, &s->REL1_QX, &s->REL1_QZ,
                               &s->REL2_QX, &s->REL2_QZ, &s->REL3_QX, &s->REL3_QZ, &s->AUXIL_W, &s->AUXIL_QZ};
-  // read_model_par.F90:147-155 record order; index 1..JMNUM (slot 0 unused)
+  // read_model_par.F90:52-60 record order; index 1..JMNUM (slot 0 unused)
   for (int c = 0; c < 24; ++c) cols[c]->assign((size_t)jmnum + 1, T(0));
   for (int j = 1; j <= jmnum; ++j)
     for (int c = 0; c < 24; ++c) (*cols[c])[j] = tab[(size_t)(j - 1) * 24 + c];
@@ -1158,6 +1167,70 @@ int orc_run(void* h, int it_begin, int it_end, void* rec_out) {
       }
     }
   });
+}
+
+// E13.6 as gfortran writes it (1X then the field): 0.DDDDDDE+XX, sign
+// and leading zero as the width allows.  Used only to reproduce the cost of
+// the reference's per-level receiver output below.
+static void put_e13_6(FILE* f, double v) {
+  char buf[64], out[32];
+  if (v == 0.0) { std::fputs(std::signbit(v) ? " -0.000000E+00" : "  0.000000E+00", f); return; }
+  std::snprintf(buf, sizeof buf, "%.5e", std::fabs(v));  // D.DDDDDe+XX, 6 significant digits
+  char dig[8];
+  int n = 0;
+  const char* c = buf;
+  for (; *c && *c != 'e'; ++c)
+    if (*c >= '0' && *c <= '9') dig[n++] = *c;
+  dig[n] = 0;
+  const int e10 = std::atoi(c + 1) + 1;
+  std::snprintf(out, sizeof out, "%s0.%sE%c%02d", v < 0 ? "-" : "", dig, e10 < 0 ? '-' : '+', std::abs(e10));
+  std::fprintf(f, " %13s", out);
+}
+
+// Runs levels it_begin..it_end and, after each, writes the receivers the
+// way the reference does (store_seismograms.F90:140-154,
+// store_seismograms_pressure.F90:76-83): per receiver and level, OPEN the
+// receiver's file with POSITION='APPEND', WRITE one line, CLOSE, for
+// REC_UW_<j>.asc, REC_Q_<j>.asc (KEY_TLQ) and REC_STRESS_<j>.asc (KEY_TLP)
+// in directory dir.  Returns the number of files opened, or -1.
+long long orc_run_ascii(void* h, int it_begin, int it_end, const char* dir, int tlv, int tlq, int tlp) {
+  Handle* hd = (Handle*)h;
+  long long opened = 0;
+  auto run = [&](auto* sim, auto zero) {
+    using T = decltype(zero);
+    const int mr = sim->MR;
+    std::vector<T> rec((size_t)std::max(mr, 1) * 10);
+    std::string path;
+    auto line = [&](const char* stem, int j, double t, const T* v, int nv) {
+      path = std::string(dir) + "/" + stem + std::to_string(j) + ".asc";
+      FILE* f = std::fopen(path.c_str(), "a");
+      if (!f) throw std::runtime_error("cannot open " + path);
+      put_e13_6(f, t);
+      for (int k = 0; k < nv; ++k) put_e13_6(f, (double)v[k]);
+      std::fputc('\n', f);
+      std::fclose(f);
+      ++opened;
+    };
+    for (int it = it_begin; it <= it_end; ++it) {
+      sim->step(it, rec.data());
+      const double t = (double)(sim->DT * (T)it);  // DT*(T) in the working precision
+      for (int j = 0; j < mr; ++j) {
+        const T* r = rec.data() + (size_t)j * 10;
+        if (tlv) {
+          line("REC_UW_", j + 1, t, r, 4);
+          if (tlq) line("REC_Q_", j + 1, t, r + 4, 4);
+        }
+        if (tlp) line("REC_STRESS_", j + 1, t, r + 8, 2);
+      }
+    }
+  };
+  try {
+    if (hd->f) run(hd->f, 0.0f); else run(hd->d, 0.0);
+  } catch (const std::exception& e) {
+    hd->err = e.what();
+    return -1;
+  }
+  return opened;
 }
 
 int orc_field_bounds(void* h, int id, int* b4) {

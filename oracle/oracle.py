@@ -23,6 +23,9 @@ SRC = ORACLE_DIR / "fdp_oracle.cpp"
 BUILD_DIR = ORACLE_DIR / "_build"
 LIB_CHECKED = BUILD_DIR / "liboracle_fdp.so"      # bounds-checked, single thread
 LIB_OMP = BUILD_DIR / "liboracle_fdp_omp.so"      # unchecked, OpenMP over rows
+# bounds-checked, with a deliberate x-index slip in the u update: only the
+# test showing that the known-answer tests catch such a slip loads it
+LIB_PLANTED = BUILD_DIR / "liboracle_fdp_planted.so"
 
 FIELD_NAMES = [
     "UM", "WM", "QX", "QZ", "TXX", "TZZ", "TXZ", "PRES",
@@ -36,10 +39,13 @@ FIELD_ID = {n: i for i, n in enumerate(FIELD_NAMES)}
 _FLAGS = ["-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
-def build(force: bool = False) -> None:
-    """Compiles both oracle libraries if missing or older than the source."""
+def build(force: bool = False, planted: bool = False) -> None:
+    """Compiles both oracle libraries (and, with ``planted``, the variant
+    with a planted index slip) if missing or older than the source."""
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     jobs = [(LIB_CHECKED, ["-O2", "-DORACLE_CHECK"]), (LIB_OMP, ["-O3", "-fopenmp"])]
+    if planted:
+        jobs.append((LIB_PLANTED, ["-O2", "-DORACLE_CHECK", "-DORACLE_PLANT_X_SLIP"]))
     procs = []
     for lib, extra in jobs:
         if force or not lib.exists() or lib.stat().st_mtime < SRC.stat().st_mtime:
@@ -60,8 +66,8 @@ _libs: dict[str, C.CDLL] = {}
 def _load(which: str = "checked") -> C.CDLL:
     if which in _libs:
         return _libs[which]
-    build()
-    lib = C.CDLL(str(LIB_CHECKED if which == "checked" else LIB_OMP))
+    build(planted=which == "planted")
+    lib = C.CDLL(str({"checked": LIB_CHECKED, "omp": LIB_OMP, "planted": LIB_PLANTED}[which]))
     vp, i32, d = C.c_void_p, C.c_int32, C.c_double
     pi32 = C.POINTER(C.c_int32)
     lib.orc_create.restype = vp
@@ -78,6 +84,8 @@ def _load(which: str = "checked") -> C.CDLL:
     lib.orc_run.argtypes = [vp, C.c_int, C.c_int, vp]
     lib.orc_field_bounds.argtypes = [vp, C.c_int, pi32]
     lib.orc_field.argtypes = [vp, C.c_int, vp, C.c_int]
+    lib.orc_run_ascii.restype = C.c_longlong
+    lib.orc_run_ascii.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int]
     for fn in ("orc_set_medium", "orc_set_profiles", "orc_set_bottom_nr", "orc_set_source", "orc_set_receivers",
                "orc_run", "orc_field_bounds", "orc_field", "orc_set_threads"):
         getattr(lib, fn).restype = C.c_int
@@ -89,8 +97,8 @@ class Oracle:
     """CPU restatement with the interface of ``fdporo.engine.Engine``."""
 
     def __init__(self, mx, mz, tpml, lin_x, lin_z, h, dt, precision="f32", stress_imaging=True, tau_eps=0.0,
-                 threads: int = 0):
-        which = "omp" if threads else "checked"
+                 threads: int = 0, planted: bool = False):
+        which = "planted" if planted else ("omp" if threads else "checked")
         self.lib = _load(which)
         self.prec = 8 if precision in ("f64", 8) else 4
         self.dtype = np.float64 if self.prec == 8 else np.float32
@@ -160,6 +168,17 @@ class Oracle:
         for k in range(n):
             self._raw[it_begin + k] = rec[k, : self.mr].copy()
 
+    def time_loop_ascii(self, it_begin, it_end, directory) -> int:
+        """Levels it_begin..it_end followed, each, by the reference's receiver
+        output: per receiver an OPEN/WRITE/CLOSE of REC_UW_<j>.asc, REC_Q_<j>.asc
+        (KEY_TLQ) and REC_STRESS_<j>.asc (KEY_TLP) in ``directory``.  Returns
+        the number of files opened."""
+        n = self.lib.orc_run_ascii(self._h, it_begin, it_end, str(directory).encode(), int(bool(self.rec_flags & 1)),
+                                   int(bool(self.rec_flags & 2)), int(bool(self.rec_flags & 4)))
+        if n < 0:
+            raise RuntimeError("oracle: " + self.lib.orc_error(self._h).decode())
+        return int(n)
+
     def synchronize(self):
         pass
 
@@ -191,11 +210,13 @@ class Oracle:
         self._check(self.lib.orc_field(self._h, FIELD_ID[name], v.ctypes.data_as(C.c_void_p), 1))
 
 
-def make_oracle(inp, threads: int = 0) -> Oracle:
-    """An oracle loaded with the same prepared inputs as a GPU engine."""
+def make_oracle(inp, threads: int = 0, planted: bool = False) -> Oracle:
+    """An oracle loaded with the same prepared inputs as a GPU engine
+    (``planted``: the variant with a deliberate index slip, for the test
+    that shows the known-answer tests catch one)."""
     o = Oracle(inp.mx, inp.mz, inp.tpml, inp.lin_x, inp.lin_z, inp.h, inp.dt,
                precision="f64" if inp.precision == 8 else "f32", stress_imaging=inp.stress_imaging,
-               threads=threads)
+               threads=threads, planted=planted)
     o.set_medium(inp.jm, inp.table)
     o.set_pml(inp.profiles)
     o.set_bottom_nr(inp.ab)

@@ -4,7 +4,7 @@ Restates, for checking the product's C++ set-up code (include/fdp_prep.h),
 the reference routines that run once before TIME_LOOP:
   CALCUL_VELOCITY  calcul_velocity.F90:16-36
   READ_MODEL       read_model.F90:57-89 (serial build)
-  READ_MODEL_PAR   read_model_par.F90:158-169 (scaling)
+  READ_MODEL_PAR   read_model_par.F90:63-74 (scaling)
   PPML             ppml.F90:156-306
   PRE_NR_COEF1     pre_nr_coef1.F90:187-202, NONREF nonref.F90:69-204,
                    HIGDON_FD, HIGCE_FD, HIGCE2_FD, OptAbsBc

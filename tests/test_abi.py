@@ -75,3 +75,28 @@ def test_engine_raises_without_gpu():
     from fdporo import Engine, FdpError
     with pytest.raises(FdpError):
         Engine(32, 24, 4, 16, 10, 1.0, 1e-4)
+
+
+def test_errors_without_a_context_are_per_thread(fdp_lib):
+    """fdp_last_error(NULL) reports the calling thread's own last failure:
+    two threads failing at once each read their own message."""
+    import threading
+    bar = threading.Barrier(2)
+    seen = {}
+
+    def worker(tag, bad):
+        ctx = C.c_void_p()
+        bar.wait()
+        for _ in range(200):
+            rc = fdp_lib.fdp_create(C.byref(_grid(**bad)), C.byref(ctx))
+            assert rc == -1
+            seen.setdefault(tag, set()).add(fdp_lib.fdp_last_error(None))
+
+    ts = [threading.Thread(target=worker, args=("precision", dict(precision=2))),
+          threading.Thread(target=worker, args=("h", dict(h=0.0)))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert len(seen["precision"]) == 1 and len(seen["h"]) == 1
+    assert seen["precision"] != seen["h"]

@@ -89,3 +89,22 @@ def test_job_directory_round_trip(tmp_path):
     assert np.frombuffer(formats.read_record(d / "TEST.MO", 0), np.int32)[0] == med.jmnum
     tab = np.frombuffer(formats.read_record(d / "TEST.MO", 1), np.float32).reshape(-1, 24)
     np.testing.assert_array_equal(tab, med.table.astype(np.float32))
+
+
+def test_oracle_ascii_output_matches_the_writer(tmp_path):
+    """The CPU baseline's per-level receiver output (the reference's
+    OPEN/WRITE/CLOSE per receiver and level) writes the same lines as the
+    drop-in host's seismogram writer."""
+    from helpers import small_job
+    from oracle.oracle import make_oracle
+    cfg, med = small_job(nsteps=15, seed=12, n_rec=4)
+    inp = job.prepare(cfg, med, "f32")
+    a, b = make_oracle(inp), make_oracle(inp)
+    opened = a.time_loop_ascii(1, 15, tmp_path)
+    b.time_loop(1, 15)
+    rec = b.receivers(1, 15)
+    assert opened == 15 * 4 * 3
+    for j in range(4):
+        for stem, cols in (("REC_UW_", [0, 1, 2, 3]), ("REC_Q_", [4, 5, 6, 7]), ("REC_STRESS_", [8, 9])):
+            text = (tmp_path / f"{stem}{j + 1}.asc").read_text().splitlines()
+            assert text == formats.seismogram_lines(rec[:, j, :], inp.dt, 1, cols), (stem, j)

@@ -5,8 +5,8 @@
   whole shot, bit for bit against the oracle (OpenMP build), every field,
   memory variable and receiver value.
 * The layered 2048 x 2048 case (per-cell Gaussian-random-field Biot medium,
-  free surface, 512 receivers): the full grid for 200 levels in FP32, bit
-  for bit against the oracle.
+  free surface, 512 receivers): the full grid for 200 levels in FP32 and
+  for 100 levels in FP64, bit for bit against the oracle.
 * The FP32 error of the small case's seismograms against FP64 stays within
   the 1e-3 relative L2 the FP32 mode is held to.
 """
@@ -60,3 +60,20 @@ def test_layered_2048_full_grid_fp32():
     orc.time_loop(1, 200)
     compare_state(eng, orc)
     np.testing.assert_array_equal(eng.receivers(1, 200), orc.receivers(1, 200))
+
+
+def test_layered_2048_full_grid_fp64():
+    # the same full grid in the reference's working precision REAL(8), whose
+    # per-cell planes and FP64 core kernels (two CTAs of 128 registers per
+    # SM) differ from the FP32 path: 100 levels, bit for bit
+    from fdporo import job
+    from oracle.oracle import make_oracle
+    cfg, med = job.layered(mx=2048, mz=2048, nsteps=100)
+    inp = job.prepare(cfg, med, "f64")
+    eng, orc = job.make_engine(inp), make_oracle(inp, threads=THREADS)
+    assert eng.medium_info()["mode"] == "biot"
+    eng.time_loop(1, 100)
+    orc.time_loop(1, 100)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 100), orc.receivers(1, 100))
+    assert np.abs(orc.field("PRES")).max() > 0

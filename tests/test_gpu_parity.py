@@ -50,7 +50,7 @@ def test_one_step_from_random_state(prec, si):
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("si", [True, False])
 def test_shot_from_rest(prec, si):
-    # 80 levels: two graph replays of 32 levels plus 16 direct levels
+    # 80 levels: two graph replays of 32 levels plus one graph of 16 levels
     cfg, med = small_job(si=si, nsteps=80, seed=5)
     inp, eng, orc = _pair(cfg, med, prec)
     eng.time_loop(1, 80)
@@ -115,11 +115,24 @@ def test_snapshot_matches_fields():
         np.testing.assert_array_equal(snap[k], eng.field(n))
 
 
-def test_kernel_launch_count():
-    cfg, med = small_job(nsteps=70, seed=31)
+def test_kernel_launch_count(kernel_variant):
+    """Exact launches of a 70-level run, replayed as captured runs of 32, 32
+    and 6 levels, each ending with a level-counter update, after one
+    level-counter reset.  The frame/core split (also with TMA-staged cores)
+    launches a frame and a core kernel per phase and level, with the row-1
+    and receiver step folded into the next level's stress frame kernel and
+    one k_edge for the last level of each run; the other variants one kernel
+    per phase and a k_edge per level."""
+    cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=70, seed=31)
     inp, eng, _ = _pair(cfg, med, "f32")
     n0 = eng.kernel_launches()
     eng.time_loop(1, 70)
     eng.synchronize()
-    # three kernels per level plus the level-counter updates
-    assert eng.kernel_launches() - n0 >= 3 * 70
+    runs = 3
+    if kernel_variant in ("core", "coretma"):
+        core = eng.core_info()
+        assert all(x1 > x0 and z1 > z0 for x0, x1, z0, z1 in core.values())
+        expected = 70 * 4 + runs * 2 + 1
+    else:
+        expected = 70 * 3 + runs + 1
+    assert eng.kernel_launches() - n0 == expected

@@ -3,7 +3,8 @@
 Inside a run of levels the engine folds each level's row-1 and receiver
 step into the next level's stress frame kernel (and the stress samples into
 the level's velocity frame kernel), and ends every run -- a 32-level graph
-replay or the levels launched one by one after it -- with its own k_edge.
+replay or the graph of the levels left after the last one -- with its own
+k_edge.
 Splitting a shot into runs of 1, 2, 31, 32, 33 ... levels, reading the
 receivers and the state between runs, must give the oracle's values bit for
 bit at every split, with and without stress imaging and receivers.
@@ -50,3 +51,25 @@ def test_one_long_run_equals_split_runs():
         split.time_loop(a, b)
     compare_state(whole, split)
     np.testing.assert_array_equal(whole.receivers(1, 100), split.receivers(1, 100))
+
+
+def test_prepared_graphs_give_the_same_levels():
+    """fdp_prepare_run captures the graphs of a run length ahead of the run;
+    the prepared run, later runs of the same length (graph replays of an
+    already captured graph) and the oracle agree bit for bit, and preparing
+    launches nothing."""
+    from fdporo import job
+    from oracle.oracle import make_oracle
+    cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=100, si=True, per_cell=True, seed=84, n_rec=7)
+    inp = job.prepare(cfg, med, "f32")
+    eng, orc = job.make_engine(inp), make_oracle(inp)
+    randomize_state([eng, orc], inp, seed=85)
+    n0 = eng.kernel_launches()
+    eng.prepare_run(20)
+    eng.prepare_run(52)
+    assert eng.kernel_launches() == n0
+    for a, b in ((1, 20), (21, 40), (41, 92), (93, 100)):
+        eng.time_loop(a, b)
+    orc.time_loop(1, 100)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 100), orc.receivers(1, 100))
