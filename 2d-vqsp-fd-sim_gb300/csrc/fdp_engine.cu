@@ -482,6 +482,8 @@ template <class T> int run_graph(fdp_ctx* c, const Params<T>& p, int n, cudaGrap
       c->graph[n] = nullptr;
       return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
+    // moves the graph's device-side set-up out of its first launch
+    CK(c, cudaGraphUpload(c->graph[n], c->stream));
   }
   *out = c->graph[n];
   return FDP_OK;

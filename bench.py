@@ -329,16 +329,28 @@ def run_gpu(args) -> None:
         t = time.perf_counter()
         e = Engine(inp.mx, inp.mz, inp.tpml, inp.lin_x, inp.lin_z, inp.h, inp.dt, precision=args.precision,
                    stress_imaging=inp.stress_imaging, device=dev)
-        job.load_inputs(e, inp)
+        t_create = time.perf_counter()
+        e.set_medium(inp.jm, inp.table)
+        t_medium = time.perf_counter()
+        e.set_pml(inp.profiles)
+        e.set_bottom_nr(inp.ab)
+        e.set_source(inp.sourtf)
+        e.set_receivers(inp.irecx, inp.lrecx, inp.irecz, inp.lrecz, inp.rec_flags)
+        t_set = time.perf_counter()
         e.time_loop(1, WORKLOAD["mt2"])
+        e.synchronize()
+        t_run = time.perf_counter()
         rec = e.receivers(1, WORKLOAD["mt2"])
         el = time.perf_counter() - t
+        breakdown = {"create_s": t_create - t, "set_medium_s": t_medium - t_create,
+                     "set_pml_bottom_source_receivers_s": t_set - t_medium, "levels_s": t_run - t_set,
+                     "receivers_s": t + el - t_run}
         e.close()
         h2d = (inp.jm.nbytes + inp.table.nbytes + sum(p.nbytes for p in inp.profiles) + inp.ab.nbytes
                + inp.sourtf[: WORKLOAD["mt2"]].nbytes + 16 * len(inp.irecx))
         e2e = {"value": inp.cells * WORKLOAD["mt2"] * ws / _barrier_max(el, ws) / 1e9, "unit": METRIC,
                "h2d_bytes_per_step": h2d // WORKLOAD["mt2"], "d2h_bytes_per_step": rec.nbytes // WORKLOAD["mt2"],
-               "shot_seconds": el, "shots_per_hour": 3600.0 / el,
+               "shot_seconds": el, "shots_per_hour": 3600.0 / el, "breakdown": breakdown,
                "scope": f"one whole shot of {WORKLOAD['mt2']} levels: fdp_create, fdp_set_* from host buffers, "
                         "fdp_run, fdp_get_receivers"}
 
@@ -357,6 +369,11 @@ def run_gpu(args) -> None:
         accuracy = {"seismogram_rel_l2": float(np.linalg.norm(diff) / np.linalg.norm(ref)),
                     "against": "FP64 engine over the same whole shot (u, -w, p, -txx at all receivers and levels)",
                     "target": 1e-3}
+
+    # ---- batched shots against the same shots one by one (rank 0, N = 1)
+    batch = None
+    if rank == 0 and ws == 1 and not args.no_batch:
+        batch = batch_leg(dev)
 
     # ---- CPU baseline on a bounded sample (rank 0, N = 1 only)
     cpu = None
@@ -387,6 +404,7 @@ def run_gpu(args) -> None:
                      "core_cells": alg.get("core_cells"), "medium": medium, "phase_share": shares},
         "e2e": e2e,
         "accuracy": accuracy,
+        "batch": batch,
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
@@ -424,6 +442,7 @@ def plain_fp64_comparison(shots, dev: int, levels: int = 10) -> dict:
         for item, inp in zip(shots, pool.map(_prepare_batch_shot_f64, shots)):
             e = job.make_engine(inp, device=dev)
             e.time_loop(1, 3)
+            e.prepare_run(levels)
             s = torch.cuda.ExternalStream(e.stream(), device=dev)
             e0.record(s)
             e.time_loop(4, 3 + levels)
@@ -446,6 +465,72 @@ def plain_fp64_comparison(shots, dev: int, levels: int = 10) -> dict:
     err = float(np.linalg.norm(recs[0] - recs[1]) / max(np.linalg.norm(recs[1]), 1e-300))
     return {"ms_per_level": ms, "levels_timed_per_shot": levels, "cells_per_level": sum(cells),
             "fp32_seismogram_rel_l2_vs_fp64": err, "error_shot_cells": small[1]}
+
+
+def batch_leg(dev: int, levels: int = 32) -> dict:
+    """The batched-shots comparison, bounded, for the default run: the 64
+    shots of the batch workload (sides 512..2048, per-shot media, 20-cell
+    PML, FP32) advanced together by fdp_batch over `levels` timed levels
+    after the batch tuned its shape on 50 levels, against the same shots one
+    after another through fdp_run in FP32 and in FP64 (the reference's
+    working precision), with the FP32 seismogram error against FP64 over
+    the whole run of the smallest shot.  shots/hour are for BATCH['mt2']
+    levels per shot."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    import torch
+    from fdporo import job
+    from fdporo.engine import Batch
+    shots = job.batch_shots(BATCH["shots"], nsteps=BATCH["mt2"], seed=BATCH["seed"])
+    engines, cells = [], []
+    t0 = time.perf_counter()
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as pool:
+        for inp in pool.map(_prepare_batch_shot, shots):
+            engines.append(job.make_engine(inp, device=dev))
+            cells.append(inp.cells)
+    setup_s = time.perf_counter() - t0
+    total = sum(cells)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    W = 50
+    b = Batch(engines)
+    ext = torch.cuda.ExternalStream(b.stream(), device=dev)
+    b.time_loop(1, W)
+    b.synchronize()
+    e0.record(ext)
+    b.time_loop(W + 1, W + levels)
+    e1.record(ext)
+    e1.synchronize()
+    ms_batch = e0.elapsed_time(e1) / levels
+    shape = b.shape()
+    b.close()
+    # the same shots one after another (FP32), each replaying its own graphs
+    lo = W + levels + 1
+    ms_seq = 0.0
+    for e in engines:
+        e.prepare_run(levels)
+        e.time_loop(lo, lo + 2)
+        s = torch.cuda.ExternalStream(e.stream(), device=dev)
+        e0.record(s)
+        e.time_loop(lo + 3, lo + 2 + levels)
+        e1.record(s)
+        e1.synchronize()
+        ms_seq += e0.elapsed_time(e1) / levels
+        e.close()
+    per_hour = lambda ms: BATCH["shots"] * 3600.0 / (BATCH["mt2"] * ms / 1e3)
+    fp64 = plain_fp64_comparison(shots, dev)
+    return {"shots": BATCH["shots"], "cells_per_level": total, "levels_timed": levels, "setup_s": setup_s,
+            "tile_shape": {"units_per_item": shape[0], "waves": shape[1]},
+            "batch_fp32": {"ms_per_level": ms_batch, "shots_per_hour": per_hour(ms_batch),
+                           "gcell_updates_per_s": total / (ms_batch / 1e3) / 1e9},
+            "sequential_fp32": {"ms_per_level": ms_seq, "shots_per_hour": per_hour(ms_seq)},
+            "sequential_fp64": {"ms_per_level": fp64["ms_per_level"], "shots_per_hour": per_hour(fp64["ms_per_level"]),
+                                "levels_timed_per_shot": fp64["levels_timed_per_shot"]},
+            "batch_vs_sequential_fp32": ms_seq / ms_batch,
+            "batch_fp32_vs_sequential_fp64": fp64["ms_per_level"] / ms_batch,
+            "fp32_seismogram_rel_l2_vs_fp64": fp64["fp32_seismogram_rel_l2_vs_fp64"],
+            "note": "the factor against the FP64 single-shot path is FP32 against FP64 on HBM-bound kernels; "
+                    "batching itself is batch_vs_sequential_fp32"}
 
 
 def run_batch(args) -> None:
@@ -502,6 +587,7 @@ def run_batch(args) -> None:
     lo += W
     ms_seq = 0.0
     for e in engines:
+        e.prepare_run(K)
         s = torch.cuda.ExternalStream(e.stream(), device=dev)
         e0.record(s)
         e.time_loop(lo, lo + K - 1)
@@ -616,6 +702,7 @@ def run_large(args) -> None:
     # the plain single-shot path: the first shot alone
     lo = W + K + 1
     owner.time_loop(lo, lo + W - 1)
+    owner.prepare_run(K)
     owner.synchronize()
     lo += W
     st = torch.cuda.ExternalStream(owner.stream(), device=dev)
@@ -713,6 +800,7 @@ def run_edge(args) -> None:
             edge.attach(eng)
         ext = torch.cuda.ExternalStream(eng.stream())
         eng.time_loop(1, 40)
+        eng.prepare_run(320)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(ext)
         eng.time_loop(41, 40 + 320)
@@ -759,6 +847,7 @@ def main() -> None:
     ap.add_argument("--edge-output", choices=["damp", "correct"], default="damp")
     ap.add_argument("--shots", type=int, default=BATCH["shots"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-batch", action="store_true", help="leave out the batched-shots leg of the default run")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
