@@ -171,10 +171,10 @@ __global__ void __launch_bounds__(kBX * kBZ, 1) k_core_tma(const __grid_constant
           ozz.v[j] = ozz.v[j] + p.DTE * TZZv;
           opr.v[j] = opr.v[j] + p.DTE * PRv;
         }
-        st4(p.TXZ + c0, oxz);
-        st4(p.TXX + c0, oxx);
-        st4(p.TZZ + c0, ozz);
-        st4(p.PRES + c0, opr);
+        st4(p.oTXZ + c0, oxz);
+        st4(p.oTXX + c0, oxx);
+        st4(p.oTZZ + c0, ozz);
+        st4(p.oPRES + c0, opr);
       } else {
         // box rows: TXX from L, TZZ and PRES from L-2, TXZ from L-1
         const V4<float> xxr[3] = {in4(0, ty, -4), in4(0, ty, 0), in4(0, ty, 4)};
@@ -212,10 +212,10 @@ __global__ void __launch_bounds__(kBX * kBZ, 1) k_core_tma(const __grid_constant
             owm.v[j] = w0 + Cw * qz0 + R1w * Xs + R3w * Pp;
           }
         }
-        st4(p.QX + c0, oqx);
-        st4(p.UM + c0, oum);
-        st4(p.QZ + c0, oqz);
-        st4(p.WM + c0, owm);
+        st4(p.oQX + c0, oqx);
+        st4(p.oUM + c0, oum);
+        st4(p.oQZ + c0, oqz);
+        st4(p.oWM + c0, owm);
       }
     }
     __syncthreads();  // every thread is done with stage s

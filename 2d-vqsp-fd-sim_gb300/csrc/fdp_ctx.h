@@ -11,6 +11,7 @@
 
 #include "fdp.h"
 #include "fdp_core_tma.cuh"
+#include "fdp_march.cuh"
 
 struct DevArr {
   void* p = nullptr;
@@ -81,10 +82,31 @@ struct fdp_ctx {
   // set while jm, coef, planes and aux belong to a share with other
   // contexts (the share frees them, not this context)
   std::shared_ptr<MediumShare> medium_share;
-  // captured runs of levels, indexed by their length (1..kRunGraphs); the
-  // longest is replayed over and over, a shorter one ends a run
+  // march variant (FDP_KERNEL_VARIANT=march): each level's interior in one
+  // pass, the levels alternating between the two buffers of each wavefield
+  // array.  fields[] always holds the current level's buffers and alt[] the
+  // other ones; cur tells which of the two allocations fields[] is (0 or 1).
+  bool march = false;
+  DevArr alt[8];
+  int cur = 0;
+  fdp::MarchGrid mg{};
+  int march_ctas = 0;
+  // the frame kernels' rectangles beside the march kernel (stress: F less
+  // its band; velocity: F) and their unit lists
+  int ms[4] = {0, 0, 0, 0}, mv[4] = {0, 0, 0, 0};
+  DevArr mframe_s, mframe_v;
+  int nmframe_s = 0, nmframe_v = 0;
+  // tensor maps of the march kernel, per current buffer; ready once the
+  // medium is held as Biot planes
+  fdp::MarchMaps mmaps[2]{};
+  bool march_ready = false;
+  // set while a batch holds the context (its kernels update in place)
+  bool in_batch = false;
+  // captured runs of levels, indexed by the current buffer and by their
+  // length (1..kRunGraphs); the longest is replayed over and over, a
+  // shorter one ends a run
   static constexpr int kRunGraphs = 32;
-  cudaGraphExec_t graph[kRunGraphs + 1] = {};
+  cudaGraphExec_t graph[2][kRunGraphs + 1] = {};
   bool params_dirty = true;
   // bumped by every change of the device parameters (set_*, a shared
   // medium, an attached edge); a batch refuses to run a shot whose count

@@ -29,6 +29,7 @@
 #include "fdp.h"
 #include "fdp_ctx.h"
 #include "fdp_core_tma.cuh"
+#include "fdp_march.cuh"
 
 using fdp::Params;
 using fdp::kPadX;
@@ -216,7 +217,8 @@ template <class T> void fill_params(fdp_ctx* c, Params<T>& p) {
   p.DTE = p.DT + (T)c->g.tau_eps;
   const size_t off = (size_t)kPadZ * c->pitch + kPadX;
   T** f[8] = {&p.UM, &p.WM, &p.QX, &p.QZ, &p.TXX, &p.TZZ, &p.TXZ, &p.PRES};
-  for (int k = 0; k < 8; ++k) *f[k] = (T*)c->fields[k].p + off;
+  T** o[8] = {&p.oUM, &p.oWM, &p.oQX, &p.oQZ, &p.oTXX, &p.oTZZ, &p.oTXZ, &p.oPRES};
+  for (int k = 0; k < 8; ++k) *f[k] = *o[k] = (T*)c->fields[k].p + off;
   p.JM = c->jm.p ? (const int32_t*)c->jm.p + off : nullptr;
   p.coef = (const T*)c->coef.p;
   p.cld = c->jmnum + 1;
@@ -341,33 +343,20 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
   c->launches += 1;
 }
 
-// Core rectangles and frame unit lists.  A core cell of the stress phase
-// needs 3 <= I <= MX-2, 2 <= L <= MZ-2, L != LIN_Z; of the velocity phase
-// 4 <= I <= MX-2, 2 <= L <= MZ-2 (the interior branches).  The core starts
-// on a 16-byte-aligned column and spans whole groups of four.
-int plan_core(fdp_ctx* c) {
-  auto rect = [&](int r[4], int xmin, int zmin) {
-    int x0 = xmin;
-    while ((x0 - c->PMLL) % 4 != 0) ++x0;
-    const int n4 = (c->MX - 2 - x0 + 1) / 4;
-    r[0] = x0; r[1] = x0 + 4 * std::max(n4, 0);
-    r[2] = zmin; r[3] = c->MZ - 1;
-    if (r[1] <= r[0] || r[3] <= r[2]) { r[0] = r[1] = r[2] = r[3] = 0; }
-  };
-  // under stress imaging, rows 2..4 stay with the stress frame, whose unit
-  // holding them also writes the mirror rows 0 and 1 from them
-  rect(c->cs, 3, c->g.stress_imaging ? 5 : 2);
-  rect(c->cv, 4, 2);
+// Frame unit lists of the frame kernels beside core rectangles cs (stress)
+// and cv (velocity): the columns split at the cores' edges ([PMLL, x0),
+// [x0, x1), [x1, PMLXH]) so that no unit straddles a core edge, units of
+// kBX columns from each segment's start; a unit is listed when it holds a
+// cell outside the core (or, when the stress core leaves the source row to
+// the frame, a cell of the source row).
+int build_units(fdp_ctx* c, const int cs[4], const int cv[4], bool src_in_core, DevArr& frame_s, int& nframe_s,
+                DevArr& frame_v, int& nframe_v) {
   auto in = [](const int r[4], int I, int L) { return I >= r[0] && I < r[1] && L >= r[2] && L < r[3]; };
-  // frame units: the columns split at the core's edges ([PMLL, x0), [x0,
-  // x1), [x1, PMLXH]) so that no unit straddles a core edge, units of kBX
-  // columns from each segment's start; a unit is listed when it holds a
-  // cell outside the core
   std::vector<int> us, uv;
   for (int ph = 0; ph < 2; ++ph) {
     const int rows = fdp::kBZ * (ph == 0 ? fdp::kRZS : fdp::kRZV);
     const int gy = (c->NZ + rows - 1) / rows;
-    const int* r = ph == 0 ? c->cs : c->cv;
+    const int* r = ph == 0 ? cs : cv;
     std::vector<int>& out = ph == 0 ? us : uv;
     std::vector<std::pair<int, int>> segs;
     if (r[1] > r[0]) segs = {{c->PMLL, r[0]}, {r[0], r[1]}, {r[1], c->PMLXH + 1}};
@@ -389,23 +378,108 @@ int plan_core(fdp_ctx* c) {
       for (const auto& sg : segs)
         for (int I0 = sg.first; I0 < sg.second; I0 += fdp::kBX) {
           const int I1 = std::min(I0 + fdp::kBX, sg.second);
-          // a unit is listed when some cell of it lies outside the core
-          // rectangle (or on the source row, for the stress phase)
           const int lo = std::max(la, 0), hi = std::min(lb, c->PMLZH);
           bool frame = false;
           if (lo <= hi)
-            frame = !(in(r, I0, lo) && in(r, I1 - 1, hi)) || (ph == 0 && c->g.lin_z >= lo && c->g.lin_z <= hi);
+            frame = !(in(r, I0, lo) && in(r, I1 - 1, hi)) ||
+                    (ph == 0 && !src_in_core && c->g.lin_z >= lo && c->g.lin_z <= hi);
           if (frame) { out.push_back(I0); out.push_back(I1); out.push_back(tag); out.push_back(w); }
         }
     }
   }
-  c->nframe_s = (int)us.size() / 4;
-  c->nframe_v = (int)uv.size() / 4;
+  nframe_s = (int)us.size() / 4;
+  nframe_v = (int)uv.size() / 4;
   int rc;
-  if ((rc = dev_alloc(c, c->frame_s, us.size() * sizeof(int))) != FDP_OK) return rc;
-  if ((rc = dev_alloc(c, c->frame_v, uv.size() * sizeof(int))) != FDP_OK) return rc;
-  if ((rc = copy_sync(c, c->frame_s.p, us.data(), us.size() * sizeof(int), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
-  return copy_sync(c, c->frame_v.p, uv.data(), uv.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if ((rc = dev_alloc(c, frame_s, us.size() * sizeof(int))) != FDP_OK) return rc;
+  if ((rc = dev_alloc(c, frame_v, uv.size() * sizeof(int))) != FDP_OK) return rc;
+  if ((rc = copy_sync(c, frame_s.p, us.data(), us.size() * sizeof(int), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+  return copy_sync(c, frame_v.p, uv.data(), uv.size() * sizeof(int), cudaMemcpyHostToDevice);
+}
+
+// The march variant's region F and its launch (see fdp_march.cuh); false
+// when the context cannot run it (FP64, a grid too small for a region F).
+bool plan_march(fdp_ctx* c) {
+  if (c->prec != 4) return false;
+  // The new stresses the march kernel computes two cells and two rows
+  // around F are interior ones (columns 3..MX-2 and rows from 2,
+  // strain_uw_xx.F90:80, time_loop.F90:93-124), as are the velocities of F
+  // (columns 4..MX-2, inh_qx_int.F90:40).  Its first halo row of stresses
+  // (two above F) reads velocities from four rows above F on, which stays
+  // below the stress-imaging row 1 that the stress frame kernel writes
+  // meanwhile.  The frame kernels write the new stresses of a band of one
+  // vector and two rows along F's edges, and every cell outside F.
+  int fx0 = 5;
+  while ((fx0 - c->PMLL) % 4 != 0) ++fx0;
+  const int nvec = (c->MX - 3 - fx0) / 4;
+  const int fz0 = 6, fz1 = c->MZ - 3;
+  if (nvec < 3 || fz1 - fz0 < 5) return false;
+  const int fx1 = fx0 + 4 * nvec;
+  fdp::MarchGrid& m = c->mg;
+  m.fx0 = fx0; m.fx1 = fx1; m.fz0 = fz0; m.fz1 = fz1;
+  m.sx0 = fx0 + 4; m.sx1 = fx1 - 4; m.sz0 = fz0 + 2; m.sz1 = fz1 - 2;
+  m.nvec = nvec;
+  m.nstrips = (nvec + fdp::kMarchVec - 1) / fdp::kMarchVec;
+  m.total = (long long)m.nstrips * (fz1 - fz0);
+  // one CTA per SM (the stages take most of an SM's shared memory), the
+  // strips' rows split evenly among them
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->g.device);
+  const char* ec = std::getenv("FDP_MARCH_CTAS");
+  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sms, m.total);
+  if (cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)fdp::kMarchSmem) != cudaSuccess)
+    return false;
+  c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
+  c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
+  return true;
+}
+
+// The march kernel's tensor maps for each of the two buffers of the fields
+// (indexed like cur) over the medium's Biot planes; the march levels run
+// only with them (a medium of another kind leaves the context on the
+// frame/core split).
+int make_march_maps(fdp_ctx* c) {
+  c->march_ready = false;
+  if (!c->march || c->medium_mode != fdp::M_BIOT || !c->planes.p) return FDP_OK;
+  const size_t pstride = (size_t)c->rows_alloc * c->pitch;
+  int rc;
+  for (int b = 0; b < 2; ++b) {
+    const DevArr* f = b == c->cur ? c->fields : c->alt;
+    fdp::MarchMaps& m = c->mmaps[b];
+    for (int k = 0; k < 8; ++k)
+      if ((rc = make_field_map(c, &m.f[k], f[k].p, fdp::kMarchW, fdp::kMarchR)) != FDP_OK) return rc;
+    for (int k = 0; k < 10; ++k)
+      if ((rc = make_field_map(c, &m.pl[k], (float*)c->planes.p + (size_t)k * pstride, fdp::kMarchW, fdp::kMarchR)) !=
+          FDP_OK)
+        return rc;
+  }
+  c->march_ready = true;
+  return FDP_OK;
+}
+
+// Core rectangles and frame unit lists.  A core cell of the stress phase
+// needs 3 <= I <= MX-2, 2 <= L <= MZ-2, L != LIN_Z; of the velocity phase
+// 4 <= I <= MX-2, 2 <= L <= MZ-2 (the interior branches).  The core starts
+// on a 16-byte-aligned column and spans whole groups of four.  With the
+// march variant, also F and the frame units beside it.
+int plan_core(fdp_ctx* c) {
+  auto rect = [&](int r[4], int xmin, int zmin) {
+    int x0 = xmin;
+    while ((x0 - c->PMLL) % 4 != 0) ++x0;
+    const int n4 = (c->MX - 2 - x0 + 1) / 4;
+    r[0] = x0; r[1] = x0 + 4 * std::max(n4, 0);
+    r[2] = zmin; r[3] = c->MZ - 1;
+    if (r[1] <= r[0] || r[3] <= r[2]) { r[0] = r[1] = r[2] = r[3] = 0; }
+  };
+  // under stress imaging, rows 2..4 stay with the stress frame, whose unit
+  // holding them also writes the mirror rows 0 and 1 from them
+  rect(c->cs, 3, c->g.stress_imaging ? 5 : 2);
+  rect(c->cv, 4, 2);
+  int rc = build_units(c, c->cs, c->cv, false, c->frame_s, c->nframe_s, c->frame_v, c->nframe_v);
+  if (rc != FDP_OK) return rc;
+  if (c->march && !plan_march(c)) c->march = false;  // the frame/core split runs the context
+  if (c->march) rc = build_units(c, c->ms, c->mv, true, c->mframe_s, c->nmframe_s, c->mframe_v, c->nmframe_v);
+  return rc;
 }
 
 template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_off, int mode = 0) {
@@ -425,6 +499,20 @@ template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_
   }
 }
 
+// Whether the levels run as march levels: the march variant planned a deep
+// interior and has its tensor maps, and neither a batch (whose kernels
+// update in place) nor an attached learned edge (whose kernels work on the
+// current buffers after every level) holds the context.
+bool use_march(const fdp_ctx* c) {
+  return c->march && c->march_ready && !c->in_batch && !(c->edge && c->edge_attached);
+}
+
+// After a march level the other buffers are current.
+void flip_buffers(fdp_ctx* c) {
+  for (int k = 0; k < 8; ++k) std::swap(c->fields[k], c->alt[k]);
+  c->cur ^= 1;
+}
+
 // Whether a run of levels folds the row-1/receiver step of each level into
 // the next level's stress frame kernel (and its stress samples into the
 // level's velocity frame kernel), leaving one k_edge at the end of the run:
@@ -435,8 +523,73 @@ bool defer_edge(const fdp_ctx* c) {
          edge_threads(c) > 0;
 }
 
+// The wavefield pointers of p: reads from `in`, the phase's new values to
+// `out` (arrays of the eight fields UM WM QX QZ TXX TZZ TXZ PRES).
+template <class T> void set_fields(const fdp_ctx* c, Params<T>& p, const DevArr* in, const DevArr* out) {
+  const size_t off = (size_t)kPadZ * c->pitch + kPadX;
+  T** f[8] = {&p.UM, &p.WM, &p.QX, &p.QZ, &p.TXX, &p.TZZ, &p.TXZ, &p.PRES};
+  T** o[8] = {&p.oUM, &p.oWM, &p.oQX, &p.oQZ, &p.oTXX, &p.oTZZ, &p.oTXZ, &p.oPRES};
+  for (int k = 0; k < 8; ++k) {
+    *f[k] = (T*)in[k].p + off;
+    *o[k] = (T*)out[k].p + off;
+  }
+}
+
+// One level of the march variant: the stress and then the velocity frame
+// kernel on the side stream, beside the march kernel over the deep interior
+// on the context's stream; every kernel reads the current buffers (A) and
+// writes the other ones (B), which are current after the level.  The
+// stress frame kernel also finishes the previous level of the run (row 1,
+// the velocity and the stress samples of the receivers: both stay in A
+// through this level); the run's last level is finished by k_edge.
+template <class T, bool SI, int MODE>
+void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool first, bool last) {
+  const DevArr* A = c->fields;
+  const DevArr* B = c->alt;
+  DevArr sv[8];  // velocities in A, stresses in B
+  for (int k = 0; k < 8; ++k) sv[k] = k < 4 ? A[k] : B[k];
+  Params<T> ps = base;
+  ps.cs_x0 = c->ms[0]; ps.cs_x1 = c->ms[1]; ps.cs_z0 = c->ms[2]; ps.cs_z1 = c->ms[3];
+  ps.cv_x0 = c->mv[0]; ps.cv_x1 = c->mv[1]; ps.cv_z0 = c->mv[2]; ps.cv_z1 = c->mv[3];
+  ps.cs_src = 1;  // the march kernel adds the source term itself
+  Params<T> pv = ps, pm = ps;
+  set_fields(c, ps, A, sv);   // stresses A -> B; velocities read (row 1 finished) in A
+  set_fields(c, pv, sv, B);   // reads the new stresses (B) and the old velocities (A)
+  set_fields(c, pm, A, B);
+  const dim3 blk(fdp::kBX, fdp::kBZ, 1);
+  const bool defer = !first && edge_threads(c) > 0;
+  const int mr_blocks = (c->mr + fdp::kBX * fdp::kBZ - 1) / (fdp::kBX * fdp::kBZ);
+  cudaEventRecord(c->fork, c->stream);
+  cudaStreamWaitEvent(c->side, c->fork, 0);
+  fdp::k_stress_frame<T, SI, MODE><<<c->nmframe_s + (defer ? mr_blocks : 0), blk, 0, c->side>>>(
+      ps, (const int4*)c->mframe_s.p, c->nmframe_s, it_off, defer ? 2 : 0);
+  fdp::k_velocity_frame<T, SI, MODE><<<c->nmframe_v, blk, 0, c->side>>>(pv, (const int4*)c->mframe_v.p,
+                                                                          c->nmframe_v, it_off);
+  if (c->core_ev[0][0]) cudaEventRecord(c->core_ev[0][0], c->stream);
+  if constexpr (std::is_same<T, float>::value && MODE == fdp::M_BIOT)
+    fdp::k_march<MODE><<<c->march_ctas, fdp::kMarchThreads, fdp::kMarchSmem, c->stream>>>(pm, c->mmaps[c->cur],
+                                                                                        c->mg, it_off);
+  if (c->core_ev[0][1]) cudaEventRecord(c->core_ev[0][1], c->stream);
+  cudaEventRecord(c->join, c->side);
+  cudaStreamWaitEvent(c->stream, c->join, 0);
+  c->launches += 3;
+  flip_buffers(c);
+  if (last && edge_threads(c) > 0) {
+    Params<T> pe = base;
+    set_fields(c, pe, c->fields, c->fields);
+    fdp::k_edge<T, SI><<<(edge_threads(c) + kBlockX - 1) / kBlockX, kBlockX, 0, c->stream>>>(pe, it_off, 1);
+    c->launches += 1;
+  }
+}
+
 // Level it_off of a run of levels; `first` and `last` mark the run's ends.
 template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_off, bool first, bool last) {
+  if (use_march(c)) {
+    // the march levels run FP32 contexts with a Biot-plane medium only
+    if (c->g.stress_imaging) launch_level_march<T, true, fdp::M_BIOT>(c, p, it_off, first, last);
+    else launch_level_march<T, false, fdp::M_BIOT>(c, p, it_off, first, last);
+    return FDP_OK;
+  }
   const bool defer = defer_edge(c);
   launch<T>(c, p, 0, it_off, defer && !first ? kDeferPrev : 0);
   launch<T>(c, p, 1, it_off, defer ? kFrameSamples : 0);
@@ -447,6 +600,7 @@ template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_o
 
 // Kernel launches of a run of n levels.
 long long run_launches(const fdp_ctx* c, int n) {
+  if (use_march(c)) return (long long)n * 3 + (edge_threads(c) > 0 ? 1 : 0);
   const int cores = c->use_core ? (!c->fused[0] && c->cs[1] > c->cs[0]) + (!c->fused[1] && c->cv[1] > c->cv[0]) : 0;
   const int edges = edge_threads(c) > 0 ? (defer_edge(c) ? 1 : n) : 0;
   return (long long)n * (2 + cores + (c->edge && c->edge_attached ? 3 : 0)) + edges;
@@ -454,8 +608,9 @@ long long run_launches(const fdp_ctx* c, int n) {
 
 // Frees every captured run of levels (their kernels' parameters changed).
 void drop_graphs(fdp_ctx* c) {
-  for (auto& g : c->graph)
-    if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+  for (auto& row : c->graph)
+    for (auto& g : row)
+      if (g) { cudaGraphExecDestroy(g); g = nullptr; }
 }
 
 // The captured graph of a run of n levels (1 <= n <= kChunk), captured on
@@ -467,25 +622,30 @@ template <class T> int run_graph(fdp_ctx* c, const Params<T>& p, int n, cudaGrap
     drop_graphs(c);
     c->params_dirty = false;
   }
-  if (!c->graph[n]) {
+  cudaGraphExec_t& slot = c->graph[c->cur][n];
+  if (!slot) {
     cudaGraph_t gr = nullptr;
     CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const long long before = c->launches;
+    const int cur = c->cur;
     for (int k = 0; k < n; ++k) launch_level_any<T>(c, p, k, k == 0, k == n - 1);
     fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
-    c->launches = before;  // capture only records; replays are counted by the caller
+    // capture only records: the launch count and the current buffers stay
+    // those before the run until the caller launches it
+    c->launches = before;
+    if (c->cur != cur) flip_buffers(c);
     cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
     if (e != cudaSuccess) return fail(c, FDP_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&c->graph[n], gr, 0);
+    e = cudaGraphInstantiate(&slot, gr, 0);
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) {
-      c->graph[n] = nullptr;
+      slot = nullptr;
       return fail(c, FDP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
     // moves the graph's device-side set-up out of its first launch
-    CK(c, cudaGraphUpload(c->graph[n], c->stream));
+    CK(c, cudaGraphUpload(slot, c->stream));
   }
-  *out = c->graph[n];
+  *out = slot;
   return FDP_OK;
 }
 
@@ -505,6 +665,7 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
     if (rc != FDP_OK) return rc;
     CK(c, cudaGraphLaunch(g, c->stream));
     c->launches += run_launches(c, n) + 1;
+    if (use_march(c) && (n & 1)) flip_buffers(c);  // the run ends in the other buffers
     it += n;
   }
   CK(c, cudaGetLastError());
@@ -834,6 +995,7 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   c->fused[0] = c->use_core && fused;
   c->fused[1] = c->use_core && fused;
   c->core_tma_req = c->use_core && variant && std::strcmp(variant, "coretma") == 0;
+  c->march = c->use_core && variant && std::strcmp(variant, "march") == 0;
   if (c->use_core) {
     if ((rc = plan_core(c)) != FDP_OK) return bail(rc);
     e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
@@ -842,6 +1004,9 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
 
     if (e != cudaSuccess) { c->err = std::string("side stream: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
   }
+  if (c->march)  // the second buffer of each wavefield array, zeroed like the first
+    for (int k = 0; k < 8; ++k)
+      if ((rc = dev_alloc(c, c->alt[k], fbytes)) != FDP_OK) return bail(rc);
   if (c->use_tma) {
     for (int k = 0; k < 4; ++k) {
       if ((rc = make_field_map(c, &c->tma_vel.m[k], c->fields[k].p)) != FDP_OK) return bail(rc);
@@ -888,6 +1053,7 @@ int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_
   if (rc != FDP_OK) return rc;
   CK(c, cudaStreamSynchronize(c->stream));
   if ((rc = make_core_maps(c)) != FDP_OK) return rc;
+  if ((rc = make_march_maps(c)) != FDP_OK) return rc;
   c->jmnum = jmnum;
   c->have_medium = true;
   params_changed(c);
@@ -924,7 +1090,8 @@ int fdp_share_medium(fdp_ctx* dst, fdp_ctx* src) {
   dst->jmnum = src->jmnum;
   dst->have_medium = true;
   params_changed(dst);
-  return make_core_maps(dst);
+  if ((rc = make_core_maps(dst)) != FDP_OK) return rc;
+  return make_march_maps(dst);
 }
 
 int fdp_set_pml(fdp_ctx* c, const void* const* prof) {
@@ -1105,6 +1272,12 @@ static int field_copy(fdp_ctx* c, int32_t id, void* host, bool set) {
   const size_t es = (size_t)c->prec;
   if (id <= FDP_PRES) {
     char* dev = (char*)c->fields[id].p + ((size_t)kPadZ * c->pitch + kPadX) * es;
+    if (set && c->alt[id].p) {
+      // both buffers: cells no level updates are read from either
+      char* dev2 = (char*)c->alt[id].p + ((size_t)kPadZ * c->pitch + kPadX) * es;
+      int rc = copy2d_sync(c, dev2, c->pitch * es, host, c->NX * es, c->NX * es, c->NZ, cudaMemcpyHostToDevice);
+      if (rc != FDP_OK) return rc;
+    }
     if (set)
       return copy2d_sync(c, dev, c->pitch * es, host, c->NX * es, c->NX * es, c->NZ, cudaMemcpyHostToDevice);
     else
@@ -1179,6 +1352,17 @@ int fdp_core_info(fdp_ctx* c, int32_t* rect8) {
   return FDP_OK;
 }
 
+int fdp_march_info(fdp_ctx* c, int32_t* region8, int32_t* shape4) {
+  if (!c || !region8 || !shape4) return fail(c, FDP_ERR_ARG, "null argument");
+  const bool on = use_march(c);
+  const fdp::MarchGrid& m = c->mg;
+  const int32_t r[8] = {m.fx0, m.fx1, m.fz0, m.fz1, m.sx0, m.sx1, m.sz0, m.sz1};
+  const int32_t sh[4] = {m.nstrips, fdp::kMarchR, c->march_ctas, fdp::kMarchThreads / 32};
+  for (int k = 0; k < 8; ++k) region8[k] = on ? r[k] : 0;
+  for (int k = 0; k < 4; ++k) shape4[k] = on ? sh[k] : 0;
+  return FDP_OK;
+}
+
 int fdp_get_stream(fdp_ctx* c, void** stream) {
   if (!c || !stream) return fail(c, FDP_ERR_ARG, "null argument");
   *stream = (void*)c->stream;
@@ -1199,8 +1383,8 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
     Params<T> p;
     fill_params<T>(c, p);
     const int nedge = edge_threads(c);
-    const bool core[2] = {c->use_core && !c->fused[0] && c->cs[1] > c->cs[0],
-                          c->use_core && !c->fused[1] && c->cv[1] > c->cv[0]};
+    const bool core[2] = {use_march(c) || (c->use_core && !c->fused[0] && c->cs[1] > c->cs[0]),
+                          !use_march(c) && c->use_core && !c->fused[1] && c->cv[1] > c->cv[0]};
     // every level is enqueued before the one synchronisation at the end, so
     // the device never waits for the host and each window holds device time
     // only: per level, events around the two phases and the edge, and
@@ -1212,7 +1396,25 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
       if (cudaEventCreate(&e) != cudaSuccess) { e = nullptr; rc = fail(c, FDP_ERR_CUDA, "cudaEventCreate failed"); break; }
     if (rc == FDP_OK) {
       fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
-      for (int it = it_begin; it <= it_end; ++it) {
+      for (int it = it_begin; it <= it_end && use_march(c); ++it) {
+        // march levels: entry 0 the whole level (frames beside the march
+        // kernel), entry 2 its k_edge, entry 3 the march kernel
+        const int off = it - it_begin;
+        cudaEvent_t* e = &ev[(size_t)off * 8];
+        c->core_ev[0][0] = e[4];
+        c->core_ev[0][1] = e[5];
+        cudaEventRecord(e[0], c->stream);
+        launch_level_any<T>(c, p, off, true, false);
+        cudaEventRecord(e[1], c->stream);
+        cudaEventRecord(e[2], c->stream);
+        if (nedge > 0) {
+          Params<T> pe = p;
+          set_fields(c, pe, c->fields, c->fields);
+          launch<T>(c, pe, 2, off);
+        }
+        cudaEventRecord(e[3], c->stream);
+      }
+      for (int it = it_begin; it <= it_end && !use_march(c); ++it) {
         const int off = it - it_begin;
         cudaEvent_t* e = &ev[(size_t)off * 8];
         for (int k = 0; k < 2; ++k) {
@@ -1244,7 +1446,7 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
             ms_out[3 + k] += t;
             launches_out[3 + k] += 1;
           }
-        launches_out[0] += 1; launches_out[1] += 1; launches_out[2] += nedge > 0 ? 1 : 0;
+        launches_out[0] += 1; launches_out[1] += use_march(c) ? 0 : 1; launches_out[2] += nedge > 0 ? 1 : 0;
       }
     }
     for (auto& e : ev) if (e) cudaEventDestroy(e);
@@ -1264,9 +1466,10 @@ void fdp_destroy(fdp_ctx* c) {
   drop_graphs(c);
   unshare_medium(c);
   DevArr* all[] = {&c->jm, &c->coef, &c->planes, &c->aux, &c->ab, &c->hist, &c->stf, &c->rec, &c->raw, &c->itbase,
-                   &c->errbuf, &c->frame_s, &c->frame_v, &c->diag_flag};
+                   &c->errbuf, &c->frame_s, &c->frame_v, &c->mframe_s, &c->mframe_v, &c->diag_flag};
   for (auto* a : all) if (a->p) cudaFree(a->p);
   for (auto& a : c->fields) if (a.p) cudaFree(a.p);
+  for (auto& a : c->alt) if (a.p) cudaFree(a.p);
   for (auto& a : c->prof) if (a.p) cudaFree(a.p);
   for (auto& a : c->mem) if (a.p) cudaFree(a.p);
   if (c->side) cudaStreamSynchronize(c->side);
@@ -1755,6 +1958,7 @@ int fdp_batch_create(fdp_ctx* const* shots, int32_t n, fdp_batch** out) {
     if ((rc = (b->prec == 8 ? group_occupancy_any<double>(b, G) : group_occupancy_any<float>(b, G))) != FDP_OK)
       return bail(rc);
   if ((rc = batch_set_shape(b, 2, 1)) != FDP_OK) return bail(rc);
+  for (fdp_ctx* c : b->shots) c->in_batch = true;  // in-place levels while the batch holds them
   *out = b;
   return FDP_OK;
 }
@@ -1820,6 +2024,7 @@ const char* fdp_batch_last_error(const fdp_batch* b) { return b ? b->err.c_str()
 void fdp_batch_destroy(fdp_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
+  for (fdp_ctx* c : b->shots) c->in_batch = false;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->side) cudaStreamSynchronize(b->side);
   for (DevArr* a : {&b->params, &b->first, &b->itbase, &b->units, &b->ubase}) if (a->p) cudaFree(a->p);

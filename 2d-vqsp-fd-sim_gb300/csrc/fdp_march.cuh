@@ -1,0 +1,282 @@
+// A whole time level of the deep interior in one pass (the "march" kernel).
+//
+// A level is the stress phase (time_loop.F90:93-124) and then the velocity
+// phase (time_loop.F90:133-179).  In the interior both are the 4th-order
+// stencils of the core kernels, and a cell's new velocities need the new
+// stresses only within two cells of it.  So a CTA of eight warps owns a
+// strip of 30 four-cell vectors (120 columns) and marches down a range of
+// its rows in bands of eight rows: per band each warp computes the new
+// stresses of one row for the strip's vectors and one halo vector either
+// side (lanes 0 and 31), keeps them in a shared-memory ring of 16 rows, and,
+// after a barrier, the new velocities of the row two above from that ring.
+// A cell's stencils read the old wavefield (one buffer of each pair) and
+// write the new values to the other, so no CTA reads what another writes
+// during the launch.
+//
+// Inputs arrive by bulk tensor copies (cp.async.bulk.tensor.2d), one box of
+// 128 columns by 8 rows per array: the old velocities into a ring of 24
+// rows (the 12 a band's stencils reach and the next band's 8), and the old
+// stresses and the ten coefficient planes of the band into one of two
+// stages.  One thread issues the next band's copies as a band starts, so
+// they are in flight while the band computes; every thread waits for its
+// band's copies on the stage's mbarrier with a bounded try_wait, and a wait
+// that gives up sets the status word, lets the copies in flight land
+// (bounded again) and returns.
+//
+// Per cell the pass reads the old velocities and stresses and the ten
+// coefficient planes and writes the new velocities and stresses: 26 values
+// (104 bytes in FP32), where the two phases as separate passes read the new
+// stresses and the old velocities a second time (136 bytes).
+//
+// The region F the kernel updates, [fx0, fx1) x [fz0, fz1), is chosen on
+// the host so that every stencil the kernel evaluates, including the new
+// stresses of the halo cells two columns and two rows around F, is the
+// interior one; the frame kernels update every other cell.  The kernel
+// writes the new velocities of all of F, and the new stresses of F less a
+// band of one vector and two rows along its edges: the frame kernel's
+// velocity cells next to F read the new stresses there, and the frame
+// kernels (on another stream) write them instead, so the launches need no
+// ordering between them.  The stress update of the source cell (LIN_X,
+// LIN_Z) adds the source term of stress_lin_nn.F90:58-63.
+//
+// The CTAs split the strips' rows evenly (one CTA per SM, the rows of all
+// strips taken as one sequence); a CTA whose range crosses into the next
+// strip starts again there.  FP32 with the ten planes of a Biot medium.
+#pragma once
+
+#include "fdp_core_tma.cuh"
+
+namespace fdp {
+
+constexpr int kMarchVec = 30;                  // vectors a strip updates (lanes 1..30)
+constexpr int kMarchW = 128;                   // box width: the strip's 32 vectors
+constexpr int kMarchR = 8;                     // rows per band, one per warp
+constexpr int kMarchThreads = 32 * kMarchR;
+constexpr int kMarchVRows = 3 * kMarchR;       // velocity ring rows
+constexpr int kMarchSRows = 16;                // stress ring rows
+constexpr int kMarchBox = kMarchR * kMarchW;   // floats per box
+constexpr int kMarchDirect = 14;               // boxes of a stage: stresses (4), stress planes, velocity planes (5 each)
+constexpr int kMarchVRing = 4 * kMarchVRows * kMarchW;
+constexpr int kMarchStage = kMarchDirect * kMarchBox;
+constexpr int kMarchSRing = 4 * kMarchSRows * kMarchW;
+constexpr size_t kMarchSmem = (size_t)(kMarchVRing + 2 * kMarchStage + kMarchSRing) * sizeof(float) + 128;
+static_assert(kMarchSmem <= 227 * 1024, "march stages exceed the shared memory of a CTA");
+
+// Tensor maps (boxes of 128 columns by 8 rows): the eight wavefield arrays
+// a level reads (UM WM QX QZ TXX TZZ TXZ PRES) and the ten Biot planes.
+struct MarchMaps {
+  CUtensorMap f[8];
+  CUtensorMap pl[10];
+};
+
+// The launch's work: F, where the new stresses are written, the strips of
+// kMarchVec vectors across F, and the rows of all strips as one sequence.
+struct MarchGrid {
+  int fx0, fx1, fz0, fz1;  // F
+  int sx0, sx1, sz0, sz1;  // where the kernel writes the new stresses
+  int nstrips, nvec;       // strips, vectors across F
+  long long total;         // nstrips * (fz1 - fz0)
+};
+
+// A band of a CTA: strip, the velocity rows [vlo, vhi) of its segment and
+// its index k there; its stresses are rows [vlo-2+8k, vlo+6+8k) and its
+// velocities rows [vlo-4+8k, vlo+4+8k).
+struct MarchBand {
+  int strip, vlo, vhi, k;
+};
+
+// The rows [lo, hi) of a CTA in the sequence of all strips' rows (H rows per
+// strip), as segments of one strip each and bands of kMarchR rows.
+struct MarchRange {
+  long long lo, hi;
+  int H;
+  __device__ __forceinline__ int bands_of(int vlo, int vhi) const { return (vhi - vlo + 4 + kMarchR - 1) / kMarchR; }
+  // segment `s` of the range (strip, vlo, vhi), false past the last
+  __device__ __forceinline__ bool segment(int s, int fz0, int& strip, int& vlo, int& vhi) const {
+    const long long first = lo / H + s;
+    if (lo >= hi || first * H >= hi) return false;
+    strip = (int)first;
+    vlo = fz0 + (int)(first * H >= lo ? 0 : lo - first * H);
+    vhi = fz0 + (int)((first + 1) * H <= hi ? H : hi - first * H);
+    return true;
+  }
+  __device__ __forceinline__ int count(int fz0) const {
+    int n = 0, st, a, b;
+    for (int s = 0; segment(s, fz0, st, a, b); ++s) n += bands_of(a, b);
+    return n;
+  }
+  __device__ __forceinline__ MarchBand band(int i, int fz0) const {
+    int st = 0, a = 0, b = 0;
+    for (int s = 0; segment(s, fz0, st, a, b); ++s) {
+      const int n = bands_of(a, b);
+      if (i < n) return {st, a, b, i};
+      i -= n;
+    }
+    return {st, a, b, i};
+  }
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constant__ Params<float> p,
+                                                             const __grid_constant__ MarchMaps maps, const MarchGrid g,
+                                                             int it_off) {
+  extern __shared__ unsigned char march_raw[];
+  float* const vring = reinterpret_cast<float*>(((uintptr_t)march_raw + 127) & ~(uintptr_t)127);
+  float* const stages = vring + kMarchVRing;
+  float* const sring = stages + 2 * kMarchStage;
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ int failed;
+  const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  MarchRange rg;
+  rg.H = g.fz1 - g.fz0;
+  rg.lo = (long long)blockIdx.x * g.total / gridDim.x;
+  rg.hi = (long long)(blockIdx.x + 1) * g.total / gridDim.x;
+  const int nbands = rg.count(g.fz0);
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    failed = 0;
+  }
+  __syncthreads();
+  if (nbands == 0) return;
+
+  // the copies of the CTA's i-th band into stage i % 2 (and the velocity ring)
+  auto issue = [&](int i) {
+    const MarchBand b = rg.band(i, g.fz0);
+    uint64_t* bar = &full[i & 1];
+    float* st = stages + (i & 1) * kMarchStage;
+    const int x = g.fx0 + 4 * kMarchVec * b.strip - 4 - p.PMLL + kPadX;  // padded column of the box
+    const int r = b.vlo - 2 + kMarchR * b.k;                                // first stress row
+    mbar_expect_tx(bar, (uint32_t)((b.k == 0 ? 22 : 18) * kMarchBox * sizeof(float)));
+    // velocities: rows [r+2, r+10) into ring rows ((k+1) % 3) * 8 .. (the
+    // ring row of grid row y is (y - vlo + 8) % 24); band 0 also rows
+    // [vlo-8, vlo) into ring rows 0..7
+    const int slot = ((b.k + 1) % 3) * kMarchR;
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      float* fr = vring + f * kMarchVRows * kMarchW;
+      tma_load_2d(fr + slot * kMarchW, &maps.f[f], x, r + 2 + kPadZ, bar);
+      if (b.k == 0) tma_load_2d(fr, &maps.f[f], x, b.vlo - kMarchR + kPadZ, bar);
+    }
+    // stresses and stress planes of rows [r, r+8), velocity planes of rows [r-2, r+6)
+#pragma unroll
+    for (int f = 0; f < 4; ++f) tma_load_2d(st + f * kMarchBox, &maps.f[4 + f], x, r + kPadZ, bar);
+#pragma unroll
+    for (int s = 0; s < 5; ++s) tma_load_2d(st + (4 + s) * kMarchBox, &maps.pl[s], x, r + kPadZ, bar);
+#pragma unroll
+    for (int s = 0; s < 5; ++s) tma_load_2d(st + (9 + s) * kMarchBox, &maps.pl[5 + s], x, r - 2 + kPadZ, bar);
+  };
+
+  const long long P = p.pitch;
+  const int it = *p.it_base + it_off;
+  float srcS, srcF;
+  {
+    const float SOURS = p.STF[2 * (it - 1)], SOURF = p.STF[2 * (it - 1) + 1];
+    const float SOURSP = it > 1 ? p.STF[2 * (it - 2)] : 0.f;
+    const float SOURFP = it > 1 ? p.STF[2 * (it - 2) + 1] : 0.f;
+    srcS = ((SOURS - SOURSP) / p.DT);
+    srcF = ((SOURF - SOURFP) / p.DT);
+  }
+  const int lm = lane > 0 ? lane - 1 : 0, lp = lane < 31 ? lane + 1 : 31;  // x-neighbour vectors (clamped)
+
+  if (tid == 0) issue(0);
+  bool issued_next = false;
+  int i = 0;
+  for (; i < nbands; ++i) {
+    const MarchBand b = rg.band(i, g.fz0);
+    const int st = i & 1;
+    if (tid == 0 && !issued_next && i > 0) issue(i);  // a new segment: its first band was not prefetched
+    if (!mbar_wait_bounded(&full[st], (uint32_t)((i >> 1) & 1))) failed = 1;
+    __syncthreads();
+    if (failed) {
+      if (tid == 0) atomicOr(p.err, 1);
+      break;
+    }
+    // prefetch the next band of the same segment (the next segment's first
+    // band would overwrite ring rows this band reads)
+    issued_next = false;
+    if (i + 1 < nbands && rg.band(i + 1, g.fz0).k > 0) {
+      if (tid == 0) issue(i + 1);
+      issued_next = true;
+    }
+    const float* S = stages + st * kMarchStage;
+    const int v = kMarchVec * b.strip + lane - 1;                  // the lane's vector of F
+    const int I0 = g.fx0 + 4 * v;                                  // its first column
+    const bool sok = v <= g.nvec;                                  // new stresses here (halo included)
+    const bool own = lane >= 1 && lane <= kMarchVec && v < g.nvec;  // a vector of F this CTA updates
+    auto vrow = [&](int f, int y) { return vring + (f * kMarchVRows + (y - b.vlo + kMarchR) % kMarchVRows) * kMarchW; };
+    auto srow = [&](int f, int y) { return sring + (f * kMarchSRows + ((y - b.vlo + 2) & (kMarchSRows - 1))) * kMarchW; };
+
+    // ---- new stresses of row Ls for the strip's 32 vectors
+    const int Ls = b.vlo - 2 + kMarchR * b.k + warp;
+    if (sok) {
+      StressCoreIn<float> a;
+      a.ur[0] = lds4(vrow(0, Ls) + 4 * lm); a.ur[1] = lds4(vrow(0, Ls) + 4 * lane); a.ur[2] = lds4(vrow(0, Ls) + 4 * lp);
+      a.wr[0] = lds4(vrow(1, Ls) + 4 * lm); a.wr[1] = lds4(vrow(1, Ls) + 4 * lane); a.wr[2] = lds4(vrow(1, Ls) + 4 * lp);
+      a.xr[0] = lds4(vrow(2, Ls) + 4 * lm); a.xr[1] = lds4(vrow(2, Ls) + 4 * lane); a.xr[2] = lds4(vrow(2, Ls) + 4 * lp);
+      a.um2 = lds4(vrow(0, Ls - 2) + 4 * lane); a.um1 = lds4(vrow(0, Ls - 1) + 4 * lane);
+      a.up1 = lds4(vrow(0, Ls + 1) + 4 * lane);
+      a.wm1 = lds4(vrow(1, Ls - 1) + 4 * lane); a.wp1 = lds4(vrow(1, Ls + 1) + 4 * lane);
+      a.wp2 = lds4(vrow(1, Ls + 2) + 4 * lane);
+      a.zm1 = lds4(vrow(3, Ls - 1) + 4 * lane); a.z0 = lds4(vrow(3, Ls) + 4 * lane);
+      a.zp1 = lds4(vrow(3, Ls + 1) + 4 * lane); a.zp2 = lds4(vrow(3, Ls + 2) + 4 * lane);
+      const float* srow0 = S + warp * kMarchW + 4 * lane;
+      // stage boxes 0..3: TXX TZZ TXZ PRES
+      V4<float> oxx = lds4(srow0), ozz = lds4(srow0 + kMarchBox), oxz = lds4(srow0 + 2 * kMarchBox),
+                opr = lds4(srow0 + 3 * kMarchBox);
+      V4<float> bio[5];
+#pragma unroll
+      for (int s = 0; s < 5; ++s) bio[s] = lds4(srow0 + (4 + s) * kMarchBox);
+      const long long c0 = (long long)Ls * P + (I0 - p.PMLL);
+      const int src_j = (Ls == p.LIN_Z && p.LIN_X >= I0 && p.LIN_X < I0 + 4) ? p.LIN_X - I0 : -1;
+      stress_core_math<float, MODE>(p, c0, a, bio, oxz, oxx, ozz, opr, src_j, srcS, srcF);
+      *reinterpret_cast<float4*>(srow(0, Ls) + 4 * lane) = make_float4(oxz.v[0], oxz.v[1], oxz.v[2], oxz.v[3]);
+      *reinterpret_cast<float4*>(srow(1, Ls) + 4 * lane) = make_float4(oxx.v[0], oxx.v[1], oxx.v[2], oxx.v[3]);
+      *reinterpret_cast<float4*>(srow(2, Ls) + 4 * lane) = make_float4(ozz.v[0], ozz.v[1], ozz.v[2], ozz.v[3]);
+      *reinterpret_cast<float4*>(srow(3, Ls) + 4 * lane) = make_float4(opr.v[0], opr.v[1], opr.v[2], opr.v[3]);
+      if (own && I0 >= g.sx0 && I0 < g.sx1 && Ls >= b.vlo && Ls < b.vhi && Ls >= g.sz0 && Ls < g.sz1) {
+        st4(p.oTXZ + c0, oxz);
+        st4(p.oTXX + c0, oxx);
+        st4(p.oTZZ + c0, ozz);
+        st4(p.oPRES + c0, opr);
+      }
+    }
+    __syncthreads();
+
+    // ---- new velocities of row Lv = Ls - 2 from the stress ring rows Lv-2..Lv+2
+    const int Lv = Ls - 2;
+    if (own && Lv >= b.vlo && Lv < b.vhi) {
+      VelocityCoreIn<float> a;
+      a.xxr[0] = lds4(srow(1, Lv) + 4 * lm); a.xxr[1] = lds4(srow(1, Lv) + 4 * lane);
+      a.xxr[2] = lds4(srow(1, Lv) + 4 * lp);
+      a.prr[0] = lds4(srow(3, Lv) + 4 * lm); a.prr[1] = lds4(srow(3, Lv) + 4 * lane);
+      a.prr[2] = lds4(srow(3, Lv) + 4 * lp);
+      a.xzr[0] = lds4(srow(0, Lv) + 4 * lm); a.xzr[1] = lds4(srow(0, Lv) + 4 * lane);
+      a.xzr[2] = lds4(srow(0, Lv) + 4 * lp);
+      a.prm2 = lds4(srow(3, Lv - 2) + 4 * lane); a.prm1 = lds4(srow(3, Lv - 1) + 4 * lane);
+      a.prp1 = lds4(srow(3, Lv + 1) + 4 * lane);
+      a.xzm1 = lds4(srow(0, Lv - 1) + 4 * lane); a.xzp1 = lds4(srow(0, Lv + 1) + 4 * lane);
+      a.xzp2 = lds4(srow(0, Lv + 2) + 4 * lane);
+      a.zzm2 = lds4(srow(2, Lv - 2) + 4 * lane); a.zzm1 = lds4(srow(2, Lv - 1) + 4 * lane);
+      a.zz0 = lds4(srow(2, Lv) + 4 * lane); a.zzp1 = lds4(srow(2, Lv + 1) + 4 * lane);
+      V4<float> oum = lds4(vrow(0, Lv) + 4 * lane), owm = lds4(vrow(1, Lv) + 4 * lane),
+                oqx = lds4(vrow(2, Lv) + 4 * lane), oqz = lds4(vrow(3, Lv) + 4 * lane);
+      V4<float> bio[5];
+      const float* prow = S + 9 * kMarchBox + warp * kMarchW + 4 * lane;
+#pragma unroll
+      for (int s = 0; s < 5; ++s) bio[s] = lds4(prow + s * kMarchBox);
+      const long long c0 = (long long)Lv * P + (I0 - p.PMLL);
+      velocity_core_math<float, MODE>(p, c0, a, bio, oqx, oum, oqz, owm);
+      st4(p.oQX + c0, oqx);
+      st4(p.oUM + c0, oum);
+      st4(p.oQZ + c0, oqz);
+      st4(p.oWM + c0, owm);
+    }
+    __syncthreads();  // the stage, and the ring rows the next copies overwrite, are free
+  }
+  // after a wait that gave up, let that band's copies, which may still be in
+  // flight, land before the CTA exits (bounded)
+  if (failed && tid == 0) mbar_wait_bounded(&full[i & 1], (uint32_t)((i >> 1) & 1));
+}
+
+}  // namespace fdp

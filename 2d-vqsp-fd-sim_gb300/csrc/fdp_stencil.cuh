@@ -108,7 +108,14 @@ template <class T> struct Params {
   // skip them.  Empty (x0 == x1) when the unit kernels update every cell.
   int cs_x0, cs_x1, cs_z0, cs_z1, cv_x0, cv_x1, cv_z0, cv_z1;
   T AH, BH, CH, BC, A, B, DT, DTE;
+  // the wavefield a kernel reads (UM..PRES) and the arrays it writes its
+  // phase's new values to (oUM..oPRES): the same arrays when levels update
+  // in place, the other buffer of each pair when they alternate
   T *UM, *WM, *QX, *QZ, *TXX, *TZZ, *TXZ, *PRES;
+  T *oUM, *oWM, *oQX, *oQZ, *oTXX, *oTZZ, *oTXZ, *oPRES;
+  // the stress core rectangle includes the source row LIN_Z (its update adds
+  // the source term); else the source row is left to the unit kernels
+  int cs_src;
   // medium, table mode
   const int32_t* JM;
   const T* coef;
@@ -246,8 +253,8 @@ __device__ __forceinline__ void stress_interior_rows(const Params<T>& p, int I, 
   // to memory it could alias, so interleaving would serialise the rows)
 #pragma unroll
   for (int r = 0; r < kRZS; ++r) {
-    p.TXZ[c0 + r * P] = oxz[r]; p.TXX[c0 + r * P] = oxx[r];
-    p.TZZ[c0 + r * P] = ozz[r]; p.PRES[c0 + r * P] = opr[r];
+    p.oTXZ[c0 + r * P] = oxz[r]; p.oTXX[c0 + r * P] = oxx[r];
+    p.oTZZ[c0 + r * P] = ozz[r]; p.oPRES[c0 + r * P] = opr[r];
   }
 }
 
@@ -317,8 +324,8 @@ __device__ __forceinline__ void velocity_interior_rows(const Params<T>& p, int I
   // to memory it could alias, so interleaving would serialise the rows)
 #pragma unroll
   for (int r = 0; r < kRZV; ++r) {
-    p.QX[c0 + r * P] = oqx[r]; p.UM[c0 + r * P] = oum[r];
-    p.QZ[c0 + r * P] = oqz[r]; p.WM[c0 + r * P] = owm[r];
+    p.oQX[c0 + r * P] = oqx[r]; p.oUM[c0 + r * P] = oum[r];
+    p.oQZ[c0 + r * P] = oqz[r]; p.oWM[c0 + r * P] = owm[r];
   }
 }
 
@@ -570,14 +577,14 @@ __device__ __forceinline__ void stress_cell(const Params<T>& p, const R& rd, int
   if (do_xz) {
     if (xz_z) p.PXZH[zi] = mz_new;
     if (xz_lo || xz_hi) xz_m[xz_mi] = mx_new;
-    FDP_F(p.TXZ, I, L) = txz_new;
+    FDP_F(p.oTXZ, I, L) = txz_new;
   }
   if (do_nn) {
     if (zz_pml) { p.PZZH[zj] = me_new; p.OZZH[zj] = mq_new; }
     if (xx_lo || xx_hi) { xx_me[xx_mi] = ne_new; xx_mq[xx_mi] = nq_new; }
-    FDP_F(p.TXX, I, L) = txx_new;
-    FDP_F(p.TZZ, I, L) = tzz_new;
-    FDP_F(p.PRES, I, L) = pr_new;
+    FDP_F(p.oTXX, I, L) = txx_new;
+    FDP_F(p.oTZZ, I, L) = tzz_new;
+    FDP_F(p.oPRES, I, L) = pr_new;
   }
 }
 
@@ -603,7 +610,8 @@ __device__ __forceinline__ void stress_unit_cells(const Params<T>& p, int I0, in
     const bool incol = I >= p.cs_x0 && I < p.cs_x1;
 #pragma unroll 1
     for (int L = L0; L < L0 + kRZS; ++L)
-      if (L <= p.PMLZH && (!SI || L >= 2) && !(incol && L >= p.cs_z0 && L < p.cs_z1 && L != p.LIN_Z))
+      if (L <= p.PMLZH && (!SI || L >= 2) &&
+          !(incol && L >= p.cs_z0 && L < p.cs_z1 && (p.cs_src || L != p.LIN_Z)))
         stress_cell<T, SI, MODE>(p, rd, I, L, it);
   }
 }
@@ -612,13 +620,13 @@ __device__ __forceinline__ void stress_unit_cells(const Params<T>& p, int I0, in
 // 2..4 (hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53).
 template <class T>
 __device__ __forceinline__ void stress_mirror(const Params<T>& p, int I) {
-  FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
-  FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
-  FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
-  FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
-  FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
-  FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
-  FDP_F(p.TXZ, I, 2) = T(0);
+  FDP_F(p.oTXZ, I, 0) = -FDP_F(p.oTXZ, I, 4);
+  FDP_F(p.oTZZ, I, 0) = -FDP_F(p.oTZZ, I, 3);
+  FDP_F(p.oPRES, I, 0) = -FDP_F(p.oPRES, I, 3);
+  FDP_F(p.oTXZ, I, 1) = -FDP_F(p.oTXZ, I, 3);
+  FDP_F(p.oTZZ, I, 1) = -FDP_F(p.oTZZ, I, 2);
+  FDP_F(p.oPRES, I, 1) = -FDP_F(p.oPRES, I, 2);
+  FDP_F(p.oTXZ, I, 2) = T(0);
 }
 
 template <class T, bool SI, int MODE, bool COH = false>
@@ -764,8 +772,8 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
         u = u0 + Cu * qx0 + R1u * X + R3u * P;
       }
     }
-    FDP_F(p.QX, I, L) = qx;
-    FDP_F(p.UM, I, L) = u;
+    FDP_F(p.oQX, I, L) = qx;
+    FDP_F(p.oUM, I, L) = u;
   }
 
   // ---------------- qz and w: I = 2-TPML .. MX-1+TPML
@@ -864,8 +872,8 @@ __device__ __forceinline__ void velocity_cell(const Params<T>& p, const R& rd, i
       qz = E * qz0 - R1 * X - R2 * P;
       w = w0 + Cw * qz0 + R1w * X + R3w * P;
     }
-    FDP_F(p.QZ, I, L) = qz;
-    FDP_F(p.WM, I, L) = w;
+    FDP_F(p.oQZ, I, L) = qz;
+    FDP_F(p.oWM, I, L) = w;
   }
 }
 
@@ -907,7 +915,7 @@ __device__ __forceinline__ void velocity_unit(const Params<T>& p, int I0, int I1
     // hplane_pmlzh0_velocity.F90:34-63
     const int LST = p.PMLZH;
     const int x = I - p.PMLL;
-    T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+    T* const f[4] = {p.oUM, p.oWM, p.oQX, p.oQZ};  // this phase's new values
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
@@ -956,7 +964,9 @@ __device__ __forceinline__ void stress_sample_thread(const Params<T>& p, int g, 
 // previous velocity phase left final, and which this phase's stresses at
 // rows 2 and 3 read), and blocks n.. take the previous level's velocity
 // samples of the receivers (velocities stay unchanged through a stress
-// phase; row-1 samples are recomputed, not read).
+// phase; row-1 samples are recomputed, not read) and, with edge_prev = 2,
+// its stress samples too (when the stresses this kernel reads are the
+// previous level's, the new ones going to other arrays).
 template <class T, bool SI, int MODE>
 __global__ void __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? FDP_STRESS_FRAME_MIN_BLOCKS : 2) k_stress_frame(const __grid_constant__ Params<T> p,
                                                             const int4* __restrict__ units, int n, int it_off,
@@ -965,6 +975,7 @@ __global__ void __launch_bounds__(kBX * kBZ, sizeof(T) == 4 ? FDP_STRESS_FRAME_M
   const int tid = (int)(threadIdx.y * kBX + threadIdx.x);
   if (b >= n) {
     edge_thread<T, SI>(p, (SI ? p.NX : 0) + (b - n) * kBX * kBZ + tid, it_off - 1);
+    if (edge_prev == 2) stress_sample_thread<T>(p, (b - n) * kBX * kBZ + tid, it_off - 1);
     return;
   }
   const int4 u = units[b];
@@ -1010,7 +1021,7 @@ __device__ __forceinline__ void velocity_bottom_unit(const Params<T>& p, int I0,
   for (int L = LST - 2; L < LST; ++L)
     if (L >= (SI ? 2 : 0) && !(incol && L >= p.cv_z0 && L < p.cv_z1)) velocity_cell<T, SI, MODE>(p, rd, I, L);
   const int x = I - p.PMLL;
-  T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+  T* const f[4] = {p.oUM, p.oWM, p.oQX, p.oQZ};  // this phase's new values
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz
@@ -1094,32 +1105,36 @@ __device__ __forceinline__ T core_coef(const Params<T>& p, int k, long long cell
 // instead of 4.20 Gcell-updates/s with one CTA of up to 252 registers).
 #define FDP_CORE_BOUNDS(T) __launch_bounds__(kBX * kBZ, 2)
 
-// core block (bx, by) of a phase: 4*kBX columns by kBZ rows of its core
+// Inputs of the interior stress update of four consecutive cells of a row
+// (columns I0..I0+3, row L): row L of u, w and qx as three vectors each
+// (columns I0-4 .. I0+7) and the column values the z stencils need.
+template <class T> struct StressCoreIn {
+  V4<T> ur[3], wr[3], xr[3];
+  V4<T> um2, um1, up1, wm1, wp1, wp2, zm1, z0, zp1, zp2;
+};
+
+// Loads them from velocity arrays at the field offset c0 of (I0, L).
+template <class T>
+__device__ __forceinline__ void load_stress_core_in(StressCoreIn<T>& a, const T* U, const T* W, const T* X,
+                                                    const T* Z, long long P) {
+  a.ur[0] = ld4(U - 4); a.ur[1] = ld4(U); a.ur[2] = ld4(U + 4);
+  a.wr[0] = ld4(W - 4); a.wr[1] = ld4(W); a.wr[2] = ld4(W + 4);
+  a.xr[0] = ld4(X - 4); a.xr[1] = ld4(X); a.xr[2] = ld4(X + 4);
+  a.um2 = ld4(U - 2 * P); a.um1 = ld4(U - P); a.up1 = ld4(U + P);
+  a.wm1 = ld4(W - P); a.wp1 = ld4(W + P); a.wp2 = ld4(W + 2 * P);
+  a.zm1 = ld4(Z - P); a.z0 = ld4(Z); a.zp1 = ld4(Z + P); a.zp2 = ld4(Z + 2 * P);
+}
+
+// The interior stress update of the four cells (strain_uw_xz.F90:81-84,
+// strain_uw_zz.F90:51,58-59, strain_q_zz.F90:48,55-56, strain_uw_xx.F90:82-83,
+// strain_q_xx.F90:77-78, stress_xz.F90:44-46, stress_nn.F90:53-59): the old
+// stresses o* become the new ones.  Cell src_j (0..3, or -1 for none) is
+// the source cell of row LIN_Z, which adds the source term of
+// stress_lin_nn.F90:58-63 (srcS = (SOURS-SOURSP)/DT, srcF the fluid one).
 template <class T, int MODE>
-__device__ __forceinline__ void stress_core_block(const Params<T>& p, int bx, int by) {
-  const int I0 = p.cs_x0 + 4 * (int)(bx * kBX + threadIdx.x);
-  const int L = p.cs_z0 + (int)(by * kBZ + threadIdx.y);
-  if (I0 >= p.cs_x1 || L >= p.cs_z1 || L == p.LIN_Z) return;
-  const long long P = p.pitch;
-  const long long c0 = (long long)L * P + (I0 - p.PMLL);
-  const T* U = p.UM + c0;
-  const T* W = p.WM + c0;
-  const T* X = p.QX + c0;
-  const T* Z = p.QZ + c0;
-  // row L of u, w, qx with the vectors either side (columns I0-4 .. I0+7),
-  // and the column values the z stencils need
-  const V4<T> ur[3] = {ld4(U - 4), ld4(U), ld4(U + 4)};
-  const V4<T> wr[3] = {ld4(W - 4), ld4(W), ld4(W + 4)};
-  const V4<T> xr[3] = {ld4(X - 4), ld4(X), ld4(X + 4)};
-  const V4<T> um2 = ld4(U - 2 * P), um1 = ld4(U - P), up1 = ld4(U + P);
-  const V4<T> wm1 = ld4(W - P), wp1 = ld4(W + P), wp2 = ld4(W + 2 * P);
-  const V4<T> zm1 = ld4(Z - P), z0 = ld4(Z), zp1 = ld4(Z + P), zp2 = ld4(Z + 2 * P);
-  V4<T> oxz = ld4c(p.TXZ + c0), oxx = ld4c(p.TXX + c0), ozz = ld4c(p.TZZ + c0), opr = ld4c(p.PRES + c0);
-  V4<T> bio[5];
-  if constexpr (MODE == M_BIOT) {
-#pragma unroll
-    for (int s = 0; s < 5; ++s) bio[s] = ld4(p.bplane[s] + c0);
-  }
+__device__ __forceinline__ void stress_core_math(const Params<T>& p, long long c0, const StressCoreIn<T>& a,
+                                                 const V4<T>* bio, V4<T>& oxz, V4<T>& oxx, V4<T>& ozz,
+                                                 V4<T>& opr, int src_j = -1, T srcS = T(0), T srcF = T(0)) {
   // value of row vector r at column I0 + j + d, d in -4..7
   auto at = [](const V4<T>* r, int j, int d) { return r[(j + d + 4) >> 2].v[(j + d + 4) & 3]; };
 #pragma unroll
@@ -1128,16 +1143,16 @@ __device__ __forceinline__ void stress_core_block(const Params<T>& p, int bx, in
     const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
     auto C = [&](int k) { return core_coef<T, MODE>(p, k, cell_, J_, bio, 0, j); };
     // strain_uw_xz.F90:81-84
-    const T exz = p.AH * (up1.v[j] - um2.v[j] + at(wr, j, 1) - at(wr, j, -2))
-                + p.BH * (ur[1].v[j] - um1.v[j] + wr[1].v[j] - at(wr, j, -1));
+    const T exz = p.AH * (a.up1.v[j] - a.um2.v[j] + at(a.wr, j, 1) - at(a.wr, j, -2))
+                + p.BH * (a.ur[1].v[j] - a.um1.v[j] + a.wr[1].v[j] - at(a.wr, j, -1));
     // strain_uw_zz.F90:51,58-59 and strain_q_zz.F90:48,55-56
-    T ezz = (p.CH * (wp1.v[j] - wr[1].v[j]));
-    ezz = p.AH * (wp2.v[j] - wm1.v[j]) + p.BC * ezz;
-    T qzz = (p.CH * (zp1.v[j] - z0.v[j]));
-    qzz = p.AH * (zp2.v[j] - zm1.v[j]) + p.BC * qzz;
+    T ezz = (p.CH * (a.wp1.v[j] - a.wr[1].v[j]));
+    ezz = p.AH * (a.wp2.v[j] - a.wm1.v[j]) + p.BC * ezz;
+    T qzz = (p.CH * (a.zp1.v[j] - a.z0.v[j]));
+    qzz = p.AH * (a.zp2.v[j] - a.zm1.v[j]) + p.BC * qzz;
     // strain_uw_xx.F90:82-83 and strain_q_xx.F90:77-78
-    const T exx = p.AH * (at(ur, j, 2) - at(ur, j, -1)) + p.BH * (at(ur, j, 1) - ur[1].v[j]);
-    const T qxx = p.AH * (at(xr, j, 2) - at(xr, j, -1)) + p.BH * (at(xr, j, 1) - xr[1].v[j]);
+    const T exx = p.AH * (at(a.ur, j, 2) - at(a.ur, j, -1)) + p.BH * (at(a.ur, j, 1) - a.ur[1].v[j]);
+    const T qxx = p.AH * (at(a.xr, j, 2) - at(a.xr, j, -1)) + p.BH * (at(a.xr, j, 1) - a.xr[1].v[j]);
     // stress_xz.F90:44-46 and stress_nn.F90:53-59
     const T TXZv = C(C_MU) * exz;
     oxz.v[j] = oxz.v[j] + p.DTE * TXZv;
@@ -1147,19 +1162,106 @@ __device__ __forceinline__ void stress_core_block(const Params<T>& p, int bx, in
     const T TXXv = s1 * exx + s2 * ezz + s3 * qxx + s3 * qzz;
     const T TZZv = z1 * exx + z2 * ezz + z3 * qxx + z3 * qzz;
     const T PRv = q1 * exx + q2 * ezz + q3 * qxx + q3 * qzz;
-    oxx.v[j] = oxx.v[j] + p.DTE * TXXv;
-    ozz.v[j] = ozz.v[j] + p.DTE * TZZv;
-    opr.v[j] = opr.v[j] + p.DTE * PRv;
+    if (j == src_j) {
+      // stress_lin_nn.F90:58-63
+      oxx.v[j] = oxx.v[j] + p.DTE * (TXXv - srcS);
+      ozz.v[j] = ozz.v[j] + p.DTE * (TZZv - srcS);
+      opr.v[j] = opr.v[j] + p.DTE * (PRv + srcF);
+    } else {
+      oxx.v[j] = oxx.v[j] + p.DTE * TXXv;
+      ozz.v[j] = ozz.v[j] + p.DTE * TZZv;
+      opr.v[j] = opr.v[j] + p.DTE * PRv;
+    }
   }
-  st4(p.TXZ + c0, oxz);
-  st4(p.TXX + c0, oxx);
-  st4(p.TZZ + c0, ozz);
-  st4(p.PRES + c0, opr);
+}
+
+// core block (bx, by) of a phase: 4*kBX columns by kBZ rows of its core
+template <class T, int MODE>
+__device__ __forceinline__ void stress_core_block(const Params<T>& p, int bx, int by) {
+  const int I0 = p.cs_x0 + 4 * (int)(bx * kBX + threadIdx.x);
+  const int L = p.cs_z0 + (int)(by * kBZ + threadIdx.y);
+  if (I0 >= p.cs_x1 || L >= p.cs_z1 || L == p.LIN_Z) return;
+  const long long P = p.pitch;
+  const long long c0 = (long long)L * P + (I0 - p.PMLL);
+  // row L of u, w, qx with the vectors either side (columns I0-4 .. I0+7),
+  // and the column values the z stencils need
+  StressCoreIn<T> a;
+  load_stress_core_in(a, p.UM + c0, p.WM + c0, p.QX + c0, p.QZ + c0, P);
+  V4<T> oxz = ld4c(p.TXZ + c0), oxx = ld4c(p.TXX + c0), ozz = ld4c(p.TZZ + c0), opr = ld4c(p.PRES + c0);
+  V4<T> bio[5];
+  if constexpr (MODE == M_BIOT) {
+#pragma unroll
+    for (int s = 0; s < 5; ++s) bio[s] = ld4(p.bplane[s] + c0);
+  }
+  stress_core_math<T, MODE>(p, c0, a, bio, oxz, oxx, ozz, opr);
+  st4(p.oTXZ + c0, oxz);
+  st4(p.oTXX + c0, oxx);
+  st4(p.oTZZ + c0, ozz);
+  st4(p.oPRES + c0, opr);
 }
 
 template <class T, int MODE>
 __global__ void FDP_CORE_BOUNDS(T) k_stress_core(const __grid_constant__ Params<T> p) {
   stress_core_block<T, MODE>(p, (int)blockIdx.x, (int)blockIdx.y);
+}
+
+// Inputs of the interior velocity update of four consecutive cells of a
+// row (columns I0..I0+3, row L): row L of txx, p and txz as three vectors
+// each (columns I0-4 .. I0+7) and the column values the z stencils need.
+template <class T> struct VelocityCoreIn {
+  V4<T> xxr[3], prr[3], xzr[3];
+  V4<T> prm2, prm1, prp1, xzm1, xzp1, xzp2, zzm2, zzm1, zz0, zzp1;
+};
+
+template <class T>
+__device__ __forceinline__ void load_velocity_core_in(VelocityCoreIn<T>& a, const T* XX, const T* ZZ, const T* XZ,
+                                                      const T* PR, long long P) {
+  a.xxr[0] = ld4(XX - 4); a.xxr[1] = ld4(XX); a.xxr[2] = ld4(XX + 4);
+  a.prr[0] = ld4(PR - 4); a.prr[1] = ld4(PR); a.prr[2] = ld4(PR + 4);
+  a.xzr[0] = ld4(XZ - 4); a.xzr[1] = ld4(XZ); a.xzr[2] = ld4(XZ + 4);
+  a.prm2 = ld4(PR - 2 * P); a.prm1 = ld4(PR - P); a.prp1 = ld4(PR + P);
+  a.xzm1 = ld4(XZ - P); a.xzp1 = ld4(XZ + P); a.xzp2 = ld4(XZ + 2 * P);
+  a.zzm2 = ld4(ZZ - 2 * P); a.zzm1 = ld4(ZZ - P); a.zz0 = ld4(ZZ); a.zzp1 = ld4(ZZ + P);
+}
+
+// The interior velocity update of the four cells (inh_qx_int.F90:44-52,
+// inh_v_uv_int.F90:45-54, inh_qz_int.F90:45-53, inh_v_w_int.F90:47-56),
+// with the old q standing in for QXP/QZP: the old o* become the new ones.
+template <class T, int MODE>
+__device__ __forceinline__ void velocity_core_math(const Params<T>& p, long long c0, const VelocityCoreIn<T>& a,
+                                                   const V4<T>* bio, V4<T>& oqx, V4<T>& oum, V4<T>& oqz,
+                                                   V4<T>& owm) {
+  const T A = p.A, B = p.B;
+  auto at = [](const V4<T>* r, int j, int d) { return r[(j + d + 4) >> 2].v[(j + d + 4) & 3]; };
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const long long cell_ = c0 + j;
+    const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
+    auto C = [&](int k) { return core_coef<T, MODE>(p, k, cell_, J_, bio, 5, j); };
+    const T pr0 = a.prr[1].v[j];
+    {
+      // inh_qx_int.F90:44-52 and inh_v_uv_int.F90:45-54
+      const T E = C(C_EQX), Cu = C(C_CU);
+      const T R1 = C(C_R1QX), R2 = C(C_R2QX), R1u = C(C_R1U), R3u = C(C_R3U);
+      const T qx0 = oqx.v[j], u0 = oum.v[j];
+      const T Xs = A * (at(a.xxr, j, 1) - at(a.xxr, j, -2) + a.xzp2.v[j] - a.xzm1.v[j])
+                 + B * (a.xxr[1].v[j] - at(a.xxr, j, -1) + a.xzp1.v[j] - a.xzr[1].v[j]);
+      const T Pp = A * (at(a.prr, j, 1) - at(a.prr, j, -2)) + B * (pr0 - at(a.prr, j, -1));
+      oqx.v[j] = E * qx0 - R1 * Xs - R2 * Pp;
+      oum.v[j] = u0 + Cu * qx0 + R1u * Xs + R3u * Pp;
+    }
+    {
+      // inh_qz_int.F90:45-53 and inh_v_w_int.F90:47-56
+      const T E = C(C_EQZ), Cw = C(C_CW);
+      const T R1 = C(C_R1QZ), R2 = C(C_R2QZ), R1w = C(C_R1W), R3w = C(C_R3W);
+      const T qz0 = oqz.v[j], w0 = owm.v[j];
+      const T Xs = A * (a.zzp1.v[j] - a.zzm2.v[j] + at(a.xzr, j, 2) - at(a.xzr, j, -1))
+                 + B * (a.zz0.v[j] - a.zzm1.v[j] + at(a.xzr, j, 1) - a.xzr[1].v[j]);
+      const T Pp = A * (a.prp1.v[j] - a.prm2.v[j]) + B * (pr0 - a.prm1.v[j]);
+      oqz.v[j] = E * qz0 - R1 * Xs - R2 * Pp;
+      owm.v[j] = w0 + Cw * qz0 + R1w * Xs + R3w * Pp;
+    }
+  }
 }
 
 template <class T, int MODE>
@@ -1169,57 +1271,19 @@ __device__ __forceinline__ void velocity_core_block(const Params<T>& p, int bx, 
   if (I0 >= p.cv_x1 || L >= p.cv_z1) return;
   const long long P = p.pitch;
   const long long c0 = (long long)L * P + (I0 - p.PMLL);
-  const T A = p.A, B = p.B;
-  const T* XX = p.TXX + c0;
-  const T* ZZ = p.TZZ + c0;
-  const T* XZ = p.TXZ + c0;
-  const T* PR = p.PRES + c0;
-  const V4<T> xxr[3] = {ld4(XX - 4), ld4(XX), ld4(XX + 4)};
-  const V4<T> prr[3] = {ld4(PR - 4), ld4(PR), ld4(PR + 4)};
-  const V4<T> xzr[3] = {ld4(XZ - 4), ld4(XZ), ld4(XZ + 4)};
-  const V4<T> prm2 = ld4(PR - 2 * P), prm1 = ld4(PR - P), prp1 = ld4(PR + P);
-  const V4<T> xzm1 = ld4(XZ - P), xzp1 = ld4(XZ + P), xzp2 = ld4(XZ + 2 * P);
-  const V4<T> zzm2 = ld4(ZZ - 2 * P), zzm1 = ld4(ZZ - P), zz0 = ld4(ZZ), zzp1 = ld4(ZZ + P);
+  VelocityCoreIn<T> a;
+  load_velocity_core_in(a, p.TXX + c0, p.TZZ + c0, p.TXZ + c0, p.PRES + c0, P);
   V4<T> oqx = ld4c(p.QX + c0), oum = ld4c(p.UM + c0), oqz = ld4c(p.QZ + c0), owm = ld4c(p.WM + c0);
   V4<T> bio[5];
   if constexpr (MODE == M_BIOT) {
 #pragma unroll
     for (int s = 0; s < 5; ++s) bio[s] = ld4(p.bplane[5 + s] + c0);
   }
-  auto at = [](const V4<T>* r, int j, int d) { return r[(j + d + 4) >> 2].v[(j + d + 4) & 3]; };
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const long long cell_ = c0 + j;
-    const int J_ = (MODE == M_TABLE) ? p.JM[cell_] : 0;
-    auto C = [&](int k) { return core_coef<T, MODE>(p, k, cell_, J_, bio, 5, j); };
-    const T pr0 = prr[1].v[j];
-    {
-      // inh_qx_int.F90:44-52 and inh_v_uv_int.F90:45-54
-      const T E = C(C_EQX), Cu = C(C_CU);
-      const T R1 = C(C_R1QX), R2 = C(C_R2QX), R1u = C(C_R1U), R3u = C(C_R3U);
-      const T qx0 = oqx.v[j], u0 = oum.v[j];
-      const T Xs = A * (at(xxr, j, 1) - at(xxr, j, -2) + xzp2.v[j] - xzm1.v[j])
-                 + B * (xxr[1].v[j] - at(xxr, j, -1) + xzp1.v[j] - xzr[1].v[j]);
-      const T Pp = A * (at(prr, j, 1) - at(prr, j, -2)) + B * (pr0 - at(prr, j, -1));
-      oqx.v[j] = E * qx0 - R1 * Xs - R2 * Pp;
-      oum.v[j] = u0 + Cu * qx0 + R1u * Xs + R3u * Pp;
-    }
-    {
-      // inh_qz_int.F90:45-53 and inh_v_w_int.F90:47-56
-      const T E = C(C_EQZ), Cw = C(C_CW);
-      const T R1 = C(C_R1QZ), R2 = C(C_R2QZ), R1w = C(C_R1W), R3w = C(C_R3W);
-      const T qz0 = oqz.v[j], w0 = owm.v[j];
-      const T Xs = A * (zzp1.v[j] - zzm2.v[j] + at(xzr, j, 2) - at(xzr, j, -1))
-                 + B * (zz0.v[j] - zzm1.v[j] + at(xzr, j, 1) - xzr[1].v[j]);
-      const T Pp = A * (prp1.v[j] - prm2.v[j]) + B * (pr0 - prm1.v[j]);
-      oqz.v[j] = E * qz0 - R1 * Xs - R2 * Pp;
-      owm.v[j] = w0 + Cw * qz0 + R1w * Xs + R3w * Pp;
-    }
-  }
-  st4(p.QX + c0, oqx);
-  st4(p.UM + c0, oum);
-  st4(p.QZ + c0, oqz);
-  st4(p.WM + c0, owm);
+  velocity_core_math<T, MODE>(p, c0, a, bio, oqx, oum, oqz, owm);
+  st4(p.oQX + c0, oqx);
+  st4(p.oUM + c0, oum);
+  st4(p.oQZ + c0, oqz);
+  st4(p.oWM + c0, owm);
 }
 
 template <class T, int MODE>
@@ -1612,13 +1676,7 @@ __global__ void __launch_bounds__(kTX * 4) k_stress_tma(const __grid_constant__ 
     __syncthreads();  // rows 2..4 of this tile are final
     if (ok && I <= p.PMLXH && threadIdx.y == 0) {
       // hplane_0_stress.F90:49-53 and hplane_1_stress.F90:45-53
-      FDP_F(p.TXZ, I, 0) = -FDP_F(p.TXZ, I, 4);
-      FDP_F(p.TZZ, I, 0) = -FDP_F(p.TZZ, I, 3);
-      FDP_F(p.PRES, I, 0) = -FDP_F(p.PRES, I, 3);
-      FDP_F(p.TXZ, I, 1) = -FDP_F(p.TXZ, I, 3);
-      FDP_F(p.TZZ, I, 1) = -FDP_F(p.TZZ, I, 2);
-      FDP_F(p.PRES, I, 1) = -FDP_F(p.PRES, I, 2);
-      FDP_F(p.TXZ, I, 2) = T(0);
+      stress_mirror(p, I);
     }
   }
   if (!ok) mbar_wait_bounded(&bar, 0);  // let copies still in flight land before the CTA exits
@@ -1680,7 +1738,7 @@ __global__ void __launch_bounds__(kTX * 4) k_velocity_tma(const __grid_constant_
     if (owns_bottom) {
       // hplane_pmlzh0_velocity.F90:34-63
       const int LST = p.PMLZH, x = I - p.PMLL;
-      T* const f[4] = {p.UM, p.WM, p.QX, p.QZ};
+      T* const f[4] = {p.oUM, p.oWM, p.oQX, p.oQZ};  // this phase's new values
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         const T* ab = p.AB + ((c == 0 || c == 2) ? 8 : 0);  // ABH for u, qx; ABW for w, qz

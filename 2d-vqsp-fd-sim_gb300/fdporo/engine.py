@@ -163,6 +163,16 @@ class Engine:
         self._check(self.lib.fdp_core_info(self._ctx, _iptr(r)))
         return {"stress": tuple(int(v) for v in r[:4]), "velocity": tuple(int(v) for v in r[4:])}
 
+    def march_info(self) -> dict | None:
+        """Region and launch shape of the march kernel (fdp_march_info), or
+        None when the levels do not run as march levels."""
+        r, sh = np.zeros(8, np.int32), np.zeros(4, np.int32)
+        self._check(self.lib.fdp_march_info(self._ctx, _iptr(r), _iptr(sh)))
+        if not sh[0]:
+            return None
+        return {"region": tuple(int(v) for v in r[:4]), "stress_writes": tuple(int(v) for v in r[4:]),
+                "strips": int(sh[0]), "band_rows": int(sh[1]), "ctas": int(sh[2]), "warps": int(sh[3])}
+
     def profile(self, it_begin: int, it_end: int) -> dict:
         """Device time (ms) and launch counts over levels it_begin..it_end of
         each phase (frame and core together), of the row-1/receiver kernel,

@@ -85,6 +85,7 @@ SIGNATURES = {
     "fdp_get_stream": (C.c_int, [_VP, C.POINTER(_VP)]),
     "fdp_medium_info": (C.c_int, [_VP, _PI32, _PI32, _PI32]),
     "fdp_core_info": (C.c_int, [_VP, _PI32]),
+    "fdp_march_info": (C.c_int, [_VP, _PI32, _PI32]),
     "fdp_profile_run": (C.c_int, [_VP, _I32, _I32, _PD, C.POINTER(C.c_int64)]),
     "fdp_last_error": (C.c_char_p, [_VP]),
     "fdp_receivers_noalloc": (C.c_int, [_I32, _VP, _VP, _VP, _VP, _VP, _VP, _I32, _I32, _I32, _I32, _VP, _I32,

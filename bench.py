@@ -79,7 +79,7 @@ def prepare_inputs(precision: str, mt2: int):
     return job.prepare(cfg, med, precision)
 
 
-def algorithmic_bytes(inp, s: int, medium: dict, core: dict | None = None) -> dict:
+def algorithmic_bytes(inp, s: int, medium: dict, core: dict | None = None, march: dict | None = None) -> dict:
     """Compulsory DRAM bytes per launch of each phase for this workload:
     every wavefield value the phase reads or read-modify-writes, the
     material coefficients of each cell as the engine holds them (one value
@@ -114,6 +114,20 @@ def algorithmic_bytes(inp, s: int, medium: dict, core: dict | None = None) -> di
         out["stress_core"] = ns * (12 * s + med_s)
         out["velocity_core"] = nv * (12 * s + med_v)
         out["core_cells"] = {"stress": ns, "velocity": nv}
+    if march:
+        # the march kernel: per cell of its region the old velocities and
+        # stresses read once, the new velocities written, and the medium of
+        # both phases; the new stresses written where it writes them (the
+        # frame kernels write the band along its edges)
+        x0, x1, z0, z1 = march["region"]
+        nf = (x1 - x0) * (z1 - z0)
+        x0, x1, z0, z1 = march["stress_writes"]
+        nw = (x1 - x0) * (z1 - z0)
+        out["march"] = nf * (12 * s + med_s + med_v) + nw * 4 * s
+        # the whole level: both phases' bytes less the second reads of the
+        # new stresses and the old velocities that the march kernel saves
+        out["level"] = stress + velocity - nf * 8 * s
+        out["march_cells"] = {"region": nf, "stress_writes": nw}
     return out
 
 
@@ -307,18 +321,27 @@ def run_gpu(args) -> None:
     prof = eng.profile(lo, lo + prof_levels - 1)
     medium = eng.medium_info()
     core = eng.core_info()
-    alg = algorithmic_bytes(inp, s, medium, core)
+    march = eng.march_info()
+    alg = algorithmic_bytes(inp, s, medium, core, march)
     phases = ("stress", "velocity", "edge")
-    shares = {k: prof[k][0] / sum(prof[q][0] for q in phases) for k in phases}
+    shares = {k: prof[k][0] / max(sum(prof[q][0] for q in phases), 1e-30) for k in phases}
     peak, peak_kind = measured_peak_gbs()
-    # the dominant kernel: that of the longer phase -- its core kernel when
-    # the phase runs as frame and core kernels on two streams, else the
-    # phase's one kernel
-    phase = max(("stress", "velocity"), key=lambda k: prof[k][0])
-    kern = f"{phase}_core" if prof[f"{phase}_core"][1] > 0 else phase
-    avg_ms = prof[kern][0] / prof[kern][1]
+    if march:
+        # one pass per level over the deep interior (the march kernel) beside
+        # the frame kernels: the level's time is entry "stress" of the profile
+        kern = "march"
+        avg_ms = prof["stress_core"][0] / prof["stress_core"][1]
+        level_ms = prof["stress"][0] / prof["stress"][1]
+        phase_gbs = {"level": alg["level"] / (level_ms / 1e3) / 1e9}
+    else:
+        # the dominant kernel: that of the longer phase -- its core kernel
+        # when the phase runs as frame and core kernels on two streams, else
+        # the phase's one kernel
+        phase = max(("stress", "velocity"), key=lambda k: prof[k][0])
+        kern = f"{phase}_core" if prof[f"{phase}_core"][1] > 0 else phase
+        avg_ms = prof[kern][0] / prof[kern][1]
+        phase_gbs = {k: alg[k] / (prof[k][0] / prof[k][1] / 1e3) / 1e9 for k in ("stress", "velocity")}
     achieved = alg[kern] / (avg_ms / 1e3) / 1e9
-    phase_gbs = {k: alg[k] / (prof[k][0] / prof[k][1] / 1e3) / 1e9 for k in ("stress", "velocity")}
     eng.close()
 
     # ---- end to end through the C ABI: one whole shot (create, upload, run, download)
@@ -401,7 +424,8 @@ def run_gpu(args) -> None:
                      "alg_bytes_per_cell": {"stress": alg["per_cell_stress"], "velocity": alg["per_cell_velocity"]},
                      "kernel_ms": {k: prof[k][0] / max(prof[k][1], 1) for k in prof},
                      "phase_gbs": phase_gbs, "phase_frac": {k: v / peak for k, v in phase_gbs.items()},
-                     "core_cells": alg.get("core_cells"), "medium": medium, "phase_share": shares},
+                     "core_cells": alg.get("core_cells"), "march": march, "march_cells": alg.get("march_cells"),
+                     "medium": medium, "phase_share": shares},
         "e2e": e2e,
         "accuracy": accuracy,
         "batch": batch,

@@ -107,7 +107,8 @@ enum fdp_field_id {
  * phase in one launch; "global" runs one unit kernel per phase over the
  * whole grid; "tma" the TMA-staged variant of the latter; "coretma" the
  * default split with TMA-staged persistent core kernels (FP32 contexts with
- * a Biot-plane medium; others keep the per-thread-load core). */
+ * a Biot-plane medium; others keep the per-thread-load core); "march" both
+ * phases of the deep interior in one pass (fdp_march_info). */
 int fdp_create(const fdp_grid* grid, fdp_ctx** out);
 
 /* Medium: JM(PMLL:PMLXH, 0:PMLZH) (nx = MX+2*TPML, nz = PMLZH+1) after
@@ -242,6 +243,21 @@ int fdp_medium_info(fdp_ctx* ctx, int32_t* mode, int32_t* planes_stress, int32_t
  * columns [x0, x1) and rows [z0, z1) (the source row excluded), rect[4..7]
  * the velocity core; zeros when the context runs other kernels. */
 int fdp_core_info(fdp_ctx* ctx, int32_t* rect8);
+
+/* The march variant (FDP_KERNEL_VARIANT=march): each level's deep
+ * interior in one kernel pass (stress phase, then velocity phase, from
+ * bands of rows staged in shared memory by bulk tensor copies), the levels
+ * alternating between two buffers of each wavefield array, with the frame
+ * kernels on the side stream.  region8 = the columns [x0, x1) and rows
+ * [z0, z1) the march kernel updates, then those where it writes the new
+ * stresses (the frame kernels write a band along the edges); shape4 =
+ * strips of 30 four-cell vectors across, rows per band, CTAs of the
+ * launch, warps per CTA.  All zero when the context's levels do not run as
+ * march levels (another variant, FP64, a medium not held as Biot planes, a
+ * grid too small, a batch or an attached learned edge holding it).  No
+ * counterpart in the reference (a kernel arrangement of
+ * time_loop.F90:93-179). */
+int fdp_march_info(fdp_ctx* ctx, int32_t* region8, int32_t* shape4);
 
 /* Last error message of the context (or of the last failed call that has
  * no context -- fdp_create, fdp_receivers_noalloc -- when ctx is NULL). */

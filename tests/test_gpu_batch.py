@@ -129,3 +129,28 @@ def test_batch_rejects_bad_shots():
     with pytest.raises(FdpError) as err:
         Batch([a, a])
     assert err.value.code == -1
+
+
+def test_march_shots_in_and_out_of_a_batch(monkeypatch):
+    """Contexts made with the march variant alternate between two buffers of
+    each field when run alone; a batch holding them updates them in place.
+    Levels run alone (an odd number, so the current buffers are the second
+    ones), then in a batch, then alone again equal the oracle bit for bit."""
+    from fdporo.engine import Batch
+    monkeypatch.setenv("FDP_KERNEL_VARIANT", "march")
+    engs, orcs = _shots("f32", True, per_cell=True, nsteps=60)
+    assert engs[1].march_info() is not None
+    for e in engs:
+        e.time_loop(1, 7)
+    with Batch(engs) as b:
+        assert engs[1].march_info() is None  # the batch holds it: in-place levels
+        b.set_shape(-1, 0)
+        b.time_loop(8, 45)
+        b.synchronize()
+    assert engs[1].march_info() is not None
+    for e in engs:
+        e.time_loop(46, 60)
+    for e, o in zip(engs, orcs):
+        o.time_loop(1, 60)
+        compare_state(e, o)
+        np.testing.assert_array_equal(e.receivers(1, 60), o.receivers(1, 60))

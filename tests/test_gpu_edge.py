@@ -136,3 +136,25 @@ def test_training_is_bit_reproducible():
         params.append(ed.params())
     assert np.any(params[0] != 0)
     np.testing.assert_array_equal(params[0], params[1])
+
+
+def test_attached_edge_runs_march_contexts_in_place(monkeypatch):
+    """A context made with the march variant runs its levels in place while a
+    learned edge is attached (the edge's kernels work on the current buffers
+    after every level); with a fresh edge, whose corrections are zero, it
+    equals the same context without one, which runs march levels."""
+    from fdporo import edge as E
+    from fdporo import job
+    monkeypatch.setenv("FDP_KERNEL_VARIANT", "march")
+    pair = E.make_pair(11, n=96, margin=40, depth_margin=60, nsteps=80)
+    a, b = job.make_engine(pair.trunc), job.make_engine(pair.trunc)
+    assert a.march_info() is not None
+    E.Edge(seed=1).attach(b)
+    assert b.march_info() is None
+    a.time_loop(1, 33)
+    b.time_loop(1, 33)
+    a.time_loop(34, 80)
+    b.time_loop(34, 80)
+    b.synchronize()
+    compare_state(a, b)
+    assert np.abs(a.field("UM")).max() > 0

@@ -1,0 +1,111 @@
+"""The march variant against the oracle.
+
+With FDP_KERNEL_VARIANT=march, an FP32 context whose medium is held as the
+ten Biot planes runs each level's deep interior as one kernel pass (the
+stress phase, then the velocity phase, from bands of rows staged in shared
+memory by bulk tensor copies), beside the frame kernels on the side stream,
+and the levels alternate between two buffers of each wavefield array.
+Every field, PML memory variable, the bottom history and every receiver
+value must equal the oracle's bit for bit: from random states and from
+rest, both free-surface modes, grids whose width leaves a partial strip,
+sources inside the march region, runs of odd length (which end in the
+other buffers), any split of the rows among the CTAs, and the full 2048^2
+layered grid.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import compare_state, randomize_state, small_job
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def march(monkeypatch):
+    monkeypatch.setenv("FDP_KERNEL_VARIANT", "march")
+
+
+def _pair(cfg, med, prec="f32"):
+    from fdporo import job
+    from oracle.oracle import make_oracle
+    inp = job.prepare(cfg, med, prec)
+    return inp, job.make_engine(inp), make_oracle(inp)
+
+
+@pytest.mark.parametrize("si", [True, False])
+@pytest.mark.parametrize("mx,mz", [(72, 56), (160, 100), (251, 90), (300, 40)])
+def test_random_state(si, mx, mz):
+    cfg, med = small_job(mx=mx, mz=mz, tpml=6, nsteps=40, si=si, per_cell=True, seed=mx + mz)
+    inp, eng, orc = _pair(cfg, med)
+    info = eng.march_info()
+    assert info is not None
+    assert info["strips"] == -(-((info["region"][1] - info["region"][0]) // 4) // 30)
+    randomize_state([eng, orc], inp, seed=7)
+    for a, b in ((1, 1), (2, 9), (10, 40)):
+        eng.time_loop(a, b)
+        orc.time_loop(a, b)
+        compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 40), orc.receivers(1, 40))
+
+
+@pytest.mark.parametrize("si", [True, False])
+def test_shot_from_rest_with_the_source_inside(si):
+    cfg, med = small_job(mx=160, mz=120, tpml=8, nsteps=70, si=si, per_cell=True, seed=77, n_rec=9)
+    inp, eng, orc = _pair(cfg, med)
+    x0, x1, z0, z1 = eng.march_info()["region"]
+    assert x0 <= inp.lin_x < x1 and z0 <= inp.lin_z < z1
+    eng.time_loop(1, 70)
+    orc.time_loop(1, 70)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 70), orc.receivers(1, 70))
+    assert np.abs(orc.field("PRES")).max() > 0
+
+
+@pytest.mark.parametrize("ctas", [1, 2, 5, 13, 152])
+def test_any_split_of_the_rows_among_ctas(ctas, monkeypatch):
+    monkeypatch.setenv("FDP_MARCH_CTAS", str(ctas))
+    cfg, med = small_job(mx=200, mz=70, tpml=5, nsteps=12, si=True, per_cell=True, seed=90 + ctas)
+    inp, eng, orc = _pair(cfg, med)
+    info = eng.march_info()
+    assert info["ctas"] == min(ctas, info["strips"] * (info["region"][3] - info["region"][2]))
+    randomize_state([eng, orc], inp, seed=91)
+    eng.time_loop(1, 12)
+    orc.time_loop(1, 12)
+    compare_state(eng, orc)
+
+
+def test_launch_count():
+    """Per level the stress and the velocity frame kernel and the march
+    kernel; per captured run (32, 32 and 6 levels) one k_edge and one
+    level-counter update; one level-counter reset per run of fdp_run."""
+    cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=70, per_cell=True, seed=31)
+    inp, eng, _ = _pair(cfg, med)
+    assert eng.march_info() is not None
+    n0 = eng.kernel_launches()
+    eng.time_loop(1, 70)
+    eng.synchronize()
+    assert eng.kernel_launches() - n0 == 70 * 3 + 3 * 2 + 1
+
+
+def test_fp64_and_table_media_keep_the_split():
+    cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=10, per_cell=True, seed=5)
+    _, e64, _ = _pair(cfg, med, "f64")
+    assert e64.march_info() is None
+    cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=10, per_cell=False, seed=5)
+    _, etab, _ = _pair(cfg, med)
+    assert etab.march_info() is None
+
+
+def test_layered_2048_full_grid():
+    from fdporo import job
+    from oracle.oracle import make_oracle
+    cfg, med = job.layered(mx=2048, mz=2048, nsteps=101)
+    inp = job.prepare(cfg, med, "f32")
+    eng, orc = job.make_engine(inp), make_oracle(inp, threads=min(16, os.cpu_count() or 1))
+    assert eng.march_info() is not None
+    eng.time_loop(1, 101)
+    orc.time_loop(1, 101)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 101), orc.receivers(1, 101))

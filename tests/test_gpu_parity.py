@@ -14,13 +14,15 @@ from helpers import compare_state, randomize_state, small_job
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(autouse=True, params=["core", "fused", "global", "tma", "coretma"])
+@pytest.fixture(autouse=True, params=["core", "fused", "global", "tma", "coretma", "march"])
 def kernel_variant(request, monkeypatch):
     """Runs every test with each kernel variant fdp_create can select through
     FDP_KERNEL_VARIANT: the frame/core split on two streams (the default)
     or in one launch per phase, the unit kernels over the whole grid, the
-    TMA-staged kernels, and the split with TMA-staged persistent core
-    kernels (FP32 Biot media; the others keep the per-thread-load core)."""
+    TMA-staged kernels, the split with TMA-staged persistent core kernels
+    (FP32 Biot media; the others keep the per-thread-load core), and the
+    march kernel doing both phases of the deep interior in one pass (FP32
+    Biot media; the others keep the split)."""
     monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
     return request.param
 
@@ -129,7 +131,9 @@ def test_kernel_launch_count(kernel_variant):
     eng.time_loop(1, 70)
     eng.synchronize()
     runs = 3
-    if kernel_variant in ("core", "coretma"):
+    if kernel_variant in ("core", "coretma", "march"):
+        # (a table medium: the march variant leaves it to the split)
+        assert eng.march_info() is None
         core = eng.core_info()
         assert all(x1 > x0 and z1 > z0 for x0, x1, z0, z1 in core.values())
         expected = 70 * 4 + runs * 2 + 1

@@ -20,10 +20,19 @@ pytestmark = pytest.mark.gpu
 SPLITS = [(1, 1), (2, 3), (4, 34), (35, 66), (67, 67), (68, 100)]
 
 
+@pytest.fixture(params=["core", "march"])
+def variant(request, monkeypatch):
+    """The default split and the march variant, whose levels alternate
+    between two buffers of each field (runs of odd length end in the other
+    buffers)."""
+    monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("si", [True, False])
 @pytest.mark.parametrize("n_rec", [9, 0])
-def test_split_runs_match_oracle(prec, si, n_rec):
+def test_split_runs_match_oracle(prec, si, n_rec, variant):
     from fdporo import job
     from oracle.oracle import make_oracle
     cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=100, si=si, per_cell=True, seed=81, n_rec=max(n_rec, 1))
@@ -41,7 +50,7 @@ def test_split_runs_match_oracle(prec, si, n_rec):
             np.testing.assert_array_equal(eng.receivers(1, b), orc.receivers(1, b))
 
 
-def test_one_long_run_equals_split_runs():
+def test_one_long_run_equals_split_runs(variant):
     from fdporo import job
     cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=100, si=True, per_cell=True, seed=83, n_rec=11)
     inp = job.prepare(cfg, med, "f32")
@@ -53,7 +62,7 @@ def test_one_long_run_equals_split_runs():
     np.testing.assert_array_equal(whole.receivers(1, 100), split.receivers(1, 100))
 
 
-def test_prepared_graphs_give_the_same_levels():
+def test_prepared_graphs_give_the_same_levels(variant):
     """fdp_prepare_run captures the graphs of a run length ahead of the run;
     the prepared run, later runs of the same length (graph replays of an
     already captured graph) and the oracle agree bit for bit, and preparing

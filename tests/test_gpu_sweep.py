@@ -62,3 +62,34 @@ def test_random_case_matches_oracle(k, monkeypatch):
         orc.time_loop(a, b)
     compare_state(eng, orc)
     np.testing.assert_array_equal(eng.receivers(1, c["levels"]), orc.receivers(1, c["levels"]))
+
+
+@pytest.mark.parametrize("k", range(80))
+def test_random_case_matches_oracle_march(k, monkeypatch):
+    """Other draws with the march variant and any number of CTAs (FP64,
+    table media and grids too small for its region run the split)."""
+    from fdporo import job
+    from oracle.oracle import make_oracle
+    c = _case(500 + k)
+    monkeypatch.setenv("FDP_KERNEL_VARIANT", "march")
+    monkeypatch.setenv("FDP_MARCH_CTAS", str(1 + k % 13))
+    cfg, med = small_job(mx=c["mx"], mz=c["mz"], tpml=c["tpml"], nsteps=c["levels"], si=c["si"],
+                         per_cell=True, seed=c["seed"], n_rec=c["n_rec"], ktbo=c["ktbo"],
+                         wc=200.0 if c["ktbo"] else 0.0)
+    if c["ktbo"]:
+        cfg.omg = 60.0
+    try:
+        inp = job.prepare(cfg, med, c["prec"])
+    except Exception as ex:
+        pytest.skip(f"set-up refuses {c}: {ex}")
+    if not (2 <= inp.lin_z <= c["mz"] - 2):
+        pytest.skip(f"source row {inp.lin_z} outside 2..MZ-2 for {c}")
+    eng, orc = job.make_engine(inp), make_oracle(inp)
+    randomize_state([eng, orc], inp, seed=c["seed"] + 1)
+    for a, b in ((1, c["split"]), (c["split"] + 1, c["levels"])):
+        if a > b:
+            continue
+        eng.time_loop(a, b)
+        orc.time_loop(a, b)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, c["levels"]), orc.receivers(1, c["levels"]))
