@@ -80,41 +80,24 @@ struct MarchGrid {
 
 // A band of a CTA: strip, the velocity rows [vlo, vhi) of its segment and
 // its index k there; its stresses are rows [vlo-2+8k, vlo+6+8k) and its
-// velocities rows [vlo-4+8k, vlo+4+8k).
+// velocities rows [vlo-4+8k, vlo+4+8k).  strip < 0: past the CTA's range.
 struct MarchBand {
   int strip, vlo, vhi, k;
 };
 
-// The rows [lo, hi) of a CTA in the sequence of all strips' rows (H rows per
-// strip), as segments of one strip each and bands of kMarchR rows.
-struct MarchRange {
-  long long lo, hi;
-  int H;
-  __device__ __forceinline__ int bands_of(int vlo, int vhi) const { return (vhi - vlo + 4 + kMarchR - 1) / kMarchR; }
-  // segment `s` of the range (strip, vlo, vhi), false past the last
-  __device__ __forceinline__ bool segment(int s, int fz0, int& strip, int& vlo, int& vhi) const {
-    const long long first = lo / H + s;
-    if (lo >= hi || first * H >= hi) return false;
-    strip = (int)first;
-    vlo = fz0 + (int)(first * H >= lo ? 0 : lo - first * H);
-    vhi = fz0 + (int)((first + 1) * H <= hi ? H : hi - first * H);
-    return true;
-  }
-  __device__ __forceinline__ int count(int fz0) const {
-    int n = 0, st, a, b;
-    for (int s = 0; segment(s, fz0, st, a, b); ++s) n += bands_of(a, b);
-    return n;
-  }
-  __device__ __forceinline__ MarchBand band(int i, int fz0) const {
-    int st = 0, a = 0, b = 0;
-    for (int s = 0; segment(s, fz0, st, a, b); ++s) {
-      const int n = bands_of(a, b);
-      if (i < n) return {st, a, b, i};
-      i -= n;
-    }
-    return {st, a, b, i};
-  }
-};
+// 16 bytes of shared memory (a 16-byte-aligned shared address)
+__device__ __forceinline__ V4<float> lds4s(const float* s) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"((uint32_t)__cvta_generic_to_shared(s)));
+  return {{v.x, v.y, v.z, v.w}};
+}
+__device__ __forceinline__ void sts4s(float* s, const V4<float>& v) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"((uint32_t)__cvta_generic_to_shared(s)), "f"(v.v[0]),
+               "f"(v.v[1]), "f"(v.v[2]), "f"(v.v[3])
+               : "memory");
+}
 
 template <int MODE>
 __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constant__ Params<float> p,
@@ -127,22 +110,30 @@ __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constan
   __shared__ __align__(8) uint64_t full[2];
   __shared__ int failed;
   const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  MarchRange rg;
-  rg.H = g.fz1 - g.fz0;
-  rg.lo = (long long)blockIdx.x * g.total / gridDim.x;
-  rg.hi = (long long)(blockIdx.x + 1) * g.total / gridDim.x;
-  const int nbands = rg.count(g.fz0);
+  // the CTA's rows [lo, hi) of the sequence of all strips' rows (H per strip)
+  const int H = g.fz1 - g.fz0;
+  const long long lo = (long long)blockIdx.x * g.total / gridDim.x;
+  const long long hi = (long long)(blockIdx.x + 1) * g.total / gridDim.x;
+  auto seg_end = [&](int strip) {  // the end of strip `strip`'s rows in the range
+    const long long e = (long long)(strip + 1) * H;
+    return g.fz0 + (int)((e <= hi ? e : hi) - (long long)strip * H);
+  };
+  auto next = [&](const MarchBand& b) -> MarchBand {
+    if (b.k + 1 < (b.vhi - b.vlo + 4 + kMarchR - 1) / kMarchR) return {b.strip, b.vlo, b.vhi, b.k + 1};
+    const int s = b.strip + 1;
+    if ((long long)s * H >= hi) return {-1, 0, 0, 0};
+    return {s, g.fz0, seg_end(s), 0};
+  };
   if (tid == 0) {
     mbar_init(&full[0], 1);
     mbar_init(&full[1], 1);
     failed = 0;
   }
   __syncthreads();
-  if (nbands == 0) return;
+  if (lo >= hi) return;
 
-  // the copies of the CTA's i-th band into stage i % 2 (and the velocity ring)
-  auto issue = [&](int i) {
-    const MarchBand b = rg.band(i, g.fz0);
+  // the copies of band b (the CTA's i-th) into stage i % 2 and the velocity ring
+  auto issue = [&](const MarchBand& b, int i) {
     uint64_t* bar = &full[i & 1];
     float* st = stages + (i & 1) * kMarchStage;
     const int x = g.fx0 + 4 * kMarchVec * b.strip - 4 - p.PMLL + kPadX;  // padded column of the box
@@ -179,14 +170,14 @@ __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constan
   }
   const int lm = lane > 0 ? lane - 1 : 0, lp = lane < 31 ? lane + 1 : 31;  // x-neighbour vectors (clamped)
 
-  if (tid == 0) issue(0);
-  bool issued_next = false;
+  const int strip0 = (int)(lo / H);
+  MarchBand b = {strip0, g.fz0 + (int)(lo - (long long)strip0 * H), seg_end(strip0), 0};
+  if (tid == 0) issue(b, 0);
+  bool issued = true;  // the copies of band i are issued
   int i = 0;
-  for (; i < nbands; ++i) {
-    const MarchBand b = rg.band(i, g.fz0);
-    const int st = i & 1;
-    if (tid == 0 && !issued_next && i > 0) issue(i);  // a new segment: its first band was not prefetched
-    if (!mbar_wait_bounded(&full[st], (uint32_t)((i >> 1) & 1))) failed = 1;
+  for (; b.strip >= 0; ++i) {
+    if (tid == 0 && !issued) issue(b, i);  // a new segment: its first band was not prefetched
+    if (!mbar_wait_bounded(&full[i & 1], (uint32_t)((i >> 1) & 1))) failed = 1;
     __syncthreads();
     if (failed) {
       if (tid == 0) atomicOr(p.err, 1);
@@ -194,46 +185,53 @@ __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constan
     }
     // prefetch the next band of the same segment (the next segment's first
     // band would overwrite ring rows this band reads)
-    issued_next = false;
-    if (i + 1 < nbands && rg.band(i + 1, g.fz0).k > 0) {
-      if (tid == 0) issue(i + 1);
-      issued_next = true;
-    }
-    const float* S = stages + st * kMarchStage;
+    const MarchBand nb = next(b);
+    issued = nb.strip >= 0 && nb.k > 0;
+    if (issued && tid == 0) issue(nb, i + 1);
+
+    const float* S = stages + (i & 1) * kMarchStage;
     const int v = kMarchVec * b.strip + lane - 1;                  // the lane's vector of F
     const int I0 = g.fx0 + 4 * v;                                  // its first column
     const bool sok = v <= g.nvec;                                  // new stresses here (halo included)
     const bool own = lane >= 1 && lane <= kMarchVec && v < g.nvec;  // a vector of F this CTA updates
-    auto vrow = [&](int f, int y) { return vring + (f * kMarchVRows + (y - b.vlo + kMarchR) % kMarchVRows) * kMarchW; };
-    auto srow = [&](int f, int y) { return sring + (f * kMarchSRows + ((y - b.vlo + 2) & (kMarchSRows - 1))) * kMarchW; };
+    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + 8) % 24,
+    // stress ring (Ls + d - vlo + 2) % 16
+    const int vbase = (kMarchR * b.k + 6 + warp) % kMarchVRows;
+    const int sbase = kMarchR * b.k + warp;
+    auto vrow = [&](int f, int d) {
+      int r = vbase + d;
+      r = r >= kMarchVRows ? r - kMarchVRows : (r < 0 ? r + kMarchVRows : r);
+      return vring + (f * kMarchVRows + r) * kMarchW;
+    };
+    auto srow = [&](int f, int d) { return sring + (f * kMarchSRows + ((sbase + d) & (kMarchSRows - 1))) * kMarchW; };
 
     // ---- new stresses of row Ls for the strip's 32 vectors
     const int Ls = b.vlo - 2 + kMarchR * b.k + warp;
     if (sok) {
       StressCoreIn<float> a;
-      a.ur[0] = lds4(vrow(0, Ls) + 4 * lm); a.ur[1] = lds4(vrow(0, Ls) + 4 * lane); a.ur[2] = lds4(vrow(0, Ls) + 4 * lp);
-      a.wr[0] = lds4(vrow(1, Ls) + 4 * lm); a.wr[1] = lds4(vrow(1, Ls) + 4 * lane); a.wr[2] = lds4(vrow(1, Ls) + 4 * lp);
-      a.xr[0] = lds4(vrow(2, Ls) + 4 * lm); a.xr[1] = lds4(vrow(2, Ls) + 4 * lane); a.xr[2] = lds4(vrow(2, Ls) + 4 * lp);
-      a.um2 = lds4(vrow(0, Ls - 2) + 4 * lane); a.um1 = lds4(vrow(0, Ls - 1) + 4 * lane);
-      a.up1 = lds4(vrow(0, Ls + 1) + 4 * lane);
-      a.wm1 = lds4(vrow(1, Ls - 1) + 4 * lane); a.wp1 = lds4(vrow(1, Ls + 1) + 4 * lane);
-      a.wp2 = lds4(vrow(1, Ls + 2) + 4 * lane);
-      a.zm1 = lds4(vrow(3, Ls - 1) + 4 * lane); a.z0 = lds4(vrow(3, Ls) + 4 * lane);
-      a.zp1 = lds4(vrow(3, Ls + 1) + 4 * lane); a.zp2 = lds4(vrow(3, Ls + 2) + 4 * lane);
+      a.ur[0] = lds4s(vrow(0, 0) + 4 * lm); a.ur[1] = lds4s(vrow(0, 0) + 4 * lane); a.ur[2] = lds4s(vrow(0, 0) + 4 * lp);
+      a.wr[0] = lds4s(vrow(1, 0) + 4 * lm); a.wr[1] = lds4s(vrow(1, 0) + 4 * lane); a.wr[2] = lds4s(vrow(1, 0) + 4 * lp);
+      a.xr[0] = lds4s(vrow(2, 0) + 4 * lm); a.xr[1] = lds4s(vrow(2, 0) + 4 * lane); a.xr[2] = lds4s(vrow(2, 0) + 4 * lp);
+      a.um2 = lds4s(vrow(0, -2) + 4 * lane); a.um1 = lds4s(vrow(0, -1) + 4 * lane);
+      a.up1 = lds4s(vrow(0, 1) + 4 * lane);
+      a.wm1 = lds4s(vrow(1, -1) + 4 * lane); a.wp1 = lds4s(vrow(1, 1) + 4 * lane);
+      a.wp2 = lds4s(vrow(1, 2) + 4 * lane);
+      a.zm1 = lds4s(vrow(3, -1) + 4 * lane); a.z0 = lds4s(vrow(3, 0) + 4 * lane);
+      a.zp1 = lds4s(vrow(3, 1) + 4 * lane); a.zp2 = lds4s(vrow(3, 2) + 4 * lane);
       const float* srow0 = S + warp * kMarchW + 4 * lane;
       // stage boxes 0..3: TXX TZZ TXZ PRES
-      V4<float> oxx = lds4(srow0), ozz = lds4(srow0 + kMarchBox), oxz = lds4(srow0 + 2 * kMarchBox),
-                opr = lds4(srow0 + 3 * kMarchBox);
+      V4<float> oxx = lds4s(srow0), ozz = lds4s(srow0 + kMarchBox), oxz = lds4s(srow0 + 2 * kMarchBox),
+                opr = lds4s(srow0 + 3 * kMarchBox);
       V4<float> bio[5];
 #pragma unroll
-      for (int s = 0; s < 5; ++s) bio[s] = lds4(srow0 + (4 + s) * kMarchBox);
+      for (int s = 0; s < 5; ++s) bio[s] = lds4s(srow0 + (4 + s) * kMarchBox);
       const long long c0 = (long long)Ls * P + (I0 - p.PMLL);
       const int src_j = (Ls == p.LIN_Z && p.LIN_X >= I0 && p.LIN_X < I0 + 4) ? p.LIN_X - I0 : -1;
       stress_core_math<float, MODE>(p, c0, a, bio, oxz, oxx, ozz, opr, src_j, srcS, srcF);
-      *reinterpret_cast<float4*>(srow(0, Ls) + 4 * lane) = make_float4(oxz.v[0], oxz.v[1], oxz.v[2], oxz.v[3]);
-      *reinterpret_cast<float4*>(srow(1, Ls) + 4 * lane) = make_float4(oxx.v[0], oxx.v[1], oxx.v[2], oxx.v[3]);
-      *reinterpret_cast<float4*>(srow(2, Ls) + 4 * lane) = make_float4(ozz.v[0], ozz.v[1], ozz.v[2], ozz.v[3]);
-      *reinterpret_cast<float4*>(srow(3, Ls) + 4 * lane) = make_float4(opr.v[0], opr.v[1], opr.v[2], opr.v[3]);
+      sts4s(srow(0, 0) + 4 * lane, oxz);
+      sts4s(srow(1, 0) + 4 * lane, oxx);
+      sts4s(srow(2, 0) + 4 * lane, ozz);
+      sts4s(srow(3, 0) + 4 * lane, opr);
       if (own && I0 >= g.sx0 && I0 < g.sx1 && Ls >= b.vlo && Ls < b.vhi && Ls >= g.sz0 && Ls < g.sz1) {
         st4(p.oTXZ + c0, oxz);
         st4(p.oTXX + c0, oxx);
@@ -247,24 +245,24 @@ __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constan
     const int Lv = Ls - 2;
     if (own && Lv >= b.vlo && Lv < b.vhi) {
       VelocityCoreIn<float> a;
-      a.xxr[0] = lds4(srow(1, Lv) + 4 * lm); a.xxr[1] = lds4(srow(1, Lv) + 4 * lane);
-      a.xxr[2] = lds4(srow(1, Lv) + 4 * lp);
-      a.prr[0] = lds4(srow(3, Lv) + 4 * lm); a.prr[1] = lds4(srow(3, Lv) + 4 * lane);
-      a.prr[2] = lds4(srow(3, Lv) + 4 * lp);
-      a.xzr[0] = lds4(srow(0, Lv) + 4 * lm); a.xzr[1] = lds4(srow(0, Lv) + 4 * lane);
-      a.xzr[2] = lds4(srow(0, Lv) + 4 * lp);
-      a.prm2 = lds4(srow(3, Lv - 2) + 4 * lane); a.prm1 = lds4(srow(3, Lv - 1) + 4 * lane);
-      a.prp1 = lds4(srow(3, Lv + 1) + 4 * lane);
-      a.xzm1 = lds4(srow(0, Lv - 1) + 4 * lane); a.xzp1 = lds4(srow(0, Lv + 1) + 4 * lane);
-      a.xzp2 = lds4(srow(0, Lv + 2) + 4 * lane);
-      a.zzm2 = lds4(srow(2, Lv - 2) + 4 * lane); a.zzm1 = lds4(srow(2, Lv - 1) + 4 * lane);
-      a.zz0 = lds4(srow(2, Lv) + 4 * lane); a.zzp1 = lds4(srow(2, Lv + 1) + 4 * lane);
-      V4<float> oum = lds4(vrow(0, Lv) + 4 * lane), owm = lds4(vrow(1, Lv) + 4 * lane),
-                oqx = lds4(vrow(2, Lv) + 4 * lane), oqz = lds4(vrow(3, Lv) + 4 * lane);
+      a.xxr[0] = lds4s(srow(1, -2) + 4 * lm); a.xxr[1] = lds4s(srow(1, -2) + 4 * lane);
+      a.xxr[2] = lds4s(srow(1, -2) + 4 * lp);
+      a.prr[0] = lds4s(srow(3, -2) + 4 * lm); a.prr[1] = lds4s(srow(3, -2) + 4 * lane);
+      a.prr[2] = lds4s(srow(3, -2) + 4 * lp);
+      a.xzr[0] = lds4s(srow(0, -2) + 4 * lm); a.xzr[1] = lds4s(srow(0, -2) + 4 * lane);
+      a.xzr[2] = lds4s(srow(0, -2) + 4 * lp);
+      a.prm2 = lds4s(srow(3, -4) + 4 * lane); a.prm1 = lds4s(srow(3, -3) + 4 * lane);
+      a.prp1 = lds4s(srow(3, -1) + 4 * lane);
+      a.xzm1 = lds4s(srow(0, -3) + 4 * lane); a.xzp1 = lds4s(srow(0, -1) + 4 * lane);
+      a.xzp2 = lds4s(srow(0, 0) + 4 * lane);
+      a.zzm2 = lds4s(srow(2, -4) + 4 * lane); a.zzm1 = lds4s(srow(2, -3) + 4 * lane);
+      a.zz0 = lds4s(srow(2, -2) + 4 * lane); a.zzp1 = lds4s(srow(2, -1) + 4 * lane);
+      V4<float> oum = lds4s(vrow(0, -2) + 4 * lane), owm = lds4s(vrow(1, -2) + 4 * lane),
+                oqx = lds4s(vrow(2, -2) + 4 * lane), oqz = lds4s(vrow(3, -2) + 4 * lane);
       V4<float> bio[5];
       const float* prow = S + 9 * kMarchBox + warp * kMarchW + 4 * lane;
 #pragma unroll
-      for (int s = 0; s < 5; ++s) bio[s] = lds4(prow + s * kMarchBox);
+      for (int s = 0; s < 5; ++s) bio[s] = lds4s(prow + s * kMarchBox);
       const long long c0 = (long long)Lv * P + (I0 - p.PMLL);
       velocity_core_math<float, MODE>(p, c0, a, bio, oqx, oum, oqz, owm);
       st4(p.oQX + c0, oqx);
@@ -273,6 +271,7 @@ __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constan
       st4(p.oWM + c0, owm);
     }
     __syncthreads();  // the stage, and the ring rows the next copies overwrite, are free
+    b = nb;
   }
   // after a wait that gave up, let that band's copies, which may still be in
   // flight, land before the CTA exits (bounded)
