@@ -424,11 +424,18 @@ bool plan_march(fdp_ctx* c) {
   // strips' rows split evenly among them
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->g.device);
+  // bands of 4 rows (two CTAs of four warps per SM, each its own pipeline)
+  // or of 8 (one CTA of eight warps)
+  const char* er = std::getenv("FDP_MARCH_ROWS");
+  c->march_rows = er && std::atoi(er) == 8 ? 8 : 4;
   const char* ec = std::getenv("FDP_MARCH_CTAS");
-  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sms, m.total);
-  if (cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)fdp::kMarchSmem) != cudaSuccess)
-    return false;
+  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sms * (8 / c->march_rows), m.total);
+  cudaError_t e = c->march_rows == 8
+                      ? cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fdp::MarchShape<8>::kSmem)
+                      : cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fdp::MarchShape<4>::kSmem);
+  if (e != cudaSuccess) return false;
   c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
   c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
   return true;
@@ -447,10 +454,10 @@ int make_march_maps(fdp_ctx* c) {
     const DevArr* f = b == c->cur ? c->fields : c->alt;
     fdp::MarchMaps& m = c->mmaps[b];
     for (int k = 0; k < 8; ++k)
-      if ((rc = make_field_map(c, &m.f[k], f[k].p, fdp::kMarchW, fdp::kMarchR)) != FDP_OK) return rc;
+      if ((rc = make_field_map(c, &m.f[k], f[k].p, fdp::kMarchW, c->march_rows)) != FDP_OK) return rc;
     for (int k = 0; k < 10; ++k)
-      if ((rc = make_field_map(c, &m.pl[k], (float*)c->planes.p + (size_t)k * pstride, fdp::kMarchW, fdp::kMarchR)) !=
-          FDP_OK)
+      if ((rc = make_field_map(c, &m.pl[k], (float*)c->planes.p + (size_t)k * pstride, fdp::kMarchW,
+                               c->march_rows)) != FDP_OK)
         return rc;
   }
   c->march_ready = true;
@@ -566,9 +573,14 @@ void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool firs
   fdp::k_velocity_frame<T, SI, MODE><<<c->nmframe_v, blk, 0, c->side>>>(pv, (const int4*)c->mframe_v.p,
                                                                           c->nmframe_v, it_off);
   if (c->core_ev[0][0]) cudaEventRecord(c->core_ev[0][0], c->stream);
-  if constexpr (std::is_same<T, float>::value && MODE == fdp::M_BIOT)
-    fdp::k_march<MODE><<<c->march_ctas, fdp::kMarchThreads, fdp::kMarchSmem, c->stream>>>(pm, c->mmaps[c->cur],
-                                                                                        c->mg, it_off);
+  if constexpr (std::is_same<T, float>::value && MODE == fdp::M_BIOT) {
+    if (c->march_rows == 8)
+      fdp::k_march<MODE, 8><<<c->march_ctas, fdp::MarchShape<8>::kThreads, fdp::MarchShape<8>::kSmem, c->stream>>>(
+          pm, c->mmaps[c->cur], c->mg, it_off);
+    else
+      fdp::k_march<MODE, 4><<<c->march_ctas, fdp::MarchShape<4>::kThreads, fdp::MarchShape<4>::kSmem, c->stream>>>(
+          pm, c->mmaps[c->cur], c->mg, it_off);
+  }
   if (c->core_ev[0][1]) cudaEventRecord(c->core_ev[0][1], c->stream);
   cudaEventRecord(c->join, c->side);
   cudaStreamWaitEvent(c->stream, c->join, 0);
@@ -1357,7 +1369,7 @@ int fdp_march_info(fdp_ctx* c, int32_t* region8, int32_t* shape4) {
   const bool on = use_march(c);
   const fdp::MarchGrid& m = c->mg;
   const int32_t r[8] = {m.fx0, m.fx1, m.fz0, m.fz1, m.sx0, m.sx1, m.sz0, m.sz1};
-  const int32_t sh[4] = {m.nstrips, fdp::kMarchR, c->march_ctas, fdp::kMarchThreads / 32};
+  const int32_t sh[4] = {m.nstrips, c->march_rows, c->march_ctas, c->march_rows};
   for (int k = 0; k < 8; ++k) region8[k] = on ? r[k] : 0;
   for (int k = 0; k < 4; ++k) shape4[k] = on ? sh[k] : 0;
   return FDP_OK;

@@ -3,19 +3,19 @@
 // A level is the stress phase (time_loop.F90:93-124) and then the velocity
 // phase (time_loop.F90:133-179).  In the interior both are the 4th-order
 // stencils of the core kernels, and a cell's new velocities need the new
-// stresses only within two cells of it.  So a CTA of eight warps owns a
-// strip of 30 four-cell vectors (120 columns) and marches down a range of
-// its rows in bands of eight rows: per band each warp computes the new
+// stresses only within two cells of it.  So a CTA of R warps (R = 4 or 8)
+// owns a strip of 30 four-cell vectors (120 columns) and marches down a
+// range of its rows in bands of R rows: per band each warp computes the new
 // stresses of one row for the strip's vectors and one halo vector either
-// side (lanes 0 and 31), keeps them in a shared-memory ring of 16 rows, and,
+// side (lanes 0 and 31), keeps them in a shared-memory ring of 2R rows, and,
 // after a barrier, the new velocities of the row two above from that ring.
 // A cell's stencils read the old wavefield (one buffer of each pair) and
 // write the new values to the other, so no CTA reads what another writes
 // during the launch.
 //
 // Inputs arrive by bulk tensor copies (cp.async.bulk.tensor.2d), one box of
-// 128 columns by 8 rows per array: the old velocities into a ring of 24
-// rows (the 12 a band's stencils reach and the next band's 8), and the old
+// 128 columns by R rows per array: the old velocities into a ring of 3R
+// rows (the R+4 a band's stencils reach and the next band's R), and the old
 // stresses and the ten coefficient planes of the band into one of two
 // stages.  One thread issues the next band's copies as a band starts, so
 // they are in flight while the band computes; every thread waits for its
@@ -39,7 +39,7 @@
 // ordering between them.  The stress update of the source cell (LIN_X,
 // LIN_Z) adds the source term of stress_lin_nn.F90:58-63.
 //
-// The CTAs split the strips' rows evenly (one CTA per SM, the rows of all
+// The CTAs split the strips' rows evenly (8/R CTAs per SM, the rows of all
 // strips taken as one sequence); a CTA whose range crosses into the next
 // strip starts again there.  FP32 with the ten planes of a Biot medium.
 #pragma once
@@ -48,21 +48,25 @@
 
 namespace fdp {
 
-constexpr int kMarchVec = 30;                  // vectors a strip updates (lanes 1..30)
-constexpr int kMarchW = 128;                   // box width: the strip's 32 vectors
-constexpr int kMarchR = 8;                     // rows per band, one per warp
-constexpr int kMarchThreads = 32 * kMarchR;
-constexpr int kMarchVRows = 3 * kMarchR;       // velocity ring rows
-constexpr int kMarchSRows = 16;                // stress ring rows
-constexpr int kMarchBox = kMarchR * kMarchW;   // floats per box
-constexpr int kMarchDirect = 14;               // boxes of a stage: stresses (4), stress planes, velocity planes (5 each)
-constexpr int kMarchVRing = 4 * kMarchVRows * kMarchW;
-constexpr int kMarchStage = kMarchDirect * kMarchBox;
-constexpr int kMarchSRing = 4 * kMarchSRows * kMarchW;
-constexpr size_t kMarchSmem = (size_t)(kMarchVRing + 2 * kMarchStage + kMarchSRing) * sizeof(float) + 128;
-static_assert(kMarchSmem <= 227 * 1024, "march stages exceed the shared memory of a CTA");
+constexpr int kMarchVec = 30;  // vectors a strip updates (lanes 1..30)
+constexpr int kMarchW = 128;   // box width: the strip's 32 vectors
+constexpr int kMarchDirect = 14;  // boxes of a stage: stresses (4), stress planes, velocity planes (5 each)
 
-// Tensor maps (boxes of 128 columns by 8 rows): the eight wavefield arrays
+// Sizes of a CTA of R warps marching bands of R rows (R = 4 or 8).
+template <int R> struct MarchShape {
+  static constexpr int kThreads = 32 * R;
+  static constexpr int kVRows = 3 * R;  // velocity ring rows
+  static constexpr int kSRows = 2 * R;  // stress ring rows
+  static constexpr int kBox = R * kMarchW;  // floats per box
+  static constexpr int kVRing = 4 * kVRows * kMarchW;
+  static constexpr int kStage = kMarchDirect * kBox;
+  static constexpr int kSRing = 4 * kSRows * kMarchW;
+  static constexpr size_t kSmem = (size_t)(kVRing + 2 * kStage + kSRing) * sizeof(float) + 128;
+  static_assert(kSmem <= 227 * 1024, "march stages exceed the shared memory of a CTA");
+  static_assert(R >= 4 && (R & (R - 1)) == 0, "a band's stencils reach four rows back");
+};
+
+// Tensor maps (boxes of 128 columns by R rows): the eight wavefield arrays
 // a level reads (UM WM QX QZ TXX TZZ TXZ PRES) and the ten Biot planes.
 struct MarchMaps {
   CUtensorMap f[8];
@@ -79,8 +83,8 @@ struct MarchGrid {
 };
 
 // A band of a CTA: strip, the velocity rows [vlo, vhi) of its segment and
-// its index k there; its stresses are rows [vlo-2+8k, vlo+6+8k) and its
-// velocities rows [vlo-4+8k, vlo+4+8k).  strip < 0: past the CTA's range.
+// its index k there; its stresses are rows [vlo-2+Rk, vlo-2+R(k+1)) and its
+// velocities the rows two above those.  strip < 0: past the CTA's range.
 struct MarchBand {
   int strip, vlo, vhi, k;
 };
@@ -99,10 +103,13 @@ __device__ __forceinline__ void sts4s(float* s, const V4<float>& v) {
                : "memory");
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constant__ Params<float> p,
-                                                             const __grid_constant__ MarchMaps maps, const MarchGrid g,
-                                                             int it_off) {
+template <int MODE, int R>
+__global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const __grid_constant__ Params<float> p,
+                                                                           const __grid_constant__ MarchMaps maps,
+                                                                           const MarchGrid g, int it_off) {
+  using Sh = MarchShape<R>;
+  constexpr int kMarchR = R, kMarchVRows = Sh::kVRows, kMarchSRows = Sh::kSRows, kMarchBox = Sh::kBox;
+  constexpr int kMarchVRing = Sh::kVRing, kMarchStage = Sh::kStage;
   extern __shared__ unsigned char march_raw[];
   float* const vring = reinterpret_cast<float*>(((uintptr_t)march_raw + 127) & ~(uintptr_t)127);
   float* const stages = vring + kMarchVRing;
@@ -139,9 +146,9 @@ __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constan
     const int x = g.fx0 + 4 * kMarchVec * b.strip - 4 - p.PMLL + kPadX;  // padded column of the box
     const int r = b.vlo - 2 + kMarchR * b.k;                                // first stress row
     mbar_expect_tx(bar, (uint32_t)((b.k == 0 ? 22 : 18) * kMarchBox * sizeof(float)));
-    // velocities: rows [r+2, r+10) into ring rows ((k+1) % 3) * 8 .. (the
-    // ring row of grid row y is (y - vlo + 8) % 24); band 0 also rows
-    // [vlo-8, vlo) into ring rows 0..7
+    // velocities: rows [r+2, r+2+R) into ring rows ((k+1) % 3) * R .. (the
+    // ring row of grid row y is (y - vlo + R) % 3R); band 0 also rows
+    // [vlo-R, vlo) into ring rows 0..R-1
     const int slot = ((b.k + 1) % 3) * kMarchR;
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -194,9 +201,9 @@ __global__ void __launch_bounds__(kMarchThreads, 1) k_march(const __grid_constan
     const int I0 = g.fx0 + 4 * v;                                  // its first column
     const bool sok = v <= g.nvec;                                  // new stresses here (halo included)
     const bool own = lane >= 1 && lane <= kMarchVec && v < g.nvec;  // a vector of F this CTA updates
-    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + 8) % 24,
-    // stress ring (Ls + d - vlo + 2) % 16
-    const int vbase = (kMarchR * b.k + 6 + warp) % kMarchVRows;
+    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + R) % 3R,
+    // stress ring (Ls + d - vlo + 2) % 2R
+    const int vbase = (kMarchR * b.k + kMarchR - 2 + warp) % kMarchVRows;
     const int sbase = kMarchR * b.k + warp;
     auto vrow = [&](int f, int d) {
       int r = vbase + d;
