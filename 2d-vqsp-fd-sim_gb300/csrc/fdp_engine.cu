@@ -442,23 +442,18 @@ bool plan_march(fdp_ctx* c) {
 }
 
 // The march kernel's tensor maps for each of the two buffers of the fields
-// (indexed like cur) over the medium's Biot planes; the march levels run
-// only with them (a medium of another kind leaves the context on the
+// (indexed like cur); the march levels run only once the medium is held as
+// Biot planes (a medium of another kind leaves the context on the
 // frame/core split).
 int make_march_maps(fdp_ctx* c) {
   c->march_ready = false;
   if (!c->march || c->medium_mode != fdp::M_BIOT || !c->planes.p) return FDP_OK;
-  const size_t pstride = (size_t)c->rows_alloc * c->pitch;
   int rc;
   for (int b = 0; b < 2; ++b) {
     const DevArr* f = b == c->cur ? c->fields : c->alt;
     fdp::MarchMaps& m = c->mmaps[b];
     for (int k = 0; k < 8; ++k)
       if ((rc = make_field_map(c, &m.f[k], f[k].p, fdp::kMarchW, c->march_rows)) != FDP_OK) return rc;
-    for (int k = 0; k < 10; ++k)
-      if ((rc = make_field_map(c, &m.pl[k], (float*)c->planes.p + (size_t)k * pstride, fdp::kMarchW,
-                               c->march_rows)) != FDP_OK)
-        return rc;
   }
   c->march_ready = true;
   return FDP_OK;

@@ -13,15 +13,17 @@
 // write the new values to the other, so no CTA reads what another writes
 // during the launch.
 //
-// Inputs arrive by bulk tensor copies (cp.async.bulk.tensor.2d), one box of
-// 128 columns by R rows per array: the old velocities into a ring of 3R
-// rows (the R+4 a band's stencils reach and the next band's R), and the old
-// stresses and the ten coefficient planes of the band into one of two
-// stages.  One thread issues the next band's copies as a band starts, so
-// they are in flight while the band computes; every thread waits for its
-// band's copies on the stage's mbarrier with a bounded try_wait, and a wait
-// that gives up sets the status word, lets the copies in flight land
-// (bounded again) and returns.
+// The old velocities and stresses arrive by bulk tensor copies
+// (cp.async.bulk.tensor.2d), one box of 128 columns by R rows per array: the
+// velocities into a ring of 4R rows (the R+4 a band's stencils reach and the
+// next two bands' R each), the stresses into one of three stages.  One
+// thread issues the copies two bands ahead, so two bands' copies are in
+// flight while a band computes; every thread waits for its band's copies on
+// the stage's mbarrier with a bounded try_wait, and a wait that gives up
+// sets the status word, lets the copies in flight land (bounded again) and
+// returns.  The ten coefficient planes, read once per cell, go straight to
+// registers: each thread loads its vector of the next band's planes while
+// the band computes.
 //
 // Per cell the pass reads the old velocities and stresses and the ten
 // coefficient planes and writes the new velocities and stresses: 26 values
@@ -50,27 +52,27 @@ namespace fdp {
 
 constexpr int kMarchVec = 30;  // vectors a strip updates (lanes 1..30)
 constexpr int kMarchW = 128;   // box width: the strip's 32 vectors
-constexpr int kMarchDirect = 14;  // boxes of a stage: stresses (4), stress planes, velocity planes (5 each)
 
 // Sizes of a CTA of R warps marching bands of R rows (R = 4 or 8).
 template <int R> struct MarchShape {
   static constexpr int kThreads = 32 * R;
-  static constexpr int kVRows = 3 * R;  // velocity ring rows
-  static constexpr int kSRows = 2 * R;  // stress ring rows
-  static constexpr int kBox = R * kMarchW;  // floats per box
+  static constexpr int kSlots = 4;           // velocity ring slots of R rows
+  static constexpr int kVRows = kSlots * R;  // velocity ring rows
+  static constexpr int kSRows = 2 * R;       // stress ring rows
+  static constexpr int kStages = 3;          // stages of old stresses
+  static constexpr int kBox = R * kMarchW;   // floats per box
   static constexpr int kVRing = 4 * kVRows * kMarchW;
-  static constexpr int kStage = kMarchDirect * kBox;
+  static constexpr int kStage = 4 * kBox;
   static constexpr int kSRing = 4 * kSRows * kMarchW;
-  static constexpr size_t kSmem = (size_t)(kVRing + 2 * kStage + kSRing) * sizeof(float) + 128;
+  static constexpr size_t kSmem = (size_t)(kVRing + kStages * kStage + kSRing) * sizeof(float) + 128;
   static_assert(kSmem <= 227 * 1024, "march stages exceed the shared memory of a CTA");
   static_assert(R >= 4 && (R & (R - 1)) == 0, "a band's stencils reach four rows back");
 };
 
-// Tensor maps (boxes of 128 columns by R rows): the eight wavefield arrays
-// a level reads (UM WM QX QZ TXX TZZ TXZ PRES) and the ten Biot planes.
+// Tensor maps (boxes of 128 columns by R rows) of the eight wavefield arrays
+// a level reads: UM WM QX QZ TXX TZZ TXZ PRES.
 struct MarchMaps {
   CUtensorMap f[8];
-  CUtensorMap pl[10];
 };
 
 // The launch's work: F, where the new stresses are written, the strips of
@@ -108,13 +110,11 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
                                                                            const __grid_constant__ MarchMaps maps,
                                                                            const MarchGrid g, int it_off) {
   using Sh = MarchShape<R>;
-  constexpr int kMarchR = R, kMarchVRows = Sh::kVRows, kMarchSRows = Sh::kSRows, kMarchBox = Sh::kBox;
-  constexpr int kMarchVRing = Sh::kVRing, kMarchStage = Sh::kStage;
   extern __shared__ unsigned char march_raw[];
   float* const vring = reinterpret_cast<float*>(((uintptr_t)march_raw + 127) & ~(uintptr_t)127);
-  float* const stages = vring + kMarchVRing;
-  float* const sring = stages + 2 * kMarchStage;
-  __shared__ __align__(8) uint64_t full[2];
+  float* const stages = vring + Sh::kVRing;
+  float* const sring = stages + Sh::kStages * Sh::kStage;
+  __shared__ __align__(8) uint64_t full[Sh::kStages];
   __shared__ int failed;
   const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // the CTA's rows [lo, hi) of the sequence of all strips' rows (H per strip)
@@ -126,43 +126,57 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
     return g.fz0 + (int)((e <= hi ? e : hi) - (long long)strip * H);
   };
   auto next = [&](const MarchBand& b) -> MarchBand {
-    if (b.k + 1 < (b.vhi - b.vlo + 4 + kMarchR - 1) / kMarchR) return {b.strip, b.vlo, b.vhi, b.k + 1};
+    if (b.strip < 0) return b;
+    if (b.k + 1 < (b.vhi - b.vlo + 4 + R - 1) / R) return {b.strip, b.vlo, b.vhi, b.k + 1};
     const int s = b.strip + 1;
     if ((long long)s * H >= hi) return {-1, 0, 0, 0};
     return {s, g.fz0, seg_end(s), 0};
   };
   if (tid == 0) {
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
+    for (int s = 0; s < Sh::kStages; ++s) mbar_init(&full[s], 1);
     failed = 0;
   }
   __syncthreads();
   if (lo >= hi) return;
 
-  // the copies of band b (the CTA's i-th) into stage i % 2 and the velocity ring
-  auto issue = [&](const MarchBand& b, int i) {
-    uint64_t* bar = &full[i & 1];
-    float* st = stages + (i & 1) * kMarchStage;
+  // the copies of band b (the CTA's j-th): its new velocity rows into the
+  // ring, its old stresses into stage j % 3
+  auto issue = [&](const MarchBand& b, int j) {
+    uint64_t* bar = &full[j % Sh::kStages];
+    float* st = stages + (j % Sh::kStages) * Sh::kStage;
     const int x = g.fx0 + 4 * kMarchVec * b.strip - 4 - p.PMLL + kPadX;  // padded column of the box
-    const int r = b.vlo - 2 + kMarchR * b.k;                                // first stress row
-    mbar_expect_tx(bar, (uint32_t)((b.k == 0 ? 22 : 18) * kMarchBox * sizeof(float)));
-    // velocities: rows [r+2, r+2+R) into ring rows ((k+1) % 3) * R .. (the
-    // ring row of grid row y is (y - vlo + R) % 3R); band 0 also rows
-    // [vlo-R, vlo) into ring rows 0..R-1
-    const int slot = ((b.k + 1) % 3) * kMarchR;
+    const int r = b.vlo - 2 + R * b.k;                                      // first stress row
+    mbar_expect_tx(bar, (uint32_t)((b.k == 0 ? 12 : 8) * Sh::kBox * sizeof(float)));
+    // velocities: rows [r+2, r+2+R) into ring slot (k+1) % 4 (the ring row of
+    // grid row y is (y - vlo + R) % 4R); band 0 also rows [vlo-R, vlo) into
+    // slot 0
+    const int slot = ((b.k + 1) % Sh::kSlots) * R;
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
-      float* fr = vring + f * kMarchVRows * kMarchW;
+      float* fr = vring + f * Sh::kVRows * kMarchW;
       tma_load_2d(fr + slot * kMarchW, &maps.f[f], x, r + 2 + kPadZ, bar);
-      if (b.k == 0) tma_load_2d(fr, &maps.f[f], x, b.vlo - kMarchR + kPadZ, bar);
+      if (b.k == 0) tma_load_2d(fr, &maps.f[f], x, b.vlo - R + kPadZ, bar);
     }
-    // stresses and stress planes of rows [r, r+8), velocity planes of rows [r-2, r+6)
+    // stresses of rows [r, r+R)
 #pragma unroll
-    for (int f = 0; f < 4; ++f) tma_load_2d(st + f * kMarchBox, &maps.f[4 + f], x, r + kPadZ, bar);
+    for (int f = 0; f < 4; ++f) tma_load_2d(st + f * Sh::kBox, &maps.f[4 + f], x, r + kPadZ, bar);
+  };
+  // the thread's vectors of band b's planes: the stress planes of its stress
+  // row Ls when the band's velocities need that row (Ls <= vhi+1), the
+  // velocity planes of its velocity row Ls-2 when that is one of the band's
+  // (rows past those are not loaded: they may lie beyond the arrays)
+  auto load_planes = [&](const MarchBand& b, V4<float>* sp, V4<float>* vp) {
+    if (b.strip < 0) return;
+    const int v = kMarchVec * b.strip + lane - 1;
+    const int Ls = b.vlo - 2 + R * b.k + warp;
+    if (v > g.nvec || Ls > b.vhi + 1) return;
+    const long long c0 = (long long)Ls * p.pitch + (g.fx0 + 4 * v - p.PMLL);
 #pragma unroll
-    for (int s = 0; s < 5; ++s) tma_load_2d(st + (4 + s) * kMarchBox, &maps.pl[s], x, r + kPadZ, bar);
+    for (int s = 0; s < 5; ++s) sp[s] = ld4(p.bplane[s] + c0);
+    if (lane >= 1 && lane <= kMarchVec && v < g.nvec && Ls - 2 >= b.vlo && Ls - 2 < b.vhi) {
 #pragma unroll
-    for (int s = 0; s < 5; ++s) tma_load_2d(st + (9 + s) * kMarchBox, &maps.pl[5 + s], x, r - 2 + kPadZ, bar);
+      for (int s = 0; s < 5; ++s) vp[s] = ld4(p.bplane[5 + s] + c0 - 2 * p.pitch);
+    }
   };
 
   const long long P = p.pitch;
@@ -179,41 +193,57 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
 
   const int strip0 = (int)(lo / H);
   MarchBand b = {strip0, g.fz0 + (int)(lo - (long long)strip0 * H), seg_end(strip0), 0};
-  if (tid == 0) issue(b, 0);
-  bool issued = true;  // the copies of band i are issued
+  // bands issued so far: the CTA's bands 0 .. last, whose last one is `lb`
+  int last = -1;
+  MarchBand lb = b;
+  V4<float> sp[5], vp[5];
+  load_planes(b, sp, vp);
   int i = 0;
   for (; b.strip >= 0; ++i) {
-    if (tid == 0 && !issued) issue(b, i);  // a new segment: its first band was not prefetched
-    if (!mbar_wait_bounded(&full[i & 1], (uint32_t)((i >> 1) & 1))) failed = 1;
+    // issue up to two bands ahead within the band's segment (a new segment's
+    // bands would overwrite ring rows the current ones read); a segment's
+    // first band is issued as it starts
+    if (tid == 0) {
+      if (last < i) {
+        issue(b, i);
+        last = i;
+        lb = b;
+      }
+      while (last < i + 2) {
+        const MarchBand nb = next(lb);
+        if (nb.strip != b.strip || nb.vlo != b.vlo || nb.strip < 0) break;
+        issue(nb, last + 1);
+        ++last;
+        lb = nb;
+      }
+    }
+    const MarchBand nb = next(b);
+    V4<float> nsp[5], nvp[5];
+    load_planes(nb, nsp, nvp);  // in flight while this band computes
+    if (!mbar_wait_bounded(&full[i % Sh::kStages], (uint32_t)((i / Sh::kStages) & 1))) failed = 1;
     __syncthreads();
     if (failed) {
       if (tid == 0) atomicOr(p.err, 1);
       break;
     }
-    // prefetch the next band of the same segment (the next segment's first
-    // band would overwrite ring rows this band reads)
-    const MarchBand nb = next(b);
-    issued = nb.strip >= 0 && nb.k > 0;
-    if (issued && tid == 0) issue(nb, i + 1);
-
-    const float* S = stages + (i & 1) * kMarchStage;
+    const float* S = stages + (i % Sh::kStages) * Sh::kStage;
     const int v = kMarchVec * b.strip + lane - 1;                  // the lane's vector of F
     const int I0 = g.fx0 + 4 * v;                                  // its first column
     const bool sok = v <= g.nvec;                                  // new stresses here (halo included)
     const bool own = lane >= 1 && lane <= kMarchVec && v < g.nvec;  // a vector of F this CTA updates
-    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + R) % 3R,
+    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + R) % 4R,
     // stress ring (Ls + d - vlo + 2) % 2R
-    const int vbase = (kMarchR * b.k + kMarchR - 2 + warp) % kMarchVRows;
-    const int sbase = kMarchR * b.k + warp;
+    const int vbase = (R * b.k + R - 2 + warp) % Sh::kVRows;
+    const int sbase = R * b.k + warp;
     auto vrow = [&](int f, int d) {
       int r = vbase + d;
-      r = r >= kMarchVRows ? r - kMarchVRows : (r < 0 ? r + kMarchVRows : r);
-      return vring + (f * kMarchVRows + r) * kMarchW;
+      r = r >= Sh::kVRows ? r - Sh::kVRows : (r < 0 ? r + Sh::kVRows : r);
+      return vring + (f * Sh::kVRows + r) * kMarchW;
     };
-    auto srow = [&](int f, int d) { return sring + (f * kMarchSRows + ((sbase + d) & (kMarchSRows - 1))) * kMarchW; };
+    auto srow = [&](int f, int d) { return sring + (f * Sh::kSRows + ((sbase + d) & (Sh::kSRows - 1))) * kMarchW; };
 
     // ---- new stresses of row Ls for the strip's 32 vectors
-    const int Ls = b.vlo - 2 + kMarchR * b.k + warp;
+    const int Ls = b.vlo - 2 + R * b.k + warp;
     if (sok) {
       StressCoreIn<float> a;
       a.ur[0] = lds4s(vrow(0, 0) + 4 * lm); a.ur[1] = lds4s(vrow(0, 0) + 4 * lane); a.ur[2] = lds4s(vrow(0, 0) + 4 * lp);
@@ -227,14 +257,11 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
       a.zp1 = lds4s(vrow(3, 1) + 4 * lane); a.zp2 = lds4s(vrow(3, 2) + 4 * lane);
       const float* srow0 = S + warp * kMarchW + 4 * lane;
       // stage boxes 0..3: TXX TZZ TXZ PRES
-      V4<float> oxx = lds4s(srow0), ozz = lds4s(srow0 + kMarchBox), oxz = lds4s(srow0 + 2 * kMarchBox),
-                opr = lds4s(srow0 + 3 * kMarchBox);
-      V4<float> bio[5];
-#pragma unroll
-      for (int s = 0; s < 5; ++s) bio[s] = lds4s(srow0 + (4 + s) * kMarchBox);
+      V4<float> oxx = lds4s(srow0), ozz = lds4s(srow0 + Sh::kBox), oxz = lds4s(srow0 + 2 * Sh::kBox),
+                opr = lds4s(srow0 + 3 * Sh::kBox);
       const long long c0 = (long long)Ls * P + (I0 - p.PMLL);
       const int src_j = (Ls == p.LIN_Z && p.LIN_X >= I0 && p.LIN_X < I0 + 4) ? p.LIN_X - I0 : -1;
-      stress_core_math<float, MODE>(p, c0, a, bio, oxz, oxx, ozz, opr, src_j, srcS, srcF);
+      stress_core_math<float, MODE>(p, c0, a, sp, oxz, oxx, ozz, opr, src_j, srcS, srcF);
       sts4s(srow(0, 0) + 4 * lane, oxz);
       sts4s(srow(1, 0) + 4 * lane, oxx);
       sts4s(srow(2, 0) + 4 * lane, ozz);
@@ -266,23 +293,22 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
       a.zz0 = lds4s(srow(2, -2) + 4 * lane); a.zzp1 = lds4s(srow(2, -1) + 4 * lane);
       V4<float> oum = lds4s(vrow(0, -2) + 4 * lane), owm = lds4s(vrow(1, -2) + 4 * lane),
                 oqx = lds4s(vrow(2, -2) + 4 * lane), oqz = lds4s(vrow(3, -2) + 4 * lane);
-      V4<float> bio[5];
-      const float* prow = S + 9 * kMarchBox + warp * kMarchW + 4 * lane;
-#pragma unroll
-      for (int s = 0; s < 5; ++s) bio[s] = lds4s(prow + s * kMarchBox);
       const long long c0 = (long long)Lv * P + (I0 - p.PMLL);
-      velocity_core_math<float, MODE>(p, c0, a, bio, oqx, oum, oqz, owm);
+      velocity_core_math<float, MODE>(p, c0, a, vp, oqx, oum, oqz, owm);
       st4(p.oQX + c0, oqx);
       st4(p.oUM + c0, oum);
       st4(p.oQZ + c0, oqz);
       st4(p.oWM + c0, owm);
     }
-    __syncthreads();  // the stage, and the ring rows the next copies overwrite, are free
+    __syncthreads();  // the stage, and the ring rows later copies overwrite, are free
+#pragma unroll
+    for (int s = 0; s < 5; ++s) { sp[s] = nsp[s]; vp[s] = nvp[s]; }
     b = nb;
   }
-  // after a wait that gave up, let that band's copies, which may still be in
-  // flight, land before the CTA exits (bounded)
-  if (failed && tid == 0) mbar_wait_bounded(&full[i & 1], (uint32_t)((i >> 1) & 1));
+  // after a wait that gave up, let the copies still in flight (bands i..last)
+  // land before the CTA exits (bounded)
+  if (failed && tid == 0)
+    for (int j = i; j <= last; ++j) mbar_wait_bounded(&full[j % Sh::kStages], (uint32_t)((j / Sh::kStages) & 1));
 }
 
 }  // namespace fdp
