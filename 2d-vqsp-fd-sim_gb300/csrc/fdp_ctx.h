@@ -90,7 +90,7 @@ struct fdp_ctx {
   DevArr alt[8];
   int cur = 0;
   fdp::MarchGrid mg{};
-  int march_ctas = 0, march_rows = 4;
+  int march_ctas = 0, march_rows = 8;
   // the frame kernels' rectangles beside the march kernel (stress: F less
   // its band; velocity: F) and their unit lists
   int ms[4] = {0, 0, 0, 0}, mv[4] = {0, 0, 0, 0};

@@ -424,20 +424,44 @@ bool plan_march(fdp_ctx* c) {
   // strips' rows split evenly among them
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->g.device);
-  // bands of 4 rows (two CTAs of four warps per SM, each its own pipeline)
-  // or of 8 (one CTA of eight warps)
+  // bands of 8 rows (eight warps, the copies of one band ahead in flight)
+  // or of 6 (six warps, two bands ahead); measured on the layered 2048^2
+  // workload: 0.0900 and 0.0992 ms per level
   const char* er = std::getenv("FDP_MARCH_ROWS");
-  c->march_rows = er && std::atoi(er) == 8 ? 8 : 4;
+  c->march_rows = er && std::atoi(er) == 6 ? 6 : 8;
   const char* ec = std::getenv("FDP_MARCH_CTAS");
-  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sms * (8 / c->march_rows), m.total);
+  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sms, m.total);
   cudaError_t e = c->march_rows == 8
                       ? cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)fdp::MarchShape<8>::kSmem)
-                      : cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)fdp::MarchShape<4>::kSmem);
+                      : cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fdp::MarchShape<6>::kSmem);
   if (e != cudaSuccess) return false;
   c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
   c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
+  return true;
+}
+
+// The second buffer of each wavefield array, made as a copy of the first
+// when the context first gets a medium its march levels run with: cells no
+// level updates are then read from either.  false (nothing held, no error
+// recorded) when the device has no room; the context keeps the split.
+bool alloc_alt(fdp_ctx* c) {
+  if (c->alt[0].p) return true;
+  for (int k = 0; k < 8; ++k) {
+    const size_t bytes = c->fields[k].bytes;
+    cudaError_t e = cudaMalloc(&c->alt[k].p, bytes);
+    if (e == cudaSuccess) {
+      c->alt[k].bytes = bytes;
+      e = cudaMemcpyAsync(c->alt[k].p, c->fields[k].p, bytes, cudaMemcpyDeviceToDevice, c->stream);
+    }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      for (auto& a : c->alt)
+        if (a.p) { cudaFree(a.p); a.p = nullptr; a.bytes = 0; }
+      return false;
+    }
+  }
   return true;
 }
 
@@ -448,12 +472,18 @@ bool plan_march(fdp_ctx* c) {
 int make_march_maps(fdp_ctx* c) {
   c->march_ready = false;
   if (!c->march || c->medium_mode != fdp::M_BIOT || !c->planes.p) return FDP_OK;
+  if (!alloc_alt(c)) return FDP_OK;
+  const size_t pstride = (size_t)c->rows_alloc * c->pitch;
   int rc;
   for (int b = 0; b < 2; ++b) {
     const DevArr* f = b == c->cur ? c->fields : c->alt;
     fdp::MarchMaps& m = c->mmaps[b];
     for (int k = 0; k < 8; ++k)
       if ((rc = make_field_map(c, &m.f[k], f[k].p, fdp::kMarchW, c->march_rows)) != FDP_OK) return rc;
+    for (int k = 0; k < 10; ++k)
+      if ((rc = make_field_map(c, &m.pl[k], (float*)c->planes.p + (size_t)k * pstride, fdp::kMarchW,
+                               c->march_rows)) != FDP_OK)
+        return rc;
   }
   c->march_ready = true;
   return FDP_OK;
@@ -573,7 +603,7 @@ void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool firs
       fdp::k_march<MODE, 8><<<c->march_ctas, fdp::MarchShape<8>::kThreads, fdp::MarchShape<8>::kSmem, c->stream>>>(
           pm, c->mmaps[c->cur], c->mg, it_off);
     else
-      fdp::k_march<MODE, 4><<<c->march_ctas, fdp::MarchShape<4>::kThreads, fdp::MarchShape<4>::kSmem, c->stream>>>(
+      fdp::k_march<MODE, 6><<<c->march_ctas, fdp::MarchShape<6>::kThreads, fdp::MarchShape<6>::kSmem, c->stream>>>(
           pm, c->mmaps[c->cur], c->mg, it_off);
   }
   if (c->core_ev[0][1]) cudaEventRecord(c->core_ev[0][1], c->stream);
@@ -1002,7 +1032,9 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   c->fused[0] = c->use_core && fused;
   c->fused[1] = c->use_core && fused;
   c->core_tma_req = c->use_core && variant && std::strcmp(variant, "coretma") == 0;
-  c->march = c->use_core && variant && std::strcmp(variant, "march") == 0;
+  // march levels unless a variant is named ("split" or "core": the
+  // frame/core split alone); plan_core and the medium decide whether they run
+  c->march = c->use_core && (!variant || !*variant || std::strcmp(variant, "march") == 0);
   if (c->use_core) {
     if ((rc = plan_core(c)) != FDP_OK) return bail(rc);
     e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
@@ -1011,9 +1043,6 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
 
     if (e != cudaSuccess) { c->err = std::string("side stream: ") + cudaGetErrorString(e); return bail(FDP_ERR_CUDA); }
   }
-  if (c->march)  // the second buffer of each wavefield array, zeroed like the first
-    for (int k = 0; k < 8; ++k)
-      if ((rc = dev_alloc(c, c->alt[k], fbytes)) != FDP_OK) return bail(rc);
   if (c->use_tma) {
     for (int k = 0; k < 4; ++k) {
       if ((rc = make_field_map(c, &c->tma_vel.m[k], c->fields[k].p)) != FDP_OK) return bail(rc);

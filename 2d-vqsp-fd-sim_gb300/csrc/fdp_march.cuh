@@ -3,27 +3,25 @@
 // A level is the stress phase (time_loop.F90:93-124) and then the velocity
 // phase (time_loop.F90:133-179).  In the interior both are the 4th-order
 // stencils of the core kernels, and a cell's new velocities need the new
-// stresses only within two cells of it.  So a CTA of R warps (R = 4 or 8)
+// stresses only within two cells of it.  So a CTA of R warps (R = 6 or 8)
 // owns a strip of 30 four-cell vectors (120 columns) and marches down a
 // range of its rows in bands of R rows: per band each warp computes the new
 // stresses of one row for the strip's vectors and one halo vector either
-// side (lanes 0 and 31), keeps them in a shared-memory ring of 2R rows, and,
+// side (lanes 0 and 31), keeps them in a shared-memory ring of 16 rows, and,
 // after a barrier, the new velocities of the row two above from that ring.
 // A cell's stencils read the old wavefield (one buffer of each pair) and
 // write the new values to the other, so no CTA reads what another writes
 // during the launch.
 //
-// The old velocities and stresses arrive by bulk tensor copies
-// (cp.async.bulk.tensor.2d), one box of 128 columns by R rows per array: the
-// velocities into a ring of 4R rows (the R+4 a band's stencils reach and the
-// next two bands' R each), the stresses into one of three stages.  One
-// thread issues the copies two bands ahead, so two bands' copies are in
-// flight while a band computes; every thread waits for its band's copies on
-// the stage's mbarrier with a bounded try_wait, and a wait that gives up
-// sets the status word, lets the copies in flight land (bounded again) and
-// returns.  The ten coefficient planes, read once per cell, go straight to
-// registers: each thread loads its vector of the next band's planes while
-// the band computes.
+// Inputs arrive by bulk tensor copies (cp.async.bulk.tensor.2d), one box of
+// 128 columns by R rows per array: the old velocities into a ring of rows
+// (the R+4 a band's stencils reach and the bands ahead), the old stresses
+// and the ten coefficient planes into stages, one per band in flight.  One
+// thread issues the copies A bands ahead (two with bands of six rows), so
+// they are in flight while a band computes; every thread waits for its
+// band's copies on the stage's mbarrier with a bounded try_wait, and a wait
+// that gives up sets the status word, lets the copies in flight land
+// (bounded again) and returns.
 //
 // Per cell the pass reads the old velocities and stresses and the ten
 // coefficient planes and writes the new velocities and stresses: 26 values
@@ -41,7 +39,7 @@
 // ordering between them.  The stress update of the source cell (LIN_X,
 // LIN_Z) adds the source term of stress_lin_nn.F90:58-63.
 //
-// The CTAs split the strips' rows evenly (8/R CTAs per SM, the rows of all
+// The CTAs split the strips' rows evenly (one CTA per SM, the rows of all
 // strips taken as one sequence); a CTA whose range crosses into the next
 // strip starts again there.  FP32 with the ten planes of a Biot medium.
 #pragma once
@@ -53,26 +51,32 @@ namespace fdp {
 constexpr int kMarchVec = 30;  // vectors a strip updates (lanes 1..30)
 constexpr int kMarchW = 128;   // box width: the strip's 32 vectors
 
-// Sizes of a CTA of R warps marching bands of R rows (R = 4 or 8).
+constexpr int kMarchDirect = 14;  // boxes of a stage: stresses (4), stress planes, velocity planes (5 each)
+
+// Sizes of a CTA of R warps marching bands of R rows, with the copies of A
+// bands ahead in flight (R = 6: two ahead; R = 8: one ahead, as much as
+// the shared memory of a CTA holds).
 template <int R> struct MarchShape {
+  static constexpr int kAhead = R <= 6 ? 2 : 1;
   static constexpr int kThreads = 32 * R;
-  static constexpr int kSlots = 4;           // velocity ring slots of R rows
+  static constexpr int kSlots = kAhead + 2;  // velocity ring slots of R rows
   static constexpr int kVRows = kSlots * R;  // velocity ring rows
-  static constexpr int kSRows = 2 * R;       // stress ring rows
-  static constexpr int kStages = 3;          // stages of old stresses
+  static constexpr int kSRows = 16;          // stress ring rows (R + 4 needed)
+  static constexpr int kStages = kAhead + 1;
   static constexpr int kBox = R * kMarchW;   // floats per box
   static constexpr int kVRing = 4 * kVRows * kMarchW;
-  static constexpr int kStage = 4 * kBox;
+  static constexpr int kStage = kMarchDirect * kBox;
   static constexpr int kSRing = 4 * kSRows * kMarchW;
   static constexpr size_t kSmem = (size_t)(kVRing + kStages * kStage + kSRing) * sizeof(float) + 128;
   static_assert(kSmem <= 227 * 1024, "march stages exceed the shared memory of a CTA");
-  static_assert(R >= 4 && (R & (R - 1)) == 0, "a band's stencils reach four rows back");
+  static_assert(R >= 4 && R + 4 <= kSRows, "a band's stencils reach four rows back");
 };
 
-// Tensor maps (boxes of 128 columns by R rows) of the eight wavefield arrays
-// a level reads: UM WM QX QZ TXX TZZ TXZ PRES.
+// Tensor maps (boxes of 128 columns by R rows): the eight wavefield arrays
+// a level reads (UM WM QX QZ TXX TZZ TXZ PRES) and the ten Biot planes.
 struct MarchMaps {
   CUtensorMap f[8];
+  CUtensorMap pl[10];
 };
 
 // The launch's work: F, where the new stresses are written, the strips of
@@ -106,7 +110,7 @@ __device__ __forceinline__ void sts4s(float* s, const V4<float>& v) {
 }
 
 template <int MODE, int R>
-__global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const __grid_constant__ Params<float> p,
+__global__ void __launch_bounds__(MarchShape<R>::kThreads, 1) k_march(const __grid_constant__ Params<float> p,
                                                                            const __grid_constant__ MarchMaps maps,
                                                                            const MarchGrid g, int it_off) {
   using Sh = MarchShape<R>;
@@ -140,16 +144,16 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
   if (lo >= hi) return;
 
   // the copies of band b (the CTA's j-th): its new velocity rows into the
-  // ring, its old stresses into stage j % 3
+  // ring, its old stresses and planes into stage j % kStages
   auto issue = [&](const MarchBand& b, int j) {
     uint64_t* bar = &full[j % Sh::kStages];
     float* st = stages + (j % Sh::kStages) * Sh::kStage;
     const int x = g.fx0 + 4 * kMarchVec * b.strip - 4 - p.PMLL + kPadX;  // padded column of the box
     const int r = b.vlo - 2 + R * b.k;                                      // first stress row
-    mbar_expect_tx(bar, (uint32_t)((b.k == 0 ? 12 : 8) * Sh::kBox * sizeof(float)));
-    // velocities: rows [r+2, r+2+R) into ring slot (k+1) % 4 (the ring row of
-    // grid row y is (y - vlo + R) % 4R); band 0 also rows [vlo-R, vlo) into
-    // slot 0
+    mbar_expect_tx(bar, (uint32_t)((b.k == 0 ? 22 : 18) * Sh::kBox * sizeof(float)));
+    // velocities: rows [r+2, r+2+R) into ring slot (k+1) % kSlots (the ring
+    // row of grid row y is (y - vlo + R) % kVRows); band 0 also rows
+    // [vlo-R, vlo) into slot 0
     const int slot = ((b.k + 1) % Sh::kSlots) * R;
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -157,28 +161,14 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
       tma_load_2d(fr + slot * kMarchW, &maps.f[f], x, r + 2 + kPadZ, bar);
       if (b.k == 0) tma_load_2d(fr, &maps.f[f], x, b.vlo - R + kPadZ, bar);
     }
-    // stresses of rows [r, r+R)
+    // stresses and stress planes of rows [r, r+R), velocity planes of rows [r-2, r+R-2)
 #pragma unroll
     for (int f = 0; f < 4; ++f) tma_load_2d(st + f * Sh::kBox, &maps.f[4 + f], x, r + kPadZ, bar);
-  };
-  // the thread's vectors of band b's planes: the stress planes of its stress
-  // row Ls when the band's velocities need that row (Ls <= vhi+1), the
-  // velocity planes of its velocity row Ls-2 when that is one of the band's
-  // (rows past those are not loaded: they may lie beyond the arrays)
-  auto load_planes = [&](const MarchBand& b, V4<float>* sp, V4<float>* vp) {
-    if (b.strip < 0) return;
-    const int v = kMarchVec * b.strip + lane - 1;
-    const int Ls = b.vlo - 2 + R * b.k + warp;
-    if (v > g.nvec || Ls > b.vhi + 1) return;
-    const long long c0 = (long long)Ls * p.pitch + (g.fx0 + 4 * v - p.PMLL);
 #pragma unroll
-    for (int s = 0; s < 5; ++s) sp[s] = ld4(p.bplane[s] + c0);
-    if (lane >= 1 && lane <= kMarchVec && v < g.nvec && Ls - 2 >= b.vlo && Ls - 2 < b.vhi) {
+    for (int s = 0; s < 5; ++s) tma_load_2d(st + (4 + s) * Sh::kBox, &maps.pl[s], x, r + kPadZ, bar);
 #pragma unroll
-      for (int s = 0; s < 5; ++s) vp[s] = ld4(p.bplane[5 + s] + c0 - 2 * p.pitch);
-    }
+    for (int s = 0; s < 5; ++s) tma_load_2d(st + (9 + s) * Sh::kBox, &maps.pl[5 + s], x, r - 2 + kPadZ, bar);
   };
-
   const long long P = p.pitch;
   const int it = *p.it_base + it_off;
   float srcS, srcF;
@@ -196,8 +186,6 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
   // bands issued so far: the CTA's bands 0 .. last, whose last one is `lb`
   int last = -1;
   MarchBand lb = b;
-  V4<float> sp[5], vp[5];
-  load_planes(b, sp, vp);
   int i = 0;
   for (; b.strip >= 0; ++i) {
     // issue up to two bands ahead within the band's segment (a new segment's
@@ -209,7 +197,7 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
         last = i;
         lb = b;
       }
-      while (last < i + 2) {
+      while (last < i + Sh::kAhead) {
         const MarchBand nb = next(lb);
         if (nb.strip != b.strip || nb.vlo != b.vlo || nb.strip < 0) break;
         issue(nb, last + 1);
@@ -218,8 +206,6 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
       }
     }
     const MarchBand nb = next(b);
-    V4<float> nsp[5], nvp[5];
-    load_planes(nb, nsp, nvp);  // in flight while this band computes
     if (!mbar_wait_bounded(&full[i % Sh::kStages], (uint32_t)((i / Sh::kStages) & 1))) failed = 1;
     __syncthreads();
     if (failed) {
@@ -231,8 +217,8 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
     const int I0 = g.fx0 + 4 * v;                                  // its first column
     const bool sok = v <= g.nvec;                                  // new stresses here (halo included)
     const bool own = lane >= 1 && lane <= kMarchVec && v < g.nvec;  // a vector of F this CTA updates
-    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + R) % 4R,
-    // stress ring (Ls + d - vlo + 2) % 2R
+    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + R) % kVRows,
+    // stress ring (Ls + d - vlo + 2) % kSRows
     const int vbase = (R * b.k + R - 2 + warp) % Sh::kVRows;
     const int sbase = R * b.k + warp;
     auto vrow = [&](int f, int d) {
@@ -259,9 +245,12 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
       // stage boxes 0..3: TXX TZZ TXZ PRES
       V4<float> oxx = lds4s(srow0), ozz = lds4s(srow0 + Sh::kBox), oxz = lds4s(srow0 + 2 * Sh::kBox),
                 opr = lds4s(srow0 + 3 * Sh::kBox);
+      V4<float> bio[5];
+#pragma unroll
+      for (int s = 0; s < 5; ++s) bio[s] = lds4s(srow0 + (4 + s) * Sh::kBox);
       const long long c0 = (long long)Ls * P + (I0 - p.PMLL);
       const int src_j = (Ls == p.LIN_Z && p.LIN_X >= I0 && p.LIN_X < I0 + 4) ? p.LIN_X - I0 : -1;
-      stress_core_math<float, MODE>(p, c0, a, sp, oxz, oxx, ozz, opr, src_j, srcS, srcF);
+      stress_core_math<float, MODE>(p, c0, a, bio, oxz, oxx, ozz, opr, src_j, srcS, srcF);
       sts4s(srow(0, 0) + 4 * lane, oxz);
       sts4s(srow(1, 0) + 4 * lane, oxx);
       sts4s(srow(2, 0) + 4 * lane, ozz);
@@ -293,16 +282,18 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 8 / R) k_march(const 
       a.zz0 = lds4s(srow(2, -2) + 4 * lane); a.zzp1 = lds4s(srow(2, -1) + 4 * lane);
       V4<float> oum = lds4s(vrow(0, -2) + 4 * lane), owm = lds4s(vrow(1, -2) + 4 * lane),
                 oqx = lds4s(vrow(2, -2) + 4 * lane), oqz = lds4s(vrow(3, -2) + 4 * lane);
+      V4<float> bio[5];
+      const float* prow = S + 9 * Sh::kBox + warp * kMarchW + 4 * lane;
+#pragma unroll
+      for (int s = 0; s < 5; ++s) bio[s] = lds4s(prow + s * Sh::kBox);
       const long long c0 = (long long)Lv * P + (I0 - p.PMLL);
-      velocity_core_math<float, MODE>(p, c0, a, vp, oqx, oum, oqz, owm);
+      velocity_core_math<float, MODE>(p, c0, a, bio, oqx, oum, oqz, owm);
       st4(p.oQX + c0, oqx);
       st4(p.oUM + c0, oum);
       st4(p.oQZ + c0, oqz);
       st4(p.oWM + c0, owm);
     }
     __syncthreads();  // the stage, and the ring rows later copies overwrite, are free
-#pragma unroll
-    for (int s = 0; s < 5; ++s) { sp[s] = nsp[s]; vp[s] = nvp[s]; }
     b = nb;
   }
   // after a wait that gave up, let the copies still in flight (bands i..last)

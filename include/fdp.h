@@ -101,14 +101,16 @@ enum fdp_field_id {
  * PPML and ALLOC_NR do (tl_alloc.F90:44-56, ppml.F90:115-153,
  * alloc_nr.F90:42-54).  Replaces the allocations of TL_ALLOC/PPML/ALLOC_NR.
  * The environment variable FDP_KERNEL_VARIANT, read here, selects the
- * kernels, all bit-identical: unset, the interior ("core") of each phase
- * runs vectorised beside a frame kernel for the PML, free-surface, source
- * and bottom cells on a second stream; "fused" runs frame and core of a
- * phase in one launch; "global" runs one unit kernel per phase over the
- * whole grid; "tma" the TMA-staged variant of the latter; "coretma" the
- * default split with TMA-staged persistent core kernels (FP32 contexts with
- * a Biot-plane medium; others keep the per-thread-load core); "march" both
- * phases of the deep interior in one pass (fdp_march_info). */
+ * kernels, all bit-identical.  Unset (or "march"): FP32 contexts whose
+ * medium is held as Biot planes run both phases of each level's deep
+ * interior in one pass (fdp_march_info), every other context the split.
+ * "split": the interior ("core") of each phase runs vectorised beside a
+ * frame kernel for the PML, free-surface, source and bottom cells on a
+ * second stream; "fused" runs frame and core of a phase in one launch;
+ * "global" runs one unit kernel per phase over the whole grid; "tma" the
+ * TMA-staged variant of the latter; "coretma" the split with TMA-staged
+ * persistent core kernels (FP32 contexts with a Biot-plane medium; others
+ * keep the per-thread-load core). */
 int fdp_create(const fdp_grid* grid, fdp_ctx** out);
 
 /* Medium: JM(PMLL:PMLXH, 0:PMLZH) (nx = MX+2*TPML, nz = PMLZH+1) after
@@ -244,7 +246,7 @@ int fdp_medium_info(fdp_ctx* ctx, int32_t* mode, int32_t* planes_stress, int32_t
  * the velocity core; zeros when the context runs other kernels. */
 int fdp_core_info(fdp_ctx* ctx, int32_t* rect8);
 
-/* The march variant (FDP_KERNEL_VARIANT=march): each level's deep
+/* The march levels (the default for FP32 Biot media): each level's deep
  * interior in one kernel pass (stress phase, then velocity phase, from
  * bands of rows staged in shared memory by bulk tensor copies), the levels
  * alternating between two buffers of each wavefield array, with the frame

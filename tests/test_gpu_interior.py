@@ -18,7 +18,7 @@ from helpers import compare_state, randomize_state, small_job
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(autouse=True, params=["core", "fused", "global", "tma", "coretma", "march"])
+@pytest.fixture(autouse=True, params=["split", "fused", "global", "tma", "coretma", "march"])
 def kernel_variant(request, monkeypatch):
     monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
     return request.param

@@ -1,7 +1,7 @@
 """The march variant against the oracle.
 
-With FDP_KERNEL_VARIANT=march, an FP32 context whose medium is held as the
-ten Biot planes runs each level's deep interior as one kernel pass (the
+By default (or with FDP_KERNEL_VARIANT=march), an FP32 context whose
+medium is held as the ten Biot planes runs each level's deep interior as one kernel pass (the
 stress phase, then the velocity phase, from bands of rows staged in shared
 memory by bulk tensor copies), beside the frame kernels on the side stream,
 and the levels alternate between two buffers of each wavefield array.
@@ -76,6 +76,23 @@ def test_any_split_of_the_rows_among_ctas(ctas, monkeypatch):
     compare_state(eng, orc)
 
 
+@pytest.mark.parametrize("rows", [6, 8])
+@pytest.mark.parametrize("ctas", [3, 152])
+def test_band_rows(rows, ctas, monkeypatch):
+    """Bands of six rows (copies two bands ahead) and of eight (one ahead)."""
+    monkeypatch.setenv("FDP_MARCH_ROWS", str(rows))
+    monkeypatch.setenv("FDP_MARCH_CTAS", str(ctas))
+    cfg, med = small_job(mx=251, mz=97, tpml=6, nsteps=21, si=True, per_cell=True, seed=60 + rows)
+    inp, eng, orc = _pair(cfg, med)
+    info = eng.march_info()
+    assert info["band_rows"] == rows and info["warps"] == rows
+    randomize_state([eng, orc], inp, seed=61)
+    eng.time_loop(1, 21)
+    orc.time_loop(1, 21)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 21), orc.receivers(1, 21))
+
+
 def test_launch_count():
     """Per level the stress and the velocity frame kernel and the march
     kernel; per captured run (32, 32 and 6 levels) one k_edge and one
@@ -87,6 +104,24 @@ def test_launch_count():
     eng.time_loop(1, 70)
     eng.synchronize()
     assert eng.kernel_launches() - n0 == 70 * 3 + 3 * 2 + 1
+
+
+@pytest.mark.parametrize("variant,march", [(None, True), ("", True), ("split", False), ("core", False)])
+def test_default_runs_march_levels(variant, march, monkeypatch):
+    """Without FDP_KERNEL_VARIANT an FP32 Biot context runs march levels;
+    a named split keeps it on the frame/core split.  Both equal the oracle
+    bit for bit."""
+    if variant is None:
+        monkeypatch.delenv("FDP_KERNEL_VARIANT", raising=False)
+    else:
+        monkeypatch.setenv("FDP_KERNEL_VARIANT", variant)
+    cfg, med = small_job(mx=120, mz=64, tpml=6, nsteps=9, per_cell=True, seed=41)
+    inp, eng, orc = _pair(cfg, med)
+    assert (eng.march_info() is not None) == march
+    randomize_state([eng, orc], inp, seed=42)
+    eng.time_loop(1, 9)
+    orc.time_loop(1, 9)
+    compare_state(eng, orc)
 
 
 def test_fp64_and_table_media_keep_the_split():

@@ -14,15 +14,15 @@ from helpers import compare_state, randomize_state, small_job
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(autouse=True, params=["core", "fused", "global", "tma", "coretma", "march"])
+@pytest.fixture(autouse=True, params=["split", "fused", "global", "tma", "coretma", "march"])
 def kernel_variant(request, monkeypatch):
     """Runs every test with each kernel variant fdp_create can select through
-    FDP_KERNEL_VARIANT: the frame/core split on two streams (the default)
-    or in one launch per phase, the unit kernels over the whole grid, the
-    TMA-staged kernels, the split with TMA-staged persistent core kernels
-    (FP32 Biot media; the others keep the per-thread-load core), and the
-    march kernel doing both phases of the deep interior in one pass (FP32
-    Biot media; the others keep the split)."""
+    FDP_KERNEL_VARIANT: the frame/core split on two streams or in one
+    launch per phase, the unit kernels over the whole grid, the TMA-staged
+    kernels, the split with TMA-staged persistent core kernels (FP32 Biot
+    media; the others keep the per-thread-load core), and the march kernel
+    doing both phases of the deep interior in one pass (the default; FP32
+    Biot media, the others keep the split)."""
     monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
     return request.param
 
@@ -131,7 +131,7 @@ def test_kernel_launch_count(kernel_variant):
     eng.time_loop(1, 70)
     eng.synchronize()
     runs = 3
-    if kernel_variant in ("core", "coretma", "march"):
+    if kernel_variant in ("split", "coretma", "march"):
         # (a table medium: the march variant leaves it to the split)
         assert eng.march_info() is None
         core = eng.core_info()

@@ -20,9 +20,9 @@ pytestmark = pytest.mark.gpu
 SPLITS = [(1, 1), (2, 3), (4, 34), (35, 66), (67, 67), (68, 100)]
 
 
-@pytest.fixture(params=["core", "march"])
+@pytest.fixture(params=["split", "march"])
 def variant(request, monkeypatch):
-    """The default split and the march variant, whose levels alternate
+    """The frame/core split and the march variant, whose levels alternate
     between two buffers of each field (runs of odd length end in the other
     buffers)."""
     monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)

@@ -14,7 +14,7 @@ from helpers import compare_state, randomize_state, small_job
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = ["core", "fused", "global", "tma", "coretma"]
+VARIANTS = ["split", "fused", "global", "tma", "coretma"]
 
 
 def _case(k: int):
