@@ -100,8 +100,11 @@ struct fdp_ctx {
   // medium is held as Biot planes
   fdp::MarchMaps mmaps[2]{};
   bool march_ready = false;
-  // set while a batch holds the context (its kernels update in place)
-  bool in_batch = false;
+  // set while a batch holds the context (its kernels update in place);
+  // batch_march while the batch's shots mode runs march levels of it, in
+  // pairs, so that every batch run ends in the buffers the batch's work-queue
+  // kernels were given
+  bool in_batch = false, batch_march = false;
   // captured runs of levels, indexed by the current buffer and by their
   // length (1..kRunGraphs); the longest is replayed over and over, a
   // shorter one ends a run

@@ -532,11 +532,12 @@ template <class T> void launch(fdp_ctx* c, const Params<T>& p, int kind, int it_
 }
 
 // Whether the levels run as march levels: the march variant planned a deep
-// interior and has its tensor maps, and neither a batch (whose kernels
-// update in place) nor an attached learned edge (whose kernels work on the
-// current buffers after every level) holds the context.
+// interior and has its tensor maps, and neither a batch (whose work-queue
+// kernels update in place; its shots mode runs march levels in pairs) nor
+// an attached learned edge (whose kernels work on the current buffers after
+// every level) holds the context.
 bool use_march(const fdp_ctx* c) {
-  return c->march && c->march_ready && !c->in_batch && !(c->edge && c->edge_attached);
+  return c->march && c->march_ready && (!c->in_batch || c->batch_march) && !(c->edge && c->edge_attached);
 }
 
 // After a march level the other buffers are current.
@@ -709,14 +710,21 @@ template <class T> int run_t(fdp_ctx* c, int it_begin, int it_end) {
   return FDP_OK;
 }
 
-// Captures the graphs a run of n_levels levels replays (fdp_prepare_run).
+// Captures the graphs a run of n_levels levels replays (fdp_prepare_run),
+// for a run starting in either buffer when the levels are march levels
+// (capture only records, so the buffers are swapped on the host alone).
 template <class T> int prepare_t(fdp_ctx* c, int n_levels) {
   Params<T> p;
   fill_params<T>(c, p);
   cudaGraphExec_t g = nullptr;
   int rc = FDP_OK;
-  if (n_levels >= kChunk) rc = run_graph<T>(c, p, kChunk, &g);
-  if (rc == FDP_OK && n_levels % kChunk) rc = run_graph<T>(c, p, n_levels % kChunk, &g);
+  const int parities = use_march(c) ? 2 : 1;
+  for (int k = 0; k < parities && rc == FDP_OK; ++k) {
+    if (k == 1) flip_buffers(c);
+    if (n_levels >= kChunk) rc = run_graph<T>(c, p, kChunk, &g);
+    if (rc == FDP_OK && n_levels % kChunk) rc = run_graph<T>(c, p, n_levels % kChunk, &g);
+    if (k == 1) flip_buffers(c);
+  }
   return rc;
 }
 
@@ -1739,20 +1747,39 @@ int batch_set_shape(fdp_batch* b, int m, int waves) {
   return m == FDP_BATCH_SHOTS ? FDP_OK : batch_queue(b);
 }
 
+// Of n levels of the shots mode, those a shot runs as march levels: an
+// even number (a march level leaves the other buffers current, and the
+// batch's work-queue kernels keep the ones they were given).
+int shots_march_levels(fdp_ctx* c, int n) {
+  c->batch_march = true;
+  const int nm = use_march(c) ? (n & ~1) : 0;
+  c->batch_march = false;
+  return nm;
+}
+
 // The shots mode: n levels of every shot with the shot's own kernels (the
-// level sequence fdp_run launches: frame/core split, folded row-1 and
-// receiver step, one k_edge at the end), each shot on its own stream,
-// forked from and joined back to the batch stream, so that the shots run
-// side by side.  Each shot's level counter starts where the batch set it
-// and advances by n at the end.
+// level sequence fdp_run launches: march levels or the frame/core split,
+// folded row-1 and receiver step, one k_edge at the end), each shot on its
+// own stream, forked from and joined back to the batch stream, so that the
+// shots run side by side.  A shot with march levels runs an even number of
+// them as one run and the odd last level, if any, as a run of its own in
+// place.  Each shot's level counter starts where the batch set it and
+// advances by n at the end.
 template <class T> void shots_levels(fdp_batch* b, int n) {
   cudaEventRecord(b->fork, b->stream);
   for (size_t s = 0; s < b->shots.size(); ++s) {
     fdp_ctx* c = b->shots[s];
-    Params<T> p;
-    fill_params<T>(c, p);
     cudaStreamWaitEvent(c->stream, b->fork, 0);
-    for (int k = 0; k < n; ++k) launch_level_any<T>(c, p, k, k == 0, k == n - 1);
+    const int nm = shots_march_levels(c, n);
+    Params<T> p;
+    if (nm > 0) {
+      c->batch_march = true;
+      fill_params<T>(c, p);
+      for (int k = 0; k < nm; ++k) launch_level_any<T>(c, p, k, k == 0, k == nm - 1);
+      c->batch_march = false;
+    }
+    fill_params<T>(c, p);
+    for (int k = nm; k < n; ++k) launch_level_any<T>(c, p, k, k == nm, k == n - 1);
     fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
     cudaEventRecord(b->shot_ev[s], c->stream);
     cudaStreamWaitEvent(b->stream, b->shot_ev[s], 0);
@@ -1761,7 +1788,16 @@ template <class T> void shots_levels(fdp_batch* b, int n) {
 
 long long shots_launches(const fdp_batch* b, int n) {
   long long total = 0;
-  for (const fdp_ctx* c : b->shots) total += run_launches(c, n) + 1;
+  for (fdp_ctx* c : b->shots) {
+    const int nm = shots_march_levels(c, n);
+    if (nm > 0) {
+      c->batch_march = true;
+      total += run_launches(c, nm);
+      c->batch_march = false;
+    }
+    if (n > nm) total += run_launches(c, n - nm);
+    total += 1;
+  }
   return total;
 }
 

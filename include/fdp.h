@@ -178,7 +178,9 @@ int fdp_run(fdp_ctx* ctx, int32_t it_begin, int32_t it_end);
  * levels and one graph of the remaining levels, each captured on its first
  * use (and again after a set_* call changes the device parameters).  A
  * caller that times its runs, or whose first run must not pay for the
- * capture, calls this beforehand.  No counterpart in the reference. */
+ * capture, calls this beforehand.  With march levels, whose runs of odd
+ * length end in the other buffers, the graphs of both buffers are
+ * captured.  No counterpart in the reference. */
 int fdp_prepare_run(fdp_ctx* ctx, int32_t n_levels);
 
 /* Copies receiver values of levels it_first..it_first+n_levels-1 (already

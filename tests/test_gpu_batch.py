@@ -131,6 +131,30 @@ def test_batch_rejects_bad_shots():
     assert err.value.code == -1
 
 
+def test_shots_mode_march_levels_between_queue_levels():
+    """In the shots mode a shot with march levels runs them in pairs and an
+    odd last level in place, so the work-queue kernels, which update the
+    buffers they were given in place, can take over between runs: shots
+    mode and queue runs of odd and even lengths, then levels alone, equal
+    the oracle bit for bit."""
+    from fdporo.engine import Batch
+    engs, orcs = _shots("f32", True, per_cell=True, nsteps=80)
+    assert engs[1].march_info() is not None
+    with Batch(engs) as b:
+        lo = 1
+        for shape, n in (((-1, 0), 7), ((2, 1), 5), ((-1, 0), 33), ((1, 0), 2), ((-1, 0), 4)):
+            b.set_shape(*shape)
+            b.time_loop(lo, lo + n - 1)
+            lo += n
+        b.synchronize()
+    for e in engs:
+        e.time_loop(lo, 61)
+    for e, o in zip(engs, orcs):
+        o.time_loop(1, 61)
+        compare_state(e, o)
+        np.testing.assert_array_equal(e.receivers(1, 61), o.receivers(1, 61))
+
+
 def test_march_shots_in_and_out_of_a_batch(monkeypatch):
     """Contexts made with the march variant alternate between two buffers of
     each field when run alone; a batch holding them updates them in place.
