@@ -420,23 +420,26 @@ bool plan_march(fdp_ctx* c) {
   m.nvec = nvec;
   m.nstrips = (nvec + fdp::kMarchVec - 1) / fdp::kMarchVec;
   m.total = (long long)m.nstrips * (fz1 - fz0);
-  // one CTA per SM (the stages take most of an SM's shared memory), the
-  // strips' rows split evenly among them
+  // bands of 8 rows (one CTA of eight warps per SM), 6 (six warps) or 4
+  // (two CTAs of four warps per SM); the strips' rows split evenly among
+  // the CTAs
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->g.device);
-  // bands of 8 rows (eight warps, the copies of one band ahead in flight)
-  // or of 6 (six warps, two bands ahead); measured on the layered 2048^2
-  // workload: 0.0900 and 0.0992 ms per level
   const char* er = std::getenv("FDP_MARCH_ROWS");
-  c->march_rows = er && std::atoi(er) == 6 ? 6 : 8;
-  const char* ec = std::getenv("FDP_MARCH_CTAS");
-  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sms, m.total);
-  cudaError_t e = c->march_rows == 8
-                      ? cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)fdp::MarchShape<8>::kSmem)
-                      : cudaFuncSetAttribute(fdp::k_march<fdp::M_BIOT, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)fdp::MarchShape<6>::kSmem);
+  const int rows = er ? std::atoi(er) : 8;
+  c->march_rows = rows == 4 || rows == 6 ? rows : 8;
+  int per_sm = 1;
+  cudaError_t e = cudaSuccess;
+  auto shape = [&](auto kernel, size_t smem, int ctas_per_sm) {
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    per_sm = ctas_per_sm;
+  };
+  if (c->march_rows == 4) shape(fdp::k_march<fdp::M_BIOT, 4>, fdp::MarchShape<4>::kSmem, fdp::MarchShape<4>::kCtasPerSm);
+  else if (c->march_rows == 6) shape(fdp::k_march<fdp::M_BIOT, 6>, fdp::MarchShape<6>::kSmem, fdp::MarchShape<6>::kCtasPerSm);
+  else shape(fdp::k_march<fdp::M_BIOT, 8>, fdp::MarchShape<8>::kSmem, fdp::MarchShape<8>::kCtasPerSm);
   if (e != cudaSuccess) return false;
+  const char* ec = std::getenv("FDP_MARCH_CTAS");
+  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : (long long)sms * per_sm, m.total);
   c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
   c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
   return true;
@@ -603,8 +606,11 @@ void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool firs
     if (c->march_rows == 8)
       fdp::k_march<MODE, 8><<<c->march_ctas, fdp::MarchShape<8>::kThreads, fdp::MarchShape<8>::kSmem, c->stream>>>(
           pm, c->mmaps[c->cur], c->mg, it_off);
-    else
+    else if (c->march_rows == 6)
       fdp::k_march<MODE, 6><<<c->march_ctas, fdp::MarchShape<6>::kThreads, fdp::MarchShape<6>::kSmem, c->stream>>>(
+          pm, c->mmaps[c->cur], c->mg, it_off);
+    else
+      fdp::k_march<MODE, 4><<<c->march_ctas, fdp::MarchShape<4>::kThreads, fdp::MarchShape<4>::kSmem, c->stream>>>(
           pm, c->mmaps[c->cur], c->mg, it_off);
   }
   if (c->core_ev[0][1]) cudaEventRecord(c->core_ev[0][1], c->stream);

@@ -3,25 +3,26 @@
 // A level is the stress phase (time_loop.F90:93-124) and then the velocity
 // phase (time_loop.F90:133-179).  In the interior both are the 4th-order
 // stencils of the core kernels, and a cell's new velocities need the new
-// stresses only within two cells of it.  So a CTA of R warps (R = 6 or 8)
-// owns a strip of 30 four-cell vectors (120 columns) and marches down a
-// range of its rows in bands of R rows: per band each warp computes the new
-// stresses of one row for the strip's vectors and one halo vector either
-// side (lanes 0 and 31), keeps them in a shared-memory ring of 16 rows, and,
-// after a barrier, the new velocities of the row two above from that ring.
-// A cell's stencils read the old wavefield (one buffer of each pair) and
-// write the new values to the other, so no CTA reads what another writes
-// during the launch.
+// stresses only within two cells of it.  So a CTA of R warps (R = 4, 6 or
+// 8) owns a strip of 30 four-cell vectors (120 columns) and marches down a
+// range of its rows in bands of R rows.  Step k of a range computes, after
+// one block barrier, the new velocities of band k-1 (each warp one row,
+// from the new stresses of the rows two above to two below it, kept in a
+// shared-memory ring of 2R+4 rows) and the new stresses of band k (each
+// warp one row, for the strip's vectors and one halo vector either side:
+// lanes 0 and 31), which go into the ring.  A cell's stencils read the old
+// wavefield (one buffer of each pair) and write the new values to the
+// other, so no CTA reads what another writes during the launch.
 //
 // Inputs arrive by bulk tensor copies (cp.async.bulk.tensor.2d), one box of
-// 128 columns by R rows per array: the old velocities into a ring of rows
-// (the R+4 a band's stencils reach and the bands ahead), the old stresses
-// and the ten coefficient planes into stages, one per band in flight.  One
-// thread issues the copies A bands ahead (two with bands of six rows), so
-// they are in flight while a band computes; every thread waits for its
-// band's copies on the stage's mbarrier with a bounded try_wait, and a wait
-// that gives up sets the status word, lets the copies in flight land
-// (bounded again) and returns.
+// 128 columns by R rows per array: the old velocities into a ring of 4R
+// rows (the 3R+4 a step reads and the next band's R), the old stresses and
+// the five stress planes of band k and the five velocity planes of band k-1
+// into one of two stages.  One thread issues the next step's copies as a
+// step starts, so they are in flight while the step computes; every thread
+// waits for its step's copies on the stage's mbarrier with a bounded
+// try_wait, and a wait that gives up sets the status word, lets the copies
+// in flight land (bounded again) and returns.
 //
 // Per cell the pass reads the old velocities and stresses and the ten
 // coefficient planes and writes the new velocities and stresses: 26 values
@@ -39,9 +40,10 @@
 // ordering between them.  The stress update of the source cell (LIN_X,
 // LIN_Z) adds the source term of stress_lin_nn.F90:58-63.
 //
-// The CTAs split the strips' rows evenly (one CTA per SM, the rows of all
-// strips taken as one sequence); a CTA whose range crosses into the next
-// strip starts again there.  FP32 with the ten planes of a Biot medium.
+// The CTAs split the strips' rows evenly (the rows of all strips taken as
+// one sequence; one CTA per SM, two with bands of four rows); a CTA whose
+// range crosses into the next strip starts again there.  FP32 with the ten
+// planes of a Biot medium.
 #pragma once
 
 #include "fdp_core_tma.cuh"
@@ -51,25 +53,23 @@ namespace fdp {
 constexpr int kMarchVec = 30;  // vectors a strip updates (lanes 1..30)
 constexpr int kMarchW = 128;   // box width: the strip's 32 vectors
 
-constexpr int kMarchDirect = 14;  // boxes of a stage: stresses (4), stress planes, velocity planes (5 each)
+constexpr int kMarchDirect = 14;  // boxes of a stage: stresses (4), stress planes (5), velocity planes (5)
 
-// Sizes of a CTA of R warps marching bands of R rows, with the copies of A
-// bands ahead in flight (R = 6: two ahead; R = 8: one ahead, as much as
-// the shared memory of a CTA holds).
+// Sizes of a CTA of R warps marching bands of R rows (R = 4, 6 or 8).  A
+// step reads 3R+4 rows of the velocity ring while the next band's R rows
+// arrive, and 2R+4 rows of the stress ring (R written, R+4 read).
 template <int R> struct MarchShape {
-  static constexpr int kAhead = R <= 6 ? 2 : 1;
   static constexpr int kThreads = 32 * R;
-  static constexpr int kSlots = kAhead + 2;  // velocity ring slots of R rows
-  static constexpr int kVRows = kSlots * R;  // velocity ring rows
-  static constexpr int kSRows = 16;          // stress ring rows (R + 4 needed)
-  static constexpr int kStages = kAhead + 1;
-  static constexpr int kBox = R * kMarchW;   // floats per box
+  static constexpr int kVRows = 4 * R;      // velocity ring rows (slots of R)
+  static constexpr int kSRows = 2 * R + 4;  // stress ring rows
+  static constexpr int kBox = R * kMarchW;  // floats per box
   static constexpr int kVRing = 4 * kVRows * kMarchW;
   static constexpr int kStage = kMarchDirect * kBox;
   static constexpr int kSRing = 4 * kSRows * kMarchW;
-  static constexpr size_t kSmem = (size_t)(kVRing + kStages * kStage + kSRing) * sizeof(float) + 128;
+  static constexpr size_t kSmem = (size_t)(kVRing + 2 * kStage + kSRing) * sizeof(float) + 128;
+  static constexpr int kCtasPerSm = kSmem <= 113 * 1024 ? 2 : 1;
   static_assert(kSmem <= 227 * 1024, "march stages exceed the shared memory of a CTA");
-  static_assert(R >= 4 && R + 4 <= kSRows, "a band's stencils reach four rows back");
+  static_assert(R >= 4, "a band's stencils reach four rows back");
 };
 
 // Tensor maps (boxes of 128 columns by R rows): the eight wavefield arrays
@@ -88,9 +88,11 @@ struct MarchGrid {
   long long total;         // nstrips * (fz1 - fz0)
 };
 
-// A band of a CTA: strip, the velocity rows [vlo, vhi) of its segment and
-// its index k there; its stresses are rows [vlo-2+Rk, vlo-2+R(k+1)) and its
-// velocities the rows two above those.  strip < 0: past the CTA's range.
+// A step of a CTA: strip, the velocity rows [vlo, vhi) of its segment and
+// its index k there.  Band k's stresses are rows [vlo-2+Rk, vlo-2+R(k+1))
+// and its velocities the rows two above those; step k computes the
+// stresses of band k and the velocities of band k-1.  strip < 0: past the
+// CTA's range.
 struct MarchBand {
   int strip, vlo, vhi, k;
 };
@@ -110,15 +112,15 @@ __device__ __forceinline__ void sts4s(float* s, const V4<float>& v) {
 }
 
 template <int MODE, int R>
-__global__ void __launch_bounds__(MarchShape<R>::kThreads, 1) k_march(const __grid_constant__ Params<float> p,
-                                                                           const __grid_constant__ MarchMaps maps,
-                                                                           const MarchGrid g, int it_off) {
+__global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasPerSm)
+    k_march(const __grid_constant__ Params<float> p, const __grid_constant__ MarchMaps maps, const MarchGrid g,
+            int it_off) {
   using Sh = MarchShape<R>;
   extern __shared__ unsigned char march_raw[];
   float* const vring = reinterpret_cast<float*>(((uintptr_t)march_raw + 127) & ~(uintptr_t)127);
   float* const stages = vring + Sh::kVRing;
-  float* const sring = stages + Sh::kStages * Sh::kStage;
-  __shared__ __align__(8) uint64_t full[Sh::kStages];
+  float* const sring = stages + 2 * Sh::kStage;
+  __shared__ __align__(8) uint64_t full[2];
   __shared__ int failed;
   const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // the CTA's rows [lo, hi) of the sequence of all strips' rows (H per strip)
@@ -129,45 +131,55 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 1) k_march(const __gr
     const long long e = (long long)(strip + 1) * H;
     return g.fz0 + (int)((e <= hi ? e : hi) - (long long)strip * H);
   };
+  // bands of a segment: their stresses reach two rows past its last velocity row
+  auto nbands = [&](const MarchBand& b) { return (b.vhi - b.vlo + 4 + R - 1) / R; };
+  // steps k = 0 .. nbands of a segment, then the next segment's
   auto next = [&](const MarchBand& b) -> MarchBand {
     if (b.strip < 0) return b;
-    if (b.k + 1 < (b.vhi - b.vlo + 4 + R - 1) / R) return {b.strip, b.vlo, b.vhi, b.k + 1};
+    if (b.k < nbands(b)) return {b.strip, b.vlo, b.vhi, b.k + 1};
     const int s = b.strip + 1;
     if ((long long)s * H >= hi) return {-1, 0, 0, 0};
     return {s, g.fz0, seg_end(s), 0};
   };
   if (tid == 0) {
-    for (int s = 0; s < Sh::kStages; ++s) mbar_init(&full[s], 1);
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
     failed = 0;
   }
   __syncthreads();
   if (lo >= hi) return;
 
-  // the copies of band b (the CTA's j-th): its new velocity rows into the
-  // ring, its old stresses and planes into stage j % kStages
+  // the copies of step b (the CTA's j-th) on barrier j % 2: band k's new
+  // velocity rows into the ring, its old stresses and stress planes into
+  // the stage (k < nbands), and band k-1's velocity planes (k >= 1)
   auto issue = [&](const MarchBand& b, int j) {
-    uint64_t* bar = &full[j % Sh::kStages];
-    float* st = stages + (j % Sh::kStages) * Sh::kStage;
+    uint64_t* bar = &full[j & 1];
+    float* st = stages + (j & 1) * Sh::kStage;
     const int x = g.fx0 + 4 * kMarchVec * b.strip - 4 - p.PMLL + kPadX;  // padded column of the box
-    const int r = b.vlo - 2 + R * b.k;                                      // first stress row
-    mbar_expect_tx(bar, (uint32_t)((b.k == 0 ? 22 : 18) * Sh::kBox * sizeof(float)));
-    // velocities: rows [r+2, r+2+R) into ring slot (k+1) % kSlots (the ring
-    // row of grid row y is (y - vlo + R) % kVRows); band 0 also rows
-    // [vlo-R, vlo) into slot 0
-    const int slot = ((b.k + 1) % Sh::kSlots) * R;
+    const int r = b.vlo - 2 + R * b.k;                                      // band k's first stress row
+    const bool s_ = b.k < nbands(b), v_ = b.k >= 1;
+    mbar_expect_tx(bar, (uint32_t)(((s_ ? (b.k == 0 ? 17 : 13) : 0) + (v_ ? 5 : 0)) * Sh::kBox * sizeof(float)));
+    if (s_) {
+      // velocities: rows [r+2, r+2+R) into ring slot (k+1) % 4 (the ring row
+      // of grid row y is (y - vlo + R) % 4R); band 0 also rows [vlo-R, vlo)
+      // into slot 0
+      const int slot = ((b.k + 1) & 3) * R;
 #pragma unroll
-    for (int f = 0; f < 4; ++f) {
-      float* fr = vring + f * Sh::kVRows * kMarchW;
-      tma_load_2d(fr + slot * kMarchW, &maps.f[f], x, r + 2 + kPadZ, bar);
-      if (b.k == 0) tma_load_2d(fr, &maps.f[f], x, b.vlo - R + kPadZ, bar);
+      for (int f = 0; f < 4; ++f) {
+        float* fr = vring + f * Sh::kVRows * kMarchW;
+        tma_load_2d(fr + slot * kMarchW, &maps.f[f], x, r + 2 + kPadZ, bar);
+        if (b.k == 0) tma_load_2d(fr, &maps.f[f], x, b.vlo - R + kPadZ, bar);
+      }
+#pragma unroll
+      for (int f = 0; f < 4; ++f) tma_load_2d(st + f * Sh::kBox, &maps.f[4 + f], x, r + kPadZ, bar);
+#pragma unroll
+      for (int s = 0; s < 5; ++s) tma_load_2d(st + (4 + s) * Sh::kBox, &maps.pl[s], x, r + kPadZ, bar);
     }
-    // stresses and stress planes of rows [r, r+R), velocity planes of rows [r-2, r+R-2)
+    if (v_) {
+      // band k-1's velocity rows [r-R-2, r-2)
 #pragma unroll
-    for (int f = 0; f < 4; ++f) tma_load_2d(st + f * Sh::kBox, &maps.f[4 + f], x, r + kPadZ, bar);
-#pragma unroll
-    for (int s = 0; s < 5; ++s) tma_load_2d(st + (4 + s) * Sh::kBox, &maps.pl[s], x, r + kPadZ, bar);
-#pragma unroll
-    for (int s = 0; s < 5; ++s) tma_load_2d(st + (9 + s) * Sh::kBox, &maps.pl[5 + s], x, r - 2 + kPadZ, bar);
+      for (int s = 0; s < 5; ++s) tma_load_2d(st + (9 + s) * Sh::kBox, &maps.pl[5 + s], x, r - R - 2 + kPadZ, bar);
+    }
   };
   const long long P = p.pitch;
   const int it = *p.it_base + it_off;
@@ -180,57 +192,81 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 1) k_march(const __gr
     srcF = ((SOURF - SOURFP) / p.DT);
   }
   const int lm = lane > 0 ? lane - 1 : 0, lp = lane < 31 ? lane + 1 : 31;  // x-neighbour vectors (clamped)
+  auto wrapv = [](int r) { return r >= Sh::kVRows ? r - Sh::kVRows : (r < 0 ? r + Sh::kVRows : r); };
+  auto wraps = [](int r) { return r >= Sh::kSRows ? r - Sh::kSRows : (r < 0 ? r + Sh::kSRows : r); };
 
   const int strip0 = (int)(lo / H);
   MarchBand b = {strip0, g.fz0 + (int)(lo - (long long)strip0 * H), seg_end(strip0), 0};
-  // bands issued so far: the CTA's bands 0 .. last, whose last one is `lb`
-  int last = -1;
-  MarchBand lb = b;
-  int i = 0;
-  for (; b.strip >= 0; ++i) {
-    // issue up to two bands ahead within the band's segment (a new segment's
-    // bands would overwrite ring rows the current ones read); a segment's
-    // first band is issued as it starts
-    if (tid == 0) {
-      if (last < i) {
-        issue(b, i);
-        last = i;
-        lb = b;
-      }
-      while (last < i + Sh::kAhead) {
-        const MarchBand nb = next(lb);
-        if (nb.strip != b.strip || nb.vlo != b.vlo || nb.strip < 0) break;
-        issue(nb, last + 1);
-        ++last;
-        lb = nb;
-      }
-    }
+  bool issued = false;  // step b's copies are in flight
+  int vk = 0, sk = 0;   // R*k modulo the ring sizes
+  int j = 0;
+  for (; b.strip >= 0; ++j) {
+    // the next step's copies go out as this one starts when it continues the
+    // segment (a new segment's would overwrite ring rows this one reads)
     const MarchBand nb = next(b);
-    if (!mbar_wait_bounded(&full[i % Sh::kStages], (uint32_t)((i / Sh::kStages) & 1))) failed = 1;
-    __syncthreads();
-    if (failed) {
-      if (tid == 0) atomicOr(p.err, 1);
-      break;
+    const bool ahead = nb.strip == b.strip;
+    if (tid == 0) {
+      if (!issued) issue(b, j);
+      if (ahead) issue(nb, j + 1);
     }
-    const float* S = stages + (i % Sh::kStages) * Sh::kStage;
+    issued = ahead;
+    const int nbk = nbands(b);
+    const float* S = stages + (j & 1) * Sh::kStage;
     const int v = kMarchVec * b.strip + lane - 1;                  // the lane's vector of F
     const int I0 = g.fx0 + 4 * v;                                  // its first column
     const bool sok = v <= g.nvec;                                  // new stresses here (halo included)
     const bool own = lane >= 1 && lane <= kMarchVec && v < g.nvec;  // a vector of F this CTA updates
-    // ring rows of grid row Ls + d: velocity ring (Ls + d - vlo + R) % kVRows,
-    // stress ring (Ls + d - vlo + 2) % kSRows
-    const int vbase = (R * b.k + R - 2 + warp) % Sh::kVRows;
-    const int sbase = R * b.k + warp;
-    auto vrow = [&](int f, int d) {
-      int r = vbase + d;
-      r = r >= Sh::kVRows ? r - Sh::kVRows : (r < 0 ? r + Sh::kVRows : r);
-      return vring + (f * Sh::kVRows + r) * kMarchW;
-    };
-    auto srow = [&](int f, int d) { return sring + (f * Sh::kSRows + ((sbase + d) & (Sh::kSRows - 1))) * kMarchW; };
 
-    // ---- new stresses of row Ls for the strip's 32 vectors
+    // ---- new velocities of band k-1's row Lv from the stress ring (rows
+    // Lv-2..Lv+2, ring row (y - vlo + 2) % kSRows) and the old velocities
+    const int Lv = b.vlo - 4 + R * (b.k - 1) + warp;
+    const bool vel = b.k >= 1 && own && Lv >= b.vlo && Lv < b.vhi;
+    VelocityCoreIn<float> va;
+    V4<float> oum, owm, oqx, oqz;
+    if (vel) {
+      const int sb = sk - R - 2 + warp;
+      auto srow = [&](int f, int d) { return sring + (f * Sh::kSRows + wraps(sb + d)) * kMarchW; };
+      va.xxr[0] = lds4s(srow(1, 0) + 4 * lm); va.xxr[1] = lds4s(srow(1, 0) + 4 * lane);
+      va.xxr[2] = lds4s(srow(1, 0) + 4 * lp);
+      va.prr[0] = lds4s(srow(3, 0) + 4 * lm); va.prr[1] = lds4s(srow(3, 0) + 4 * lane);
+      va.prr[2] = lds4s(srow(3, 0) + 4 * lp);
+      va.xzr[0] = lds4s(srow(0, 0) + 4 * lm); va.xzr[1] = lds4s(srow(0, 0) + 4 * lane);
+      va.xzr[2] = lds4s(srow(0, 0) + 4 * lp);
+      va.prm2 = lds4s(srow(3, -2) + 4 * lane); va.prm1 = lds4s(srow(3, -1) + 4 * lane);
+      va.prp1 = lds4s(srow(3, 1) + 4 * lane);
+      va.xzm1 = lds4s(srow(0, -1) + 4 * lane); va.xzp1 = lds4s(srow(0, 1) + 4 * lane);
+      va.xzp2 = lds4s(srow(0, 2) + 4 * lane);
+      va.zzm2 = lds4s(srow(2, -2) + 4 * lane); va.zzm1 = lds4s(srow(2, -1) + 4 * lane);
+      va.zz0 = lds4s(srow(2, 0) + 4 * lane); va.zzp1 = lds4s(srow(2, 1) + 4 * lane);
+      const int vr = wrapv(vk - 4 + warp);
+      oum = lds4s(vring + (0 * Sh::kVRows + vr) * kMarchW + 4 * lane);
+      owm = lds4s(vring + (1 * Sh::kVRows + vr) * kMarchW + 4 * lane);
+      oqx = lds4s(vring + (2 * Sh::kVRows + vr) * kMarchW + 4 * lane);
+      oqz = lds4s(vring + (3 * Sh::kVRows + vr) * kMarchW + 4 * lane);
+    }
+    // this step's copies (issued a step ahead): a wait that gives up marks
+    // the CTA failed; its values are then garbage and it stops after the step
+    if (!mbar_wait_bounded(&full[j & 1], (uint32_t)((j >> 1) & 1))) failed = 1;
+    if (vel) {
+      V4<float> bio[5];
+      const float* prow = S + 9 * Sh::kBox + warp * kMarchW + 4 * lane;
+#pragma unroll
+      for (int s = 0; s < 5; ++s) bio[s] = lds4s(prow + s * Sh::kBox);
+      const long long c0 = (long long)Lv * P + (I0 - p.PMLL);
+      velocity_core_math<float, MODE>(p, c0, va, bio, oqx, oum, oqz, owm);
+      st4(p.oQX + c0, oqx);
+      st4(p.oUM + c0, oum);
+      st4(p.oQZ + c0, oqz);
+      st4(p.oWM + c0, owm);
+    }
+
+    // ---- new stresses of band k's row Ls for the strip's 32 vectors (ring
+    // rows of grid row Ls + d: velocity (Ls + d - vlo + R) % kVRows, stress
+    // (Ls - vlo + 2) % kSRows)
     const int Ls = b.vlo - 2 + R * b.k + warp;
-    if (sok) {
+    if (b.k < nbk && sok) {
+      const int vb = vk + R - 2 + warp;
+      auto vrow = [&](int f, int d) { return vring + (f * Sh::kVRows + wrapv(vb + d)) * kMarchW; };
       StressCoreIn<float> a;
       a.ur[0] = lds4s(vrow(0, 0) + 4 * lm); a.ur[1] = lds4s(vrow(0, 0) + 4 * lane); a.ur[2] = lds4s(vrow(0, 0) + 4 * lp);
       a.wr[0] = lds4s(vrow(1, 0) + 4 * lm); a.wr[1] = lds4s(vrow(1, 0) + 4 * lane); a.wr[2] = lds4s(vrow(1, 0) + 4 * lp);
@@ -251,10 +287,11 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 1) k_march(const __gr
       const long long c0 = (long long)Ls * P + (I0 - p.PMLL);
       const int src_j = (Ls == p.LIN_Z && p.LIN_X >= I0 && p.LIN_X < I0 + 4) ? p.LIN_X - I0 : -1;
       stress_core_math<float, MODE>(p, c0, a, bio, oxz, oxx, ozz, opr, src_j, srcS, srcF);
-      sts4s(srow(0, 0) + 4 * lane, oxz);
-      sts4s(srow(1, 0) + 4 * lane, oxx);
-      sts4s(srow(2, 0) + 4 * lane, ozz);
-      sts4s(srow(3, 0) + 4 * lane, opr);
+      float* sw = sring + wraps(sk + warp) * kMarchW + 4 * lane;
+      sts4s(sw, oxz);
+      sts4s(sw + Sh::kSRows * kMarchW, oxx);
+      sts4s(sw + 2 * Sh::kSRows * kMarchW, ozz);
+      sts4s(sw + 3 * Sh::kSRows * kMarchW, opr);
       if (own && I0 >= g.sx0 && I0 < g.sx1 && Ls >= b.vlo && Ls < b.vhi && Ls >= g.sz0 && Ls < g.sz1) {
         st4(p.oTXZ + c0, oxz);
         st4(p.oTXX + c0, oxx);
@@ -262,44 +299,24 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, 1) k_march(const __gr
         st4(p.oPRES + c0, opr);
       }
     }
-    __syncthreads();
-
-    // ---- new velocities of row Lv = Ls - 2 from the stress ring rows Lv-2..Lv+2
-    const int Lv = Ls - 2;
-    if (own && Lv >= b.vlo && Lv < b.vhi) {
-      VelocityCoreIn<float> a;
-      a.xxr[0] = lds4s(srow(1, -2) + 4 * lm); a.xxr[1] = lds4s(srow(1, -2) + 4 * lane);
-      a.xxr[2] = lds4s(srow(1, -2) + 4 * lp);
-      a.prr[0] = lds4s(srow(3, -2) + 4 * lm); a.prr[1] = lds4s(srow(3, -2) + 4 * lane);
-      a.prr[2] = lds4s(srow(3, -2) + 4 * lp);
-      a.xzr[0] = lds4s(srow(0, -2) + 4 * lm); a.xzr[1] = lds4s(srow(0, -2) + 4 * lane);
-      a.xzr[2] = lds4s(srow(0, -2) + 4 * lp);
-      a.prm2 = lds4s(srow(3, -4) + 4 * lane); a.prm1 = lds4s(srow(3, -3) + 4 * lane);
-      a.prp1 = lds4s(srow(3, -1) + 4 * lane);
-      a.xzm1 = lds4s(srow(0, -3) + 4 * lane); a.xzp1 = lds4s(srow(0, -1) + 4 * lane);
-      a.xzp2 = lds4s(srow(0, 0) + 4 * lane);
-      a.zzm2 = lds4s(srow(2, -4) + 4 * lane); a.zzm1 = lds4s(srow(2, -3) + 4 * lane);
-      a.zz0 = lds4s(srow(2, -2) + 4 * lane); a.zzp1 = lds4s(srow(2, -1) + 4 * lane);
-      V4<float> oum = lds4s(vrow(0, -2) + 4 * lane), owm = lds4s(vrow(1, -2) + 4 * lane),
-                oqx = lds4s(vrow(2, -2) + 4 * lane), oqz = lds4s(vrow(3, -2) + 4 * lane);
-      V4<float> bio[5];
-      const float* prow = S + 9 * Sh::kBox + warp * kMarchW + 4 * lane;
-#pragma unroll
-      for (int s = 0; s < 5; ++s) bio[s] = lds4s(prow + s * Sh::kBox);
-      const long long c0 = (long long)Lv * P + (I0 - p.PMLL);
-      velocity_core_math<float, MODE>(p, c0, a, bio, oqx, oum, oqz, owm);
-      st4(p.oQX + c0, oqx);
-      st4(p.oUM + c0, oum);
-      st4(p.oQZ + c0, oqz);
-      st4(p.oWM + c0, owm);
+    __syncthreads();  // the stage, the new stresses and the ring rows later copies overwrite
+    if (failed) {
+      if (tid == 0) atomicOr(p.err, 1);
+      break;
     }
-    __syncthreads();  // the stage, and the ring rows later copies overwrite, are free
+    if (ahead) {
+      vk = vk + R >= Sh::kVRows ? vk + R - Sh::kVRows : vk + R;
+      sk = sk + R >= Sh::kSRows ? sk + R - Sh::kSRows : sk + R;
+    } else {
+      vk = 0;
+      sk = 0;
+    }
     b = nb;
   }
-  // after a wait that gave up, let the copies still in flight (bands i..last)
-  // land before the CTA exits (bounded)
+  // after a wait that gave up, let the copies still in flight (this step's
+  // and the next one's) land before the CTA exits (bounded)
   if (failed && tid == 0)
-    for (int j = i; j <= last; ++j) mbar_wait_bounded(&full[j % Sh::kStages], (uint32_t)((j / Sh::kStages) & 1));
+    for (int q = j; q <= j + (issued ? 1 : 0); ++q) mbar_wait_bounded(&full[q & 1], (uint32_t)((q >> 1) & 1));
 }
 
 }  // namespace fdp

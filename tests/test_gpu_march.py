@@ -76,10 +76,10 @@ def test_any_split_of_the_rows_among_ctas(ctas, monkeypatch):
     compare_state(eng, orc)
 
 
-@pytest.mark.parametrize("rows", [6, 8])
+@pytest.mark.parametrize("rows", [4, 6, 8])
 @pytest.mark.parametrize("ctas", [3, 152])
 def test_band_rows(rows, ctas, monkeypatch):
-    """Bands of six rows (copies two bands ahead) and of eight (one ahead)."""
+    """Bands of four rows (two CTAs per SM), six and eight."""
     monkeypatch.setenv("FDP_MARCH_ROWS", str(rows))
     monkeypatch.setenv("FDP_MARCH_CTAS", str(ctas))
     cfg, med = small_job(mx=251, mz=97, tpml=6, nsteps=21, si=True, per_cell=True, seed=60 + rows)
