@@ -82,11 +82,12 @@ struct fdp_ctx {
   // set while jm, coef, planes and aux belong to a share with other
   // contexts (the share frees them, not this context)
   std::shared_ptr<MediumShare> medium_share;
-  // march variant (FDP_KERNEL_VARIANT=march): each level's interior in one
+  // march levels (the default for FP32 Biot media whose levels outgrow L2;
+  // FDP_KERNEL_VARIANT=march forces them): each level's interior in one
   // pass, the levels alternating between the two buffers of each wavefield
   // array.  fields[] always holds the current level's buffers and alt[] the
   // other ones; cur tells which of the two allocations fields[] is (0 or 1).
-  bool march = false;
+  bool march = false, march_forced = false;  // forced: named by FDP_KERNEL_VARIANT, whatever the grid size
   DevArr alt[8];
   int cur = 0;
   fdp::MarchGrid mg{};

@@ -420,14 +420,37 @@ bool plan_march(fdp_ctx* c) {
   m.nvec = nvec;
   m.nstrips = (nvec + fdp::kMarchVec - 1) / fdp::kMarchVec;
   m.total = (long long)m.nstrips * (fz1 - fz0);
-  // bands of 8 rows (one CTA of eight warps per SM), 6 (six warps) or 4
-  // (two CTAs of four warps per SM); the strips' rows split evenly among
-  // the CTAs
-  int sms = 152;
+  int sms = 152, l2 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->g.device);
+  cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->g.device);
+  // Unless named, march levels run only where a level's data outgrow L2:
+  // below that the split's second phase finds the first phase's output in
+  // L2.  Measured on layered grids: 1280^2 (166 MB per level in the march
+  // kernel, L2 129 MB) split 0.0379 ms, march 0.0410; 1408^2 (204 MB) 0.0476
+  // and 0.0472; 2048^2 0.0967 and 0.0833.
+  const double level_bytes = (double)nvec * 4 * (fz1 - fz0) * 104.0;
+  if (!c->march_forced && level_bytes < 1.5 * l2) return false;
+  // the same number of CTAs on every strip, each a contiguous range of the
+  // strip's rows: the CTAs then march down the same rows of every strip
+  // together, and the boxes they read at a time make up whole rows of the
+  // arrays.  Measured with bands of 8 rows: 2816^2 (24 strips) at 152 CTAs,
+  // whose ranges drift against the strips, 0.196 ms per level; at 144 (six
+  // per strip) 0.145 ms.
+  auto aligned = [&](long long slots) {
+    return m.nstrips <= slots ? slots / m.nstrips * m.nstrips : slots;
+  };
+  // bands of 8 rows (one CTA of eight warps per SM) or of 4 (two CTAs of
+  // four warps per SM), whichever leaves fewer SM slots idle (8 on a tie);
+  // 6 (six warps) on request.  2048^2 (17 strips): 136 CTAs of 8 rows
+  // 0.0853 ms, 289 of 4 rows 0.0833; 4096^2 (34 strips): 136 CTAs of 8
+  // rows 0.2900 ms, 272 of 4 rows 0.2955.
   const char* er = std::getenv("FDP_MARCH_ROWS");
-  const int rows = er ? std::atoi(er) : 8;
-  c->march_rows = rows == 4 || rows == 6 ? rows : 8;
+  const int rows = er ? std::atoi(er) : 0;
+  if (rows == 4 || rows == 6 || rows == 8) c->march_rows = rows;
+  else {
+    const double u8 = (double)aligned(sms) / sms, u4 = (double)aligned(2LL * sms) / (2.0 * sms);
+    c->march_rows = u4 > u8 + 0.02 ? 4 : 8;
+  }
   int per_sm = 1;
   cudaError_t e = cudaSuccess;
   auto shape = [&](auto kernel, size_t smem, int ctas_per_sm) {
@@ -439,7 +462,7 @@ bool plan_march(fdp_ctx* c) {
   else shape(fdp::k_march<fdp::M_BIOT, 8>, fdp::MarchShape<8>::kSmem, fdp::MarchShape<8>::kCtasPerSm);
   if (e != cudaSuccess) return false;
   const char* ec = std::getenv("FDP_MARCH_CTAS");
-  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : (long long)sms * per_sm, m.total);
+  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : aligned((long long)sms * per_sm), m.total);
   c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
   c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
   return true;
@@ -1048,7 +1071,8 @@ int fdp_create(const fdp_grid* g, fdp_ctx** out) {
   c->core_tma_req = c->use_core && variant && std::strcmp(variant, "coretma") == 0;
   // march levels unless a variant is named ("split" or "core": the
   // frame/core split alone); plan_core and the medium decide whether they run
-  c->march = c->use_core && (!variant || !*variant || std::strcmp(variant, "march") == 0);
+  c->march_forced = variant && std::strcmp(variant, "march") == 0;
+  c->march = c->use_core && (!variant || !*variant || c->march_forced);
   if (c->use_core) {
     if ((rc = plan_core(c)) != FDP_OK) return bail(rc);
     e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);

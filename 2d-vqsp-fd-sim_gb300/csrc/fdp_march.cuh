@@ -151,7 +151,11 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
 
   // the copies of step b (the CTA's j-th) on barrier j % 2: band k's new
   // velocity rows into the ring, its old stresses and stress planes into
-  // the stage (k < nbands), and band k-1's velocity planes (k >= 1)
+  // the stage (k < nbands), and band k-1's velocity planes (k >= 1).  The
+  // ring slots rotate with the CTA's steps, across segments too: step j's
+  // band goes to slot (j+1) % 4 and a segment's first rows, [vlo-R, vlo),
+  // to slot j % 4, so a ring row of step j's segment is at
+  // (4R + R*j + R - 2 + y - r) % 4R for grid row y (r its first stress row)
   auto issue = [&](const MarchBand& b, int j) {
     uint64_t* bar = &full[j & 1];
     float* st = stages + (j & 1) * Sh::kStage;
@@ -160,15 +164,12 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
     const bool s_ = b.k < nbands(b), v_ = b.k >= 1;
     mbar_expect_tx(bar, (uint32_t)(((s_ ? (b.k == 0 ? 17 : 13) : 0) + (v_ ? 5 : 0)) * Sh::kBox * sizeof(float)));
     if (s_) {
-      // velocities: rows [r+2, r+2+R) into ring slot (k+1) % 4 (the ring row
-      // of grid row y is (y - vlo + R) % 4R); band 0 also rows [vlo-R, vlo)
-      // into slot 0
-      const int slot = ((b.k + 1) & 3) * R;
+      const int slot = ((j + 1) & 3) * R, pro = (j & 3) * R;
 #pragma unroll
       for (int f = 0; f < 4; ++f) {
         float* fr = vring + f * Sh::kVRows * kMarchW;
         tma_load_2d(fr + slot * kMarchW, &maps.f[f], x, r + 2 + kPadZ, bar);
-        if (b.k == 0) tma_load_2d(fr, &maps.f[f], x, b.vlo - R + kPadZ, bar);
+        if (b.k == 0) tma_load_2d(fr + pro * kMarchW, &maps.f[f], x, b.vlo - R + kPadZ, bar);
       }
 #pragma unroll
       for (int f = 0; f < 4; ++f) tma_load_2d(st + f * Sh::kBox, &maps.f[4 + f], x, r + kPadZ, bar);
@@ -197,19 +198,20 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
 
   const int strip0 = (int)(lo / H);
   MarchBand b = {strip0, g.fz0 + (int)(lo - (long long)strip0 * H), seg_end(strip0), 0};
-  bool issued = false;  // step b's copies are in flight
-  int vk = 0, sk = 0;   // R*k modulo the ring sizes
+  int vk = 0, sk = 0;  // R*j modulo the ring sizes
   int j = 0;
+  bool issued = false;  // step j+1's copies are in flight
   for (; b.strip >= 0; ++j) {
-    // the next step's copies go out as this one starts when it continues the
-    // segment (a new segment's would overwrite ring rows this one reads)
+    // the next step's copies go out as this one starts: a new segment's
+    // first step follows the old segment's last, which computes velocities
+    // only and reads the ring slots (j-1) % 4 and j % 4, while the new
+    // segment's copies go to slots (j+1) % 4 and (j+2) % 4
     const MarchBand nb = next(b);
-    const bool ahead = nb.strip == b.strip;
     if (tid == 0) {
-      if (!issued) issue(b, j);
-      if (ahead) issue(nb, j + 1);
+      if (j == 0) issue(b, 0);
+      if (nb.strip >= 0) issue(nb, j + 1);
     }
-    issued = ahead;
+    issued = nb.strip >= 0;
     const int nbk = nbands(b);
     const float* S = stages + (j & 1) * Sh::kStage;
     const int v = kMarchVec * b.strip + lane - 1;                  // the lane's vector of F
@@ -218,7 +220,8 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
     const bool own = lane >= 1 && lane <= kMarchVec && v < g.nvec;  // a vector of F this CTA updates
 
     // ---- new velocities of band k-1's row Lv from the stress ring (rows
-    // Lv-2..Lv+2, ring row (y - vlo + 2) % kSRows) and the old velocities
+    // Lv-2..Lv+2; stress row r + w of step j's band at ring row
+    // (R*j + w) % kSRows) and the old velocities
     const int Lv = b.vlo - 4 + R * (b.k - 1) + warp;
     const bool vel = b.k >= 1 && own && Lv >= b.vlo && Lv < b.vhi;
     VelocityCoreIn<float> va;
@@ -260,9 +263,7 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
       st4(p.oWM + c0, owm);
     }
 
-    // ---- new stresses of band k's row Ls for the strip's 32 vectors (ring
-    // rows of grid row Ls + d: velocity (Ls + d - vlo + R) % kVRows, stress
-    // (Ls - vlo + 2) % kSRows)
+    // ---- new stresses of band k's row Ls for the strip's 32 vectors
     const int Ls = b.vlo - 2 + R * b.k + warp;
     if (b.k < nbk && sok) {
       const int vb = vk + R - 2 + warp;
@@ -304,13 +305,8 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
       if (tid == 0) atomicOr(p.err, 1);
       break;
     }
-    if (ahead) {
-      vk = vk + R >= Sh::kVRows ? vk + R - Sh::kVRows : vk + R;
-      sk = sk + R >= Sh::kSRows ? sk + R - Sh::kSRows : sk + R;
-    } else {
-      vk = 0;
-      sk = 0;
-    }
+    vk = vk + R >= Sh::kVRows ? vk + R - Sh::kVRows : vk + R;
+    sk = sk + R >= Sh::kSRows ? sk + R - Sh::kSRows : sk + R;
     b = nb;
   }
   // after a wait that gave up, let the copies still in flight (this step's

@@ -131,13 +131,14 @@ def test_batch_rejects_bad_shots():
     assert err.value.code == -1
 
 
-def test_shots_mode_march_levels_between_queue_levels():
+def test_shots_mode_march_levels_between_queue_levels(monkeypatch):
     """In the shots mode a shot with march levels runs them in pairs and an
     odd last level in place, so the work-queue kernels, which update the
     buffers they were given in place, can take over between runs: shots
     mode and queue runs of odd and even lengths, then levels alone, equal
     the oracle bit for bit."""
     from fdporo.engine import Batch
+    monkeypatch.setenv("FDP_KERNEL_VARIANT", "march")
     engs, orcs = _shots("f32", True, per_cell=True, nsteps=80)
     assert engs[1].march_info() is not None
     with Batch(engs) as b:

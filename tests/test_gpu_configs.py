@@ -56,6 +56,8 @@ def test_layered_2048_full_grid_fp32():
     inp = job.prepare(cfg, med, "f32")
     eng, orc = job.make_engine(inp), make_oracle(inp, threads=THREADS)
     assert eng.medium_info()["mode"] == "biot"
+    if not os.environ.get("FDP_KERNEL_VARIANT"):
+        assert eng.march_info() is not None  # the default path here: march levels
     eng.time_loop(1, 200)
     orc.time_loop(1, 200)
     compare_state(eng, orc)

@@ -106,10 +106,12 @@ def test_launch_count():
     assert eng.kernel_launches() - n0 == 70 * 3 + 3 * 2 + 1
 
 
-@pytest.mark.parametrize("variant,march", [(None, True), ("", True), ("split", False), ("core", False)])
-def test_default_runs_march_levels(variant, march, monkeypatch):
-    """Without FDP_KERNEL_VARIANT an FP32 Biot context runs march levels;
-    a named split keeps it on the frame/core split.  Both equal the oracle
+@pytest.mark.parametrize("variant,march", [(None, False), ("", False), ("split", False), ("march", True)])
+def test_variant_choice_on_a_small_grid(variant, march, monkeypatch):
+    """Without FDP_KERNEL_VARIANT an FP32 Biot context runs march levels only
+    where its levels outgrow one and a half times L2 (the 2048^2 parity
+    test of test_gpu_configs.py runs them so); this small grid keeps the
+    split unless march levels are named.  Every choice equals the oracle
     bit for bit."""
     if variant is None:
         monkeypatch.delenv("FDP_KERNEL_VARIANT", raising=False)
@@ -122,6 +124,19 @@ def test_default_runs_march_levels(variant, march, monkeypatch):
     eng.time_loop(1, 9)
     orc.time_loop(1, 9)
     compare_state(eng, orc)
+
+
+def test_default_on_a_large_grid(monkeypatch):
+    """A 2048^2 layered FP32 context runs march levels by default, with the
+    same number of CTAs on every strip."""
+    from fdporo import job
+    monkeypatch.delenv("FDP_KERNEL_VARIANT", raising=False)
+    cfg, med = job.layered(mx=2048, mz=2048, nsteps=10)
+    eng = job.make_engine(job.prepare(cfg, med, "f32"))
+    info = eng.march_info()
+    assert info is not None
+    assert info["ctas"] % info["strips"] == 0
+    assert info["band_rows"] in (4, 8)
 
 
 def test_fp64_and_table_media_keep_the_split():
