@@ -422,6 +422,7 @@ bool plan_march(fdp_ctx* c) {
   m.total = (long long)m.nstrips * (fz1 - fz0);
   int sms = 152, l2 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->g.device);
+  if (const char* es = std::getenv("FDP_MARCH_SMS")) sms = std::max(1, std::min(sms, std::atoi(es)));  // plan for fewer SMs
   cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->g.device);
   // Unless named, march levels run only where a level's data outgrow L2:
   // below that the split's second phase finds the first phase's output in
@@ -431,13 +432,23 @@ bool plan_march(fdp_ctx* c) {
   const double level_bytes = (double)nvec * 4 * (fz1 - fz0) * 104.0;
   if (!c->march_forced && level_bytes < 1.5 * l2) return false;
   // the same number of CTAs on every strip, each a contiguous range of the
-  // strip's rows: the CTAs then march down the same rows of every strip
-  // together, and the boxes they read at a time make up whole rows of the
-  // arrays.  Measured with bands of 8 rows: 2816^2 (24 strips) at 152 CTAs,
-  // whose ranges drift against the strips, 0.196 ms per level; at 144 (six
-  // per strip) 0.145 ms.
-  auto aligned = [&](long long slots) {
-    return m.nstrips <= slots ? slots / m.nstrips * m.nstrips : slots;
+  // strip's rows (or, with more strips than CTA slots, the same number of
+  // whole strips per CTA): the CTAs then march down the same rows of every
+  // strip together, and the boxes they read at a time make up whole rows of
+  // the arrays.  Measured with bands of 8 rows: 2816^2 (24 strips) at 152
+  // CTAs, whose ranges drift against the strips, 0.196 ms per level; at 144
+  // (six per strip) 0.145 ms.  aligned(slots) = the CTAs and the range of
+  // each (0: the strips' rows split evenly), and the share of the slots'
+  // time they fill.
+  const int H = fz1 - fz0;
+  struct Split { long long ctas, span; double fill; };
+  auto aligned = [&](long long slots) -> Split {
+    if (m.nstrips <= slots) {
+      const long long n = slots / m.nstrips * m.nstrips;
+      return {n, 0, (double)n / slots};
+    }
+    const long long q = (m.nstrips + slots - 1) / slots;  // strips per CTA
+    return {(m.nstrips + q - 1) / q, q * H, (double)m.nstrips / ((double)q * slots)};
   };
   // bands of 8 rows (one CTA of eight warps per SM) or of 4 (two CTAs of
   // four warps per SM), whichever leaves fewer SM slots idle (8 on a tie);
@@ -448,8 +459,7 @@ bool plan_march(fdp_ctx* c) {
   const int rows = er ? std::atoi(er) : 0;
   if (rows == 4 || rows == 6 || rows == 8) c->march_rows = rows;
   else {
-    const double u8 = (double)aligned(sms) / sms, u4 = (double)aligned(2LL * sms) / (2.0 * sms);
-    c->march_rows = u4 > u8 + 0.02 ? 4 : 8;
+    c->march_rows = aligned(2LL * sms).fill > aligned(sms).fill + 0.02 ? 4 : 8;
   }
   int per_sm = 1;
   cudaError_t e = cudaSuccess;
@@ -461,8 +471,10 @@ bool plan_march(fdp_ctx* c) {
   else if (c->march_rows == 6) shape(fdp::k_march<fdp::M_BIOT, 6>, fdp::MarchShape<6>::kSmem, fdp::MarchShape<6>::kCtasPerSm);
   else shape(fdp::k_march<fdp::M_BIOT, 8>, fdp::MarchShape<8>::kSmem, fdp::MarchShape<8>::kCtasPerSm);
   if (e != cudaSuccess) return false;
+  const Split sp = aligned((long long)sms * per_sm);
   const char* ec = std::getenv("FDP_MARCH_CTAS");
-  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : aligned((long long)sms * per_sm), m.total);
+  m.span = ec ? 0 : sp.span;
+  c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sp.ctas, m.total);
   c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
   c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
   return true;

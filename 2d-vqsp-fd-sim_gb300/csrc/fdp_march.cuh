@@ -40,8 +40,10 @@
 // ordering between them.  The stress update of the source cell (LIN_X,
 // LIN_Z) adds the source term of stress_lin_nn.F90:58-63.
 //
-// The CTAs split the strips' rows evenly (the rows of all strips taken as
-// one sequence; one CTA per SM, two with bands of four rows); a CTA whose
+// The CTAs take contiguous ranges of the rows of all strips taken as one
+// sequence (one CTA per SM, two with bands of four rows): the same number
+// of CTAs on every strip, or, with more strips than CTAs, whole strips per
+// CTA, so that the CTAs march down the same rows together.  A CTA whose
 // range crosses into the next strip starts again there.  FP32 with the ten
 // planes of a Biot medium.
 #pragma once
@@ -86,6 +88,7 @@ struct MarchGrid {
   int sx0, sx1, sz0, sz1;  // where the kernel writes the new stresses
   int nstrips, nvec;       // strips, vectors across F
   long long total;         // nstrips * (fz1 - fz0)
+  long long span;          // rows of a CTA's range (whole strips), or 0: total split evenly
 };
 
 // A step of a CTA: strip, the velocity rows [vlo, vhi) of its segment and
@@ -125,8 +128,9 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
   const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // the CTA's rows [lo, hi) of the sequence of all strips' rows (H per strip)
   const int H = g.fz1 - g.fz0;
-  const long long lo = (long long)blockIdx.x * g.total / gridDim.x;
-  const long long hi = (long long)(blockIdx.x + 1) * g.total / gridDim.x;
+  const long long lo = g.span ? blockIdx.x * g.span : (long long)blockIdx.x * g.total / gridDim.x;
+  const long long hi = g.span ? (lo + g.span < g.total ? lo + g.span : g.total)
+                              : (long long)(blockIdx.x + 1) * g.total / gridDim.x;
   auto seg_end = [&](int strip) {  // the end of strip `strip`'s rows in the range
     const long long e = (long long)(strip + 1) * H;
     return g.fz0 + (int)((e <= hi ? e : hi) - (long long)strip * H);

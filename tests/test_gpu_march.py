@@ -76,6 +76,26 @@ def test_any_split_of_the_rows_among_ctas(ctas, monkeypatch):
     compare_state(eng, orc)
 
 
+@pytest.mark.parametrize("sms", [1, 2, 3])
+def test_whole_strips_per_cta(sms, monkeypatch):
+    """With more strips than CTA slots (planned here for 1-3 SMs) every CTA
+    takes the same number of whole strips, the last one the rest."""
+    monkeypatch.setenv("FDP_MARCH_SMS", str(sms))
+    cfg, med = small_job(mx=600, mz=60, tpml=5, nsteps=13, si=True, per_cell=True, seed=70 + sms)
+    inp, eng, orc = _pair(cfg, med)
+    info = eng.march_info()
+    strips = info["strips"]
+    assert strips == 5
+    slots = sms * (2 if info["band_rows"] == 4 else 1)
+    per = -(-strips // slots)
+    assert info["ctas"] == -(-strips // per)
+    randomize_state([eng, orc], inp, seed=71)
+    eng.time_loop(1, 13)
+    orc.time_loop(1, 13)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 13), orc.receivers(1, 13))
+
+
 @pytest.mark.parametrize("rows", [4, 6, 8])
 @pytest.mark.parametrize("ctas", [3, 152])
 def test_band_rows(rows, ctas, monkeypatch):
