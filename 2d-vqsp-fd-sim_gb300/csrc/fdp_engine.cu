@@ -1802,30 +1802,39 @@ int shots_march_levels(fdp_ctx* c, int n) {
 // The shots mode: n levels of every shot with the shot's own kernels (the
 // level sequence fdp_run launches: march levels or the frame/core split,
 // folded row-1 and receiver step, one k_edge at the end), each shot on its
-// own stream, forked from and joined back to the batch stream, so that the
-// shots run side by side.  A shot with march levels runs an even number of
-// them as one run and the odd last level, if any, as a run of its own in
-// place.  Each shot's level counter starts where the batch set it and
+// own stream, forked from and joined back to the batch stream.  Shots with
+// march levels run one after another (a march kernel's CTAs fill the GPU
+// in step with one another; side by side they would contend), the others
+// side by side after them.  A shot with march levels runs an even number
+// of them as one run and the odd last level, if any, as a run of its own
+// in place.  Each shot's level counter starts where the batch set it and
 // advances by n at the end.
 template <class T> void shots_levels(fdp_batch* b, int n) {
   cudaEventRecord(b->fork, b->stream);
-  for (size_t s = 0; s < b->shots.size(); ++s) {
-    fdp_ctx* c = b->shots[s];
-    cudaStreamWaitEvent(c->stream, b->fork, 0);
-    const int nm = shots_march_levels(c, n);
-    Params<T> p;
-    if (nm > 0) {
-      c->batch_march = true;
+  cudaEvent_t after = b->fork;
+  for (int pass = 0; pass < 2; ++pass) {
+    const cudaEvent_t start = after;
+    for (size_t s = 0; s < b->shots.size(); ++s) {
+      fdp_ctx* c = b->shots[s];
+      const int nm = shots_march_levels(c, n);
+      if ((pass == 0) != (nm > 0)) continue;
+      cudaStreamWaitEvent(c->stream, pass == 0 ? after : start, 0);
+      Params<T> p;
+      if (nm > 0) {
+        c->batch_march = true;
+        fill_params<T>(c, p);
+        for (int k = 0; k < nm; ++k) launch_level_any<T>(c, p, k, k == 0, k == nm - 1);
+        c->batch_march = false;
+      }
       fill_params<T>(c, p);
-      for (int k = 0; k < nm; ++k) launch_level_any<T>(c, p, k, k == 0, k == nm - 1);
-      c->batch_march = false;
+      for (int k = nm; k < n; ++k) launch_level_any<T>(c, p, k, k == nm, k == n - 1);
+      fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
+      cudaEventRecord(b->shot_ev[s], c->stream);
+      if (pass == 0) after = b->shot_ev[s];
+      else cudaStreamWaitEvent(b->stream, b->shot_ev[s], 0);
     }
-    fill_params<T>(c, p);
-    for (int k = nm; k < n; ++k) launch_level_any<T>(c, p, k, k == nm, k == n - 1);
-    fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
-    cudaEventRecord(b->shot_ev[s], c->stream);
-    cudaStreamWaitEvent(b->stream, b->shot_ev[s], 0);
   }
+  cudaStreamWaitEvent(b->stream, after, 0);
 }
 
 long long shots_launches(const fdp_batch* b, int n) {
