@@ -698,8 +698,11 @@ def run_large(args) -> None:
     # the planes as the engine pads them: pitch of NX + 8 rounded up to 32, NZ + 4 rows
     pitch = (inp.nx + 8 + 31) // 32 * 32
     plane_bytes = (medium["planes_stress"] + medium["planes_velocity"]) * 4 * pitch * (inp.nz + 4)
-    ab = algorithmic_bytes(inp, 4, medium)
-    level_bytes = n * (ab["stress"] + ab["velocity"])
+    march = owner.march_info()
+    ab = algorithmic_bytes(inp, 4, medium, core, march)
+    # a level's compulsory bytes: 104 B per cell of a march level's deep
+    # interior, both phases' bytes elsewhere
+    level_bytes = n * (ab["level"] if march else ab["stress"] + ab["velocity"])
     cells = n * inp.cells
     # the batch tunes its shape on its first 50 levels (9 queue shapes x 2,
     # then one 32-level graph of the shots mode)
@@ -752,9 +755,9 @@ def run_large(args) -> None:
         "single_shot": {"ms_per_level": ms_single, "shots_per_hour": shots_h(ms_single, 1),
                         "gcell_updates_per_s": inp.cells / (ms_single / 1e3) / 1e9},
         "speedup_vs_single_shot_path": shots_h(ms_batch, n) / shots_h(ms_single, 1),
-        "roofline": {"bound": "hbm", "kernel": "whole level (batched phases)", "achieved": gbs, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "whole level of every shot", "achieved": gbs, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": gbs / peak, "traffic": None,
-                     "alg_bytes_per_level": level_bytes},
+                     "alg_bytes_per_level": level_bytes, "march": march},
         "device_memory": {"used_bytes": used, "medium_planes_bytes": plane_bytes,
                           "without_sharing_bytes": used + (n - 1) * plane_bytes},
         "setup_s": {"medium_and_prepare": t_prep, "engines": t_upload},
