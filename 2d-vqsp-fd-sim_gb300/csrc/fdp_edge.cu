@@ -1,17 +1,22 @@
 // Learned absorbing edge (include/fdp_edge.h): the networks, their training
 // and their application after each time level.
 //
-// One CTA of 128 threads (4 warps) evaluates one tile of up to 128 samples
-// of one network ("set" = side x depth).  Its inputs are gathered straight
-// from the wavefield and the recorded history (or from a host-provided
-// array), rounded to bfloat16 into shared memory; each warp runs its 32
-// samples through the three layers with mma.sync m16n8k16 (bf16 operands,
-// FP32 accumulators starting from the bias), tanh on the hidden layers.
-// Training continues in the same CTA: one thread per sample back-propagates
-// in FP32 from the bf16 activations and weights, then the CTA reduces every
-// parameter's gradient over its samples into its own partial, and a second
-// kernel adds the tiles' partials to the gradient in tile order (no atomics:
-// training is bit-reproducible).
+// One CTA of one warp evaluates one tile of up to 32 samples of one network
+// ("set" = side x depth), so that a level's samples (about 12 x 520 on a
+// 512^2 region) spread over all SMs.  Its inputs are gathered straight from
+// the wavefield and the recorded history (or from a host-provided array),
+// rounded to bfloat16 into shared memory; the warp runs them through the
+// three layers with mma.sync m16n8k16 (bf16 operands, FP32 accumulators
+// starting from the bias), tanh on the hidden layers.  Training continues in
+// the same CTA, on the tensor cores too: the back-propagated errors of each
+// layer (rounded to bf16) times the transposed weights give the previous
+// layer's errors, and the errors' transpose times the layer's inputs gives
+// each weight gradient, all m16n8k16 products with FP32 accumulation over
+// the tile's samples; bias gradients are FP32 sums of the unrounded errors.
+// Every operand is staged K-contiguous in shared memory (transposed copies
+// where a product contracts over samples).  The CTA writes its tile's
+// partial gradient, and a second kernel adds the tiles' partials to the
+// gradient in tile order (no atomics: training is bit-reproducible).
 // Adam updates FP32 master weights and refreshes their bf16 copies.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -40,17 +45,31 @@ constexpr int oW1 = 0, oB1 = oW1 + kHid * kIn, oW2 = oB1 + kHid, oB2 = oW2 + kHi
               oB3 = oW3 + kOut * kHid, kSetP = oB3 + kOut;
 static_assert(kSetP == FDP_EDGE_SET_PARAMS, "parameter layout of a set");
 static_assert(kIn == 3 * 4 * 8, "inputs: 3 levels x 4 cells x 8 fields");
-constexpr int kTile = 128;             // samples per CTA
+constexpr int kTile = 32;               // samples per CTA (one warp)
 constexpr int sX = kIn + 8, sH = kHid + 8;  // padded shared-memory row strides (bf16 elements)
-constexpr int sD = kHid + 1, sY = kOut + 1;  // padded FP32 gradient rows (one thread per row)
+constexpr int sQ = kTile + 8;           // rows of transposed operands: one column per sample
+constexpr int sO = 16 + 8;              // output-layer rows padded to one k-step of 16
+constexpr int sY = kOut + 1;            // FP32 rows of outputs, errors and strip values
 
-// shared memory of the network kernel (bytes)
-constexpr size_t kSmW = (size_t)(kHid * sX + kHid * sH + kOut * sH) * 2;
-constexpr size_t kSmB = (size_t)(kHid + kHid + kOut) * 4;
-constexpr size_t kSmAct = (size_t)(kTile * sX + 2 * kTile * sH) * 2;  // X, H1, H2
-constexpr size_t kSmOut = (size_t)(2 * kTile * kOut) * 4;             // Y, target
-constexpr size_t kSmInfer = kSmW + kSmB + kSmAct + kSmOut;
-constexpr size_t kSmTrain = kSmInfer + (size_t)(2 * kTile * sD + 2 * kTile * sY) * 4;  // dZ1, dZ2, dY, V
+// shared memory of the network kernel (bytes, every array 16-byte aligned)
+constexpr size_t al16(size_t b) { return (b + 15) / 16 * 16; }
+struct NetSmem {
+  // forward: weights, biases, inputs, activations, outputs, targets
+  static constexpr size_t W1 = 0, W2 = W1 + al16((size_t)kHid * sX * 2), W3 = W2 + al16((size_t)kHid * sH * 2),
+                          B = W3 + al16((size_t)kOut * sH * 2), X = B + al16((size_t)(2 * kHid + kOut) * 4),
+                          H1 = X + al16((size_t)kTile * sX * 2), H2 = H1 + al16((size_t)kTile * sH * 2),
+                          Y = H2 + al16((size_t)kTile * sH * 2), Tg = Y + al16((size_t)kTile * kOut * 4),
+                          infer = Tg + al16((size_t)kTile * kOut * 4);
+  // training: transposed weights and activations, errors
+  static constexpr size_t W2T = infer, W3T = W2T + al16((size_t)kHid * sH * 2), XT = W3T + al16((size_t)kHid * sO * 2),
+                          H1T = XT + al16((size_t)kIn * sQ * 2), H2T = H1T + al16((size_t)kHid * sQ * 2),
+                          V = H2T + al16((size_t)kHid * sQ * 2), DY = V + al16((size_t)kTile * sY * 4),
+                          DYb = DY + al16((size_t)kTile * sY * 4), DYT = DYb + al16((size_t)kTile * sO * 2),
+                          D2 = DYT + al16((size_t)16 * sQ * 2), D2T = D2 + al16((size_t)kTile * sH * 2),
+                          D1T = D2T + al16((size_t)kHid * sQ * 2), train = D1T + al16((size_t)kHid * sQ * 2);
+};
+constexpr size_t kSmInfer = NetSmem::infer;
+constexpr size_t kSmTrain = NetSmem::train;
 // Damping output: a strip value v becomes v * (1 - alpha), alpha =
 // sigmoid(y + kDampBias) per field, so a new network (y = 0) damps by 1.8 %.
 constexpr float kDampBias = -4.f;
@@ -112,34 +131,6 @@ struct NetArgs {
 
 __device__ __forceinline__ uint32_t ld32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
-// out[(o0 + i) * ldo + k0 + j] = sum over samples q < n, in order, of
-// A[q * sA + o0 + i] * B[q * sB + k0 + j] (i < MO, j < MK): one thread's
-// block of a weight gradient.
-template <int MO, int MK>
-__device__ __forceinline__ void grad_block(const float* A, int sA, const bf16* B, int sB, int n, int o0, int k0,
-                                           float* out, int ldo) {
-  float acc[MO][MK];
-#pragma unroll
-  for (int i = 0; i < MO; ++i)
-#pragma unroll
-    for (int j = 0; j < MK; ++j) acc[i][j] = 0.f;
-  for (int q = 0; q < n; ++q) {
-    float d[MO], x[MK];
-#pragma unroll
-    for (int i = 0; i < MO; ++i) d[i] = A[q * sA + o0 + i];
-#pragma unroll
-    for (int j = 0; j < MK; ++j) x[j] = __bfloat162float(B[q * sB + k0 + j]);
-#pragma unroll
-    for (int i = 0; i < MO; ++i)
-#pragma unroll
-      for (int j = 0; j < MK; ++j) acc[i][j] += d[i] * x[j];
-  }
-#pragma unroll
-  for (int i = 0; i < MO; ++i)
-#pragma unroll
-    for (int j = 0; j < MK; ++j) out[(o0 + i) * ldo + k0 + j] = acc[i][j];
-}
-
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -186,6 +177,37 @@ __device__ __forceinline__ void warp_layer(const bf16* in, int si, const bf16* W
 
 enum Src { SRC_ARRAY = 0, SRC_BAND = 1 };
 
+// One 16 x 8 tile of D = A . B^T on the tensor cores: A [16 rows][K] and
+// B^T [8 rows][K], both bf16 with K contiguous (strides sa, sb elements),
+// K a multiple of 16; d the FP32 accumulators (rows g and g+8, columns 2t
+// and 2t+1 of the tile, g = lane / 4, t = lane % 4).
+template <int K>
+__device__ __forceinline__ void mma_tile(float (&d)[4], const bf16* A, int sa, const bf16* B, int sb) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int ks = 0; ks < K / 16; ++ks) {
+    const int k0 = ks * 16 + 2 * t;
+    const uint32_t a[4] = {ld32(A + g * sa + k0), ld32(A + (g + 8) * sa + k0), ld32(A + g * sa + k0 + 8),
+                           ld32(A + (g + 8) * sa + k0 + 8)};
+    mma_bf16(d, a, ld32(B + g * sb + k0), ld32(B + g * sb + k0 + 8));
+  }
+}
+
+// Sum over the 32 samples of a 32 x 8 block of FP32 errors held as two
+// m16n8 accumulator tiles (e[mt][4]): per column 2t and 2t+1, the sum of
+// the lane's four rows, then over the eight lanes sharing t (a fixed
+// shuffle tree: the same order every time).
+__device__ __forceinline__ float2 column_sums(const float (&e)[2][4]) {
+  float s0 = (e[0][0] + e[0][2]) + (e[1][0] + e[1][2]);
+  float s1 = (e[0][1] + e[0][3]) + (e[1][1] + e[1][3]);
+#pragma unroll
+  for (int off = 4; off < 32; off <<= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, off);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, off);
+  }
+  return make_float2(s0, s1);
+}
+
 // One tile of samples through the network; TRAIN adds the backward pass.
 // Output: array source -> y[first + s]; band source -> y[out_base + s] (the
 // correction buffer).  Inputs of a band sample: 3 levels (new, the history
@@ -195,26 +217,31 @@ enum Src { SRC_ARRAY = 0, SRC_BAND = 1 };
 template <int SRC, bool TRAIN>
 __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  bf16* W1 = reinterpret_cast<bf16*>(smem);
-  bf16* W2 = W1 + kHid * sX;
-  bf16* W3 = W2 + kHid * sH;
-  float* B1 = reinterpret_cast<float*>(W3 + kOut * sH);
+  using M = NetSmem;
+  bf16* W1 = reinterpret_cast<bf16*>(smem + M::W1);
+  bf16* W2 = reinterpret_cast<bf16*>(smem + M::W2);
+  bf16* W3 = reinterpret_cast<bf16*>(smem + M::W3);
+  float* B1 = reinterpret_cast<float*>(smem + M::B);
   float* B2 = B1 + kHid;
   float* B3 = B2 + kHid;
-  bf16* X = reinterpret_cast<bf16*>(B3 + kOut);
-  bf16* H1 = X + kTile * sX;
-  bf16* H2 = H1 + kTile * sH;
-  float* Y = reinterpret_cast<float*>(H2 + kTile * sH);
-  float* Tg = Y + kTile * kOut;
+  bf16* X = reinterpret_cast<bf16*>(smem + M::X);
+  bf16* H1 = reinterpret_cast<bf16*>(smem + M::H1);
+  bf16* H2 = reinterpret_cast<bf16*>(smem + M::H2);
+  float* Y = reinterpret_cast<float*>(smem + M::Y);
+  float* Tg = reinterpret_cast<float*>(smem + M::Tg);
+  float* V = reinterpret_cast<float*>(smem + M::V);  // training only
   const int4 tile = a.tiles[blockIdx.x];
   const int set = tile.x, first = tile.y, count = tile.z;
   const int tid = threadIdx.x;
-  // weights of the set
+  // weights of the set (pairs of bf16: every matrix starts on an even offset)
   const bf16* wb = a.wb + (size_t)set * kSetP;
   const float* wf = a.wf + (size_t)set * kSetP;
-  for (int k = tid; k < kHid * kIn; k += kTile) W1[(k / kIn) * sX + k % kIn] = wb[oW1 + k];
-  for (int k = tid; k < kHid * kHid; k += kTile) W2[(k / kHid) * sH + k % kHid] = wb[oW2 + k];
-  for (int k = tid; k < kOut * kHid; k += kTile) W3[(k / kHid) * sH + k % kHid] = wb[oW3 + k];
+  for (int k = 2 * tid; k < kHid * kIn; k += 2 * kTile)
+    *reinterpret_cast<uint32_t*>(W1 + (k / kIn) * sX + k % kIn) = ld32(wb + oW1 + k);
+  for (int k = 2 * tid; k < kHid * kHid; k += 2 * kTile)
+    *reinterpret_cast<uint32_t*>(W2 + (k / kHid) * sH + k % kHid) = ld32(wb + oW2 + k);
+  for (int k = 2 * tid; k < kOut * kHid; k += 2 * kTile)
+    *reinterpret_cast<uint32_t*>(W3 + (k / kHid) * sH + k % kHid) = ld32(wb + oW3 + k);
   for (int k = tid; k < kHid; k += kTile) { B1[k] = wf[oB1 + k]; B2[k] = wf[oB2 + k]; }
   if (tid < kOut) B3[tid] = wf[oB3 + tid];
   // inputs (and targets) of sample tid
@@ -253,7 +280,6 @@ __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a
       if (valid) a.geo.cell(set, i, 0, I, L);
       const long long c = (long long)L * a.t.pitch + (I - a.t.PMLL);
       const long long ce = (long long)L * a.e.pitch + (I + a.ox - a.e.PMLL);
-      float* V = Tg + kTile * kOut + 2 * kTile * sD + kTile * sY;
 #pragma unroll
       for (int f = 0; f < 8; ++f) {
         const float v = valid ? a.t.f[f][c] : 0.f;
@@ -262,89 +288,152 @@ __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a
       }
     }
   }
-  __syncthreads();
-  // forward, warp w on rows 32w .. 32w+31
-  const int r0 = (tid >> 5) * 32;
-  warp_layer<kIn, kHid, true>(X, sX, W1, sX, B1, r0, H1, sH, nullptr);
   __syncwarp();
-  warp_layer<kHid, kHid, true>(H1, sH, W2, sH, B2, r0, H2, sH, nullptr);
+  // forward
+  warp_layer<kIn, kHid, true>(X, sX, W1, sX, B1, 0, H1, sH, nullptr);
   __syncwarp();
-  warp_layer<kHid, kOut, false>(H2, sH, W3, sH, B3, r0, nullptr, 0, Y);
-  __syncthreads();
+  warp_layer<kHid, kHid, true>(H1, sH, W2, sH, B2, 0, H2, sH, nullptr);
+  __syncwarp();
+  warp_layer<kHid, kOut, false>(H2, sH, W3, sH, B3, 0, nullptr, 0, Y);
+  __syncwarp();
   if (valid && a.y) {
     float* out = a.y + (size_t)(SRC == SRC_ARRAY ? i : tile.w + tid) * kOut;
 #pragma unroll
     for (int o = 0; o < kOut; ++o) out[o] = Y[tid * kOut + o];
   }
-  if (!TRAIN) return;
-  // backward: thread tid = sample tid
-  float* DZ1 = Tg + kTile * kOut;
-  float* DZ2 = DZ1 + kTile * sD;
-  float* DY = DZ2 + kTile * sD;
-  const float* V = DY + kTile * sY;
-  float se = 0.f;
-#pragma unroll
-  for (int o = 0; o < kOut; ++o) {
-    const float y = Y[tid * kOut + o];
-    if (SRC == SRC_BAND && a.damping) {
-      // prediction -alpha * v of the scaled correction
-      const float al = 1.f / (1.f + expf(-(y + kDampBias)));
-      const float v = V[tid * sY + o];
-      const float r = valid ? -al * v - Tg[tid * kOut + o] : 0.f;
-      se += r * r;
-      DY[tid * sY + o] = r * a.gscale * (-v) * al * (1.f - al);
-    } else {
-      const float r = valid ? y - Tg[tid * kOut + o] : 0.f;
-      se += r * r;
-      DY[tid * sY + o] = r * a.gscale;
+  if constexpr (TRAIN) {
+    bf16* W2T = reinterpret_cast<bf16*>(smem + M::W2T);
+    bf16* W3T = reinterpret_cast<bf16*>(smem + M::W3T);
+    bf16* XT = reinterpret_cast<bf16*>(smem + M::XT);
+    bf16* H1T = reinterpret_cast<bf16*>(smem + M::H1T);
+    bf16* H2T = reinterpret_cast<bf16*>(smem + M::H2T);
+    float* DY = reinterpret_cast<float*>(smem + M::DY);
+    bf16* DYb = reinterpret_cast<bf16*>(smem + M::DYb);
+    bf16* DYT = reinterpret_cast<bf16*>(smem + M::DYT);
+    bf16* D2 = reinterpret_cast<bf16*>(smem + M::D2);
+    bf16* D2T = reinterpret_cast<bf16*>(smem + M::D2T);
+    bf16* D1T = reinterpret_cast<bf16*>(smem + M::D1T);
+    const bf16 zero = __float2bfloat16_rn(0.f);
+    // transposed operands: weights W2^T, W3^T (output rows padded to 16),
+    // and the sample's column of X^T, H1^T, H2^T
+    for (int k = tid; k < kHid * kHid; k += kTile) W2T[(k % kHid) * sH + k / kHid] = W2[(k / kHid) * sH + k % kHid];
+    for (int k = tid; k < kHid * 16; k += kTile) {
+      const int j = k / 16, o = k % 16;
+      W3T[j * sO + o] = o < kOut ? W3[o * sH + j] : zero;
     }
-  }
-  for (int j = 0; j < kHid; ++j) {
-    float s = 0.f;
+    for (int k = 0; k < kIn; ++k) XT[k * sQ + tid] = X[tid * sX + k];
+    for (int k = 0; k < kHid; ++k) {
+      H1T[k * sQ + tid] = H1[tid * sH + k];
+      H2T[k * sQ + tid] = H2[tid * sH + k];
+    }
+    // output error of sample tid: d loss / d y
+    float se = 0.f;
 #pragma unroll
-    for (int o = 0; o < kOut; ++o) s += DY[tid * sY + o] * __bfloat162float(W3[o * sH + j]);
-    const float h = __bfloat162float(H2[tid * sH + j]);
-    DZ2[tid * sD + j] = s * (1.f - h * h);
-  }
-  for (int k = 0; k < kHid; ++k) {
-    float s = 0.f;
-    for (int j = 0; j < kHid; ++j) s += DZ2[tid * sD + j] * __bfloat162float(W2[j * sH + k]);
-    const float h = __bfloat162float(H1[tid * sH + k]);
-    DZ1[tid * sD + k] = s * (1.f - h * h);
-  }
-  // sum of squared errors: warps in order, then the tile's partial (the
-  // partials of all tiles are added in tile order by k_grad_reduce, so a
-  // training step is bit-reproducible)
-  __shared__ double wloss[kTile / 32];
+    for (int o = 0; o < kOut; ++o) {
+      const float y = Y[tid * kOut + o];
+      float dy;
+      if (SRC == SRC_BAND && a.damping) {
+        // prediction -alpha * v of the scaled correction
+        const float al = 1.f / (1.f + expf(-(y + kDampBias)));
+        const float v = V[tid * sY + o];
+        const float r = valid ? -al * v - Tg[tid * kOut + o] : 0.f;
+        se += r * r;
+        dy = r * a.gscale * (-v) * al * (1.f - al);
+      } else {
+        const float r = valid ? y - Tg[tid * kOut + o] : 0.f;
+        se += r * r;
+        dy = r * a.gscale;
+      }
+      DY[tid * sY + o] = dy;
+      const bf16 b = __float2bfloat16_rn(dy);
+      DYb[tid * sO + o] = b;
+      DYb[tid * sO + kOut + o] = zero;
+      DYT[o * sQ + tid] = b;
+      DYT[(kOut + o) * sQ + tid] = zero;
+    }
+    // sum of squared errors of the tile (a fixed shuffle tree); the
+    // partials of all tiles are added in tile order by k_grad_reduce, so a
+    // training step is bit-reproducible
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) se += __shfl_xor_sync(0xffffffffu, se, off);
-  if ((tid & 31) == 0) wloss[tid >> 5] = (double)se;
-  __syncthreads();
-  if (tid == 0) {
-    double t = 0.0;
-    for (int w = 0; w < kTile / 32; ++w) t += wloss[w];
-    a.tloss[blockIdx.x] = t;
-  }
-  // parameter gradients, summed over the tile's samples in sample order:
-  // each thread a block of every weight matrix's gradient, its operands
-  // loaded once per sample for the whole block
-  static_assert(kTile == 128 && kHid == 64 && kIn == 96 && kOut == 8, "gradient blocks of the thread mapping");
-  float* grad = a.part + (size_t)blockIdx.x * kSetP;
-  const int n = min(count, kTile);
-  grad_block<4, 12>(DZ1, sD, X, sX, n, (tid >> 3) * 4, (tid & 7) * 12, grad + oW1, kIn);
-  grad_block<4, 8>(DZ2, sD, H1, sH, n, (tid >> 3) * 4, (tid & 7) * 8, grad + oW2, kHid);
-  grad_block<1, 4>(DY, sY, H2, sH, n, tid >> 4, (tid & 15) * 4, grad + oW3, kHid);
-  for (int e = tid; e < 2 * kHid + kOut; e += kTile) {
-    float s = 0.f;
-    if (e < kHid) {
-      for (int q = 0; q < n; ++q) s += DZ1[q * sD + e];
-      grad[oB1 + e] = s;
-    } else if (e < 2 * kHid) {
-      for (int q = 0; q < n; ++q) s += DZ2[q * sD + (e - kHid)];
-      grad[oB2 + e - kHid] = s;
-    } else {
-      for (int q = 0; q < n; ++q) s += DY[q * sY + (e - 2 * kHid)];
-      grad[oB3 + e - 2 * kHid] = s;
+    for (int off = 16; off > 0; off >>= 1) se += __shfl_xor_sync(0xffffffffu, se, off);
+    if (tid == 0) a.tloss[blockIdx.x] = (double)se;
+    __syncwarp();
+    float* grad = a.part + (size_t)blockIdx.x * kSetP;
+    const int g = tid >> 2, t = tid & 3;
+    // hidden layer 2: E2 = (dY . W3) * (1 - H2^2); bf16 copies E2 (rows) and
+    // E2^T; bias gradient from the FP32 values
+    for (int nt = 0; nt < kHid / 8; ++nt) {
+      float e[2][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_tile<16>(d, DYb + 16 * mt * sO, sO, W3T + 8 * nt * sO, sO);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int q = 16 * mt + g + 8 * (r >> 1), j = 8 * nt + 2 * t + (r & 1);
+          const float h = __bfloat162float(H2[q * sH + j]);
+          e[mt][r] = d[r] * (1.f - h * h);
+          const bf16 b = __float2bfloat16_rn(e[mt][r]);
+          D2[q * sH + j] = b;
+          D2T[j * sQ + q] = b;
+        }
+      }
+      const float2 sum = column_sums(e);
+      if (g == 0) { grad[oB2 + 8 * nt + 2 * t] = sum.x; grad[oB2 + 8 * nt + 2 * t + 1] = sum.y; }
+    }
+    __syncwarp();
+    // hidden layer 1: E1 = (E2 . W2) * (1 - H1^2); bf16 E1^T
+    for (int nt = 0; nt < kHid / 8; ++nt) {
+      float e[2][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_tile<kHid>(d, D2 + 16 * mt * sH, sH, W2T + 8 * nt * sH, sH);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int q = 16 * mt + g + 8 * (r >> 1), k = 8 * nt + 2 * t + (r & 1);
+          const float h = __bfloat162float(H1[q * sH + k]);
+          e[mt][r] = d[r] * (1.f - h * h);
+          D1T[k * sQ + q] = __float2bfloat16_rn(e[mt][r]);
+        }
+      }
+      const float2 sum = column_sums(e);
+      if (g == 0) { grad[oB1 + 8 * nt + 2 * t] = sum.x; grad[oB1 + 8 * nt + 2 * t + 1] = sum.y; }
+    }
+    __syncwarp();
+    // weight gradients over the tile's samples: dW3 = dY^T . H2 (rows 8..15
+    // of the padded dY^T are zero), dW2 = E2^T . H1, dW1 = E1^T . X
+    for (int nt = 0; nt < kHid / 8; ++nt) {
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+      mma_tile<kTile>(d, DYT, sQ, H2T + 8 * nt * sQ, sQ);
+      grad[oW3 + g * kHid + 8 * nt + 2 * t] = d[0];
+      grad[oW3 + g * kHid + 8 * nt + 2 * t + 1] = d[1];
+    }
+    for (int mt = 0; mt < kHid / 16; ++mt)
+      for (int nt = 0; nt < kHid / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_tile<kTile>(d, D2T + 16 * mt * sQ, sQ, H1T + 8 * nt * sQ, sQ);
+        const int j = 16 * mt + g, k = 8 * nt + 2 * t;
+        grad[oW2 + j * kHid + k] = d[0];
+        grad[oW2 + j * kHid + k + 1] = d[1];
+        grad[oW2 + (j + 8) * kHid + k] = d[2];
+        grad[oW2 + (j + 8) * kHid + k + 1] = d[3];
+      }
+    for (int mt = 0; mt < kHid / 16; ++mt)
+      for (int nt = 0; nt < kIn / 8; ++nt) {
+        float d[4] = {0.f, 0.f, 0.f, 0.f};
+        mma_tile<kTile>(d, D1T + 16 * mt * sQ, sQ, XT + 8 * nt * sQ, sQ);
+        const int k = 16 * mt + g, c = 8 * nt + 2 * t;
+        grad[oW1 + k * kIn + c] = d[0];
+        grad[oW1 + k * kIn + c + 1] = d[1];
+        grad[oW1 + (k + 8) * kIn + c] = d[2];
+        grad[oW1 + (k + 8) * kIn + c + 1] = d[3];
+      }
+    // output-layer bias: the FP32 output errors summed over samples in order
+    if (tid < kOut) {
+      float s = 0.f;
+      for (int q = 0; q < kTile; ++q) s += DY[q * sY + tid];
+      grad[oB3 + tid] = s;
     }
   }
 }

@@ -6,7 +6,11 @@ A numpy restatement of what include/fdp_edge.h specifies and
 rounded to bfloat16 (round to nearest even), products accumulated exactly
 here (float64) where the GPU accumulates in FP32 in its own order, so
 comparisons carry a tolerance; loss = mean over samples and outputs of
-(y - target)^2 and its gradient; Adam with beta1 0.9, beta2 0.999, eps 1e-8.
+(y - target)^2 and its gradient, back-propagated as the kernels do on the
+tensor cores: each layer's error rounded to bfloat16 before it multiplies
+the weights (the previous layer's error) or the layer's inputs (the weight
+gradient), bias gradients summed from the unrounded errors; Adam with beta1
+0.9, beta2 0.999, eps 1e-8.
 
 `exact=True` drops every rounding, which makes the forward pass a smooth
 function whose gradient the tests check against central differences --
@@ -74,9 +78,12 @@ def gradients(params: np.ndarray, sets: np.ndarray, x: np.ndarray, target: np.nd
         r = Y - np.asarray(target[idx], np.float64)
         loss += float(np.sum(r * r))
         dY = 2.0 * r / (n * OUT)
-        dZ2 = (dY @ W3) * (1.0 - H2 * H2)
-        dZ1 = (dZ2 @ W2) * (1.0 - H1 * H1)
-        g = {"W1": dZ1.T @ X, "b1": dZ1.sum(0), "W2": dZ2.T @ H1, "b2": dZ2.sum(0), "W3": dY.T @ H2, "b3": dY.sum(0)}
+        # the tensor-core operands: errors rounded to bf16 (none with exact)
+        q = (lambda v: np.asarray(v, np.float64)) if exact else (lambda v: bf16(v).astype(np.float64))
+        dZ2 = (q(dY) @ W3) * (1.0 - H2 * H2)
+        dZ1 = (q(dZ2) @ W2) * (1.0 - H1 * H1)
+        g = {"W1": q(dZ1).T @ X, "b1": dZ1.sum(0), "W2": q(dZ2).T @ H1, "b2": dZ2.sum(0), "W3": q(dY).T @ H2,
+             "b3": dY.sum(0)}
         for k, (o, m) in OFF.items():
             grad[s * SET_PARAMS + o:s * SET_PARAMS + o + m] = g[k].ravel()
     return grad, loss / (n * OUT)
