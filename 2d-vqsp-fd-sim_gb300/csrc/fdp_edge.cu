@@ -233,15 +233,39 @@ __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a
   const int4 tile = a.tiles[blockIdx.x];
   const int set = tile.x, first = tile.y, count = tile.z;
   const int tid = threadIdx.x;
-  // weights of the set (pairs of bf16: every matrix starts on an even offset)
+  // weights of the set, 8 bf16 per 16-byte load (every matrix and row of
+  // the set starts on a 16-byte boundary: kSetP, oW2, oW3, kIn and kHid are
+  // multiples of 8, as are the shared-memory strides)
+  static_assert(kSetP % 8 == 0 && oW2 % 8 == 0 && oW3 % 8 == 0 && kIn % 8 == 0 && kHid % 8 == 0 && sX % 8 == 0 &&
+                    sH % 8 == 0, "16-byte weight loads");
   const bf16* wb = a.wb + (size_t)set * kSetP;
   const float* wf = a.wf + (size_t)set * kSetP;
-  for (int k = 2 * tid; k < kHid * kIn; k += 2 * kTile)
-    *reinterpret_cast<uint32_t*>(W1 + (k / kIn) * sX + k % kIn) = ld32(wb + oW1 + k);
-  for (int k = 2 * tid; k < kHid * kHid; k += 2 * kTile)
-    *reinterpret_cast<uint32_t*>(W2 + (k / kHid) * sH + k % kHid) = ld32(wb + oW2 + k);
-  for (int k = 2 * tid; k < kOut * kHid; k += 2 * kTile)
-    *reinterpret_cast<uint32_t*>(W3 + (k / kHid) * sH + k % kHid) = ld32(wb + oW3 + k);
+  {
+    constexpr int n1 = kHid * kIn / 8, n2 = kHid * kHid / 8, n3 = kOut * kHid / 8;
+    uint4 v1[n1 / kTile], v2[n2 / kTile], v3[n3 / kTile];
+#pragma unroll
+    for (int r = 0; r < n1 / kTile; ++r) v1[r] = reinterpret_cast<const uint4*>(wb + oW1)[tid + r * kTile];
+#pragma unroll
+    for (int r = 0; r < n2 / kTile; ++r) v2[r] = reinterpret_cast<const uint4*>(wb + oW2)[tid + r * kTile];
+#pragma unroll
+    for (int r = 0; r < n3 / kTile; ++r) v3[r] = reinterpret_cast<const uint4*>(wb + oW3)[tid + r * kTile];
+#pragma unroll
+    for (int r = 0; r < n1 / kTile; ++r) {
+      const int k = 8 * (tid + r * kTile);
+      *reinterpret_cast<uint4*>(W1 + (k / kIn) * sX + k % kIn) = v1[r];
+    }
+#pragma unroll
+    for (int r = 0; r < n2 / kTile; ++r) {
+      const int k = 8 * (tid + r * kTile);
+      *reinterpret_cast<uint4*>(W2 + (k / kHid) * sH + k % kHid) = v2[r];
+    }
+#pragma unroll
+    for (int r = 0; r < n3 / kTile; ++r) {
+      const int k = 8 * (tid + r * kTile);
+      *reinterpret_cast<uint4*>(W3 + (k / kHid) * sH + k % kHid) = v3[r];
+    }
+    static_assert(n1 % kTile == 0 && n2 % kTile == 0 && n3 % kTile == 0, "weight loads per lane");
+  }
   for (int k = tid; k < kHid; k += kTile) { B1[k] = wf[oB1 + k]; B2[k] = wf[oB2 + k]; }
   if (tid < kOut) B3[tid] = wf[oB3 + tid];
   // inputs (and targets) of sample tid
@@ -439,7 +463,9 @@ __global__ void __launch_bounds__(kTile) k_net(const __grid_constant__ NetArgs a
 }
 
 // Adds the tiles' partial gradients to the gradient of their sets, each
-// parameter's partials in tile order, and their losses to the loss.
+// parameter's partials in tile order, and their losses to the loss.  The
+// tiles are sorted by set, so a set's tiles are the range a binary search
+// finds.
 __global__ void k_grad_reduce(const int4* __restrict__ tiles, int ntiles, const float* __restrict__ part,
                               const double* __restrict__ tloss, float* grad, double* loss) {
   const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -450,9 +476,13 @@ __global__ void k_grad_reduce(const int4* __restrict__ tiles, int ntiles, const 
   }
   if (k >= kSets * kSetP) return;
   const int set = k / kSetP, e = k % kSetP;
+  int lo = 0, hi = ntiles;  // first tile of the set
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (tiles[mid].x < set) lo = mid + 1; else hi = mid;
+  }
   float g = grad[k];
-  for (int q = 0; q < ntiles; ++q)
-    if (tiles[q].x == set) g += part[(size_t)q * kSetP + e];
+  for (int q = lo; q < ntiles && tiles[q].x == set; ++q) g += part[(size_t)q * kSetP + e];
   grad[k] = g;
 }
 
