@@ -295,16 +295,19 @@ def run_gpu(args) -> None:
     eng = job.make_engine(inp, device=dev)
     ext = torch.cuda.ExternalStream(eng.stream(), device=dev)
 
-    # ---- warm-up; the CUDA graphs of a run of args.steps levels are captured
-    # here, before the clock starts (fdp_run replays them)
-    eng.time_loop(1, args.warmup)
+    # ---- the CUDA graphs of the warm-up and of a run of args.steps levels
+    # are captured here, before the clock starts (fdp_run replays them)
+    eng.prepare_run(args.warmup)
     eng.prepare_run(args.steps)
     eng.synchronize()
-    # ---- timed region
-    n0 = eng.kernel_launches()
+    # ---- timed region, right after the warm-up levels (which run once the
+    # clock sampler is up, so that the GPU goes from them straight into the
+    # timed levels instead of from an idle pause)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clk:
         _barrier(ws)
+        eng.time_loop(1, args.warmup)
+        n0 = eng.kernel_launches()
         torch.cuda.synchronize()
         e0.record(ext)
         eng.time_loop(args.warmup + 1, args.warmup + args.steps)
