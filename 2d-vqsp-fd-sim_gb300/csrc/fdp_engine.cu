@@ -787,6 +787,13 @@ template <class F> void parallel_for(size_t n, F fn, size_t grain = 65536) {
 // A host array left uninitialised at allocation: the set-up writes every
 // element it uploads from its worker threads, so a single-threaded zero
 // fill of hundreds of MB (and its page faults) is not paid up front.
+// Whether the n values at a have one bit pattern.
+template <class T> bool same_run(const T* a, size_t n) {
+  for (size_t i = 1; i < n; ++i)
+    if (std::memcmp(&a[0], &a[i], sizeof(T)) != 0) return false;
+  return true;
+}
+
 template <class T> struct HostBuf {
   std::unique_ptr<T[]> p;
   size_t n = 0;
@@ -795,43 +802,14 @@ template <class T> struct HostBuf {
   const T& operator[](size_t i) const { return p[i]; }
   T* data() { return p.get(); }
   size_t size() const { return n; }
-};
-
-template <class T>
-void derive_table(const int32_t jmnum, const T* tab, HostBuf<T>& out) {
-  // table24 columns (.MO record order, read_model_par.F90:52-60)
-  enum { MU, SXX1, SXX2, SXX3, SZZ1, SZZ2, SZZ3, P1, P2, P3, R1U, R1W, R2U, R2W, R3U, R3W,
-         R1QX, R1QZ, R2QX, R2QZ, R3QX, R3QZ, AUXW, AUXQZ };
-  const size_t ld = (size_t)jmnum + 1;
-  out.reset(ld * fdp::C_NCOEF);
-  for (int k = 0; k < fdp::C_NCOEF; ++k) out[(size_t)k * ld] = T(0);  // index 0: no material
-  parallel_for((size_t)jmnum, [&](size_t jb, size_t je) {
-  for (int j = (int)jb + 1; j <= (int)je; ++j) {
-    const T* r = tab + (size_t)(j - 1) * 24;
-    auto put = [&](int k, T v) { out[(size_t)k * ld + j] = v; };
-    put(fdp::C_MU, r[MU]);
-    put(fdp::C_SXX1, r[SXX1]); put(fdp::C_SXX2, r[SXX2]); put(fdp::C_SXX3, r[SXX3]);
-    put(fdp::C_SZZ1, r[SZZ1]); put(fdp::C_SZZ2, r[SZZ2]); put(fdp::C_SZZ3, r[SZZ3]);
-    put(fdp::C_P1, r[P1]); put(fdp::C_P2, r[P2]); put(fdp::C_P3, r[P3]);
-    // inh_qx_int.F90:44 and inh_v_uv_int.F90:46, evaluated per material
-    // each exponential evaluated once (the same call gives the same value)
-    const T eqx = std::exp(-r[R3QX]), eqz = std::exp(-r[R3QZ]);
-    put(fdp::C_EQX, eqx);
-    put(fdp::C_CU, (r[R2U] / r[R3QX]) * (T(1) - eqx));
-    put(fdp::C_R1QX, r[R1QX]); put(fdp::C_R2QX, r[R2QX]);
-    put(fdp::C_R1U, r[R1U]); put(fdp::C_R3U, r[R3U]);
-    put(fdp::C_EQZ, eqz);
-    put(fdp::C_CW, (r[R2W] / r[R3QZ]) * (T(1) - eqz));
-    put(fdp::C_R1QZ, r[R1QZ]); put(fdp::C_R2QZ, r[R2QZ]);
-    put(fdp::C_R1W, r[R1W]); put(fdp::C_R3W, r[R3W]);
-    put(fdp::C_AUXW, r[AUXW]); put(fdp::C_AUXQZ, r[AUXQZ]);
+  // hands the memory to a thread of its own that frees it, so that the
+  // caller does not wait for hundreds of megabytes to be unmapped
+  void release_later() {
+    if (n >= ((size_t)1 << 24)) std::thread([q = std::move(p)]() mutable { q.reset(); }).detach();
+    p.reset();
+    n = 0;
   }
-  });
-}
-
-// Materials at most this many use table mode when some coefficient varies;
-// a larger table (one material per cell) is expanded into per-cell planes.
-constexpr int kMaxTableMaterials = 4096;
+};
 
 // Hashes of a column's bit patterns and of its negation's: four
 // interleaved 64-bit FNV-1a lanes each (independent multiply chains),
@@ -863,6 +841,80 @@ template <class T> void column_hash(const T* a, size_t n, uint64_t& hpos, uint64
   }
 }
 
+// The derived table of every material (column k at out[k * (jmnum+1) + j],
+// index 0 unused), and per column whether it is constant and the hashes
+// of its bit patterns and of their negation: materials in blocks of 65536,
+// derived and hashed block by block in parallel while the block is in
+// cache, the blocks' hashes combined in block order.
+template <class T>
+void derive_table(const int32_t jmnum, const T* tab, HostBuf<T>& out, bool* constant, uint64_t* hpos,
+                  uint64_t* hneg) {
+  // table24 columns (.MO record order, read_model_par.F90:52-60)
+  enum { MU, SXX1, SXX2, SXX3, SZZ1, SZZ2, SZZ3, P1, P2, P3, R1U, R1W, R2U, R2W, R3U, R3W,
+         R1QX, R1QZ, R2QX, R2QZ, R3QX, R3QZ, AUXW, AUXQZ };
+  const size_t ld = (size_t)jmnum + 1;
+  out.reset(ld * fdp::C_NCOEF);
+  for (int k = 0; k < fdp::C_NCOEF; ++k) out[(size_t)k * ld] = T(0);  // index 0: no material
+  constexpr size_t kBlk = 65536;
+  constexpr int NC = fdp::C_NCOEF;
+  const size_t nblk = ((size_t)jmnum + kBlk - 1) / kBlk;
+  std::vector<uint64_t> bp(nblk * NC), bn(nblk * NC);
+  std::vector<char> bconst(nblk * NC);
+  using U = typename std::conditional<sizeof(T) == 8, uint64_t, uint32_t>::type;
+  std::vector<U> bfirst(nblk * NC);
+  parallel_for(nblk, [&](size_t b0, size_t b1) {
+  for (size_t blk = b0; blk < b1; ++blk) {
+  const int jb = (int)(blk * kBlk), je = (int)std::min((size_t)jmnum, (blk + 1) * kBlk);
+  for (int j = jb + 1; j <= je; ++j) {
+    const T* r = tab + (size_t)(j - 1) * 24;
+    auto put = [&](int k, T v) { out[(size_t)k * ld + j] = v; };
+    put(fdp::C_MU, r[MU]);
+    put(fdp::C_SXX1, r[SXX1]); put(fdp::C_SXX2, r[SXX2]); put(fdp::C_SXX3, r[SXX3]);
+    put(fdp::C_SZZ1, r[SZZ1]); put(fdp::C_SZZ2, r[SZZ2]); put(fdp::C_SZZ3, r[SZZ3]);
+    put(fdp::C_P1, r[P1]); put(fdp::C_P2, r[P2]); put(fdp::C_P3, r[P3]);
+    // inh_qx_int.F90:44 and inh_v_uv_int.F90:46, evaluated per material
+    // each exponential evaluated once (the same call gives the same value)
+    const T eqx = std::exp(-r[R3QX]), eqz = std::exp(-r[R3QZ]);
+    put(fdp::C_EQX, eqx);
+    put(fdp::C_CU, (r[R2U] / r[R3QX]) * (T(1) - eqx));
+    put(fdp::C_R1QX, r[R1QX]); put(fdp::C_R2QX, r[R2QX]);
+    put(fdp::C_R1U, r[R1U]); put(fdp::C_R3U, r[R3U]);
+    put(fdp::C_EQZ, eqz);
+    put(fdp::C_CW, (r[R2W] / r[R3QZ]) * (T(1) - eqz));
+    put(fdp::C_R1QZ, r[R1QZ]); put(fdp::C_R2QZ, r[R2QZ]);
+    put(fdp::C_R1W, r[R1W]); put(fdp::C_R3W, r[R3W]);
+    put(fdp::C_AUXW, r[AUXW]); put(fdp::C_AUXQZ, r[AUXQZ]);
+  }
+  for (int k = 0; k < NC; ++k) {
+    const T* col = &out[(size_t)k * ld + jb + 1];
+    const size_t n = (size_t)(je - jb);
+    column_hash(col, n, bp[blk * NC + k], bn[blk * NC + k]);
+    U f;
+    std::memcpy(&f, col, sizeof(T));
+    bfirst[blk * NC + k] = f;
+    bconst[blk * NC + k] = same_run(col, n);
+  }
+  }
+  }, 1);
+  const uint64_t prime = 1099511628211ULL;
+  for (int k = 0; k < NC; ++k) {
+    uint64_t p = 1469598103934665603ULL, q = p;
+    bool cst = true;
+    for (size_t blk = 0; blk < nblk; ++blk) {
+      p = (p ^ bp[blk * NC + k]) * prime;
+      q = (q ^ bn[blk * NC + k]) * prime;
+      cst = cst && bconst[blk * NC + k] && bfirst[blk * NC + k] == bfirst[k];
+    }
+    hpos[k] = p;
+    hneg[k] = q;
+    constant[k] = cst;
+  }
+}
+
+// Materials at most this many use table mode when some coefficient varies;
+// a larger table (one material per cell) is expanded into per-cell planes.
+constexpr int kMaxTableMaterials = 4096;
+
 template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate);
 
 // same_bits over many elements, split across the host's cores.
@@ -893,7 +945,9 @@ template <class T> bool same_bits(const T* a, const T* b, size_t n, bool negate)
 // table is large, else the kernels index the table through JM.
 template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum, const T* table24) {
   HostBuf<T> t;
-  derive_table<T>(jmnum, table24, t);
+  bool constant[fdp::C_NCOEF];
+  uint64_t hpos[fdp::C_NCOEF], hneg[fdp::C_NCOEF];
+  derive_table<T>(jmnum, table24, t, constant, hpos, hneg);
   const size_t ld = (size_t)jmnum + 1;
   int rc;
   // AUXIL_W / AUXIL_QZ of JM(I,0) (inh_w_qz_int_1_si.F90:32)
@@ -906,27 +960,9 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
   if ((rc = dev_alloc(c, c->aux, aux.size() * sizeof(T))) != FDP_OK) return rc;
   if ((rc = copy_sync(c, c->aux.p, aux.data(), aux.size() * sizeof(T), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
   // column classification (the AUXIL columns are served by `aux` above):
-  // constant columns, and hashes of every column and of its negation, in
-  // parallel; a hash match is confirmed by comparing every bit
-  bool constant[fdp::C_NCOEF];
-  uint64_t hpos[fdp::C_NCOEF], hneg[fdp::C_NCOEF];
-  {
-    auto classify = [&](int k) {
-      const T* col = &t[(size_t)k * ld + 1];
-      bool cst = true;
-      for (int j = 1; j < jmnum && cst; ++j) cst = same_bits(&col[0], &col[j], 1, false);
-      constant[k] = cst;
-      hpos[k] = hneg[k] = 0;
-      if (!cst) column_hash(col, (size_t)jmnum, hpos[k], hneg[k]);
-    };
-    if (jmnum < 65536) {
-      for (int k = 0; k < fdp::C_NCOEF; ++k) classify(k);
-    } else {
-      std::vector<std::thread> th;
-      for (int k = 0; k < fdp::C_NCOEF; ++k) th.emplace_back(classify, k);
-      for (auto& x : th) x.join();
-    }
-  }
+  // constant columns and the hashes of every column and of its negation
+  // come with the derived table; a hash match is confirmed by comparing
+  // every bit
   // plane assignment: first on the hashes alone, then every column placed
   // on an earlier plane is confirmed bit for bit in one parallel pass; a
   // failed confirmation (a hash collision) redoes the assignment with a
@@ -1012,7 +1048,9 @@ template <class T> int build_medium(fdp_ctx* c, const int32_t* jm, int32_t jmnum
       }
     }, 16);
     if ((rc = copy_sync(c, c->planes.p, pl.data(), pl.size() * sizeof(T), cudaMemcpyHostToDevice)) != FDP_OK) return rc;
+    pl.release_later();
   }
+  t.release_later();
   return FDP_OK;
 }
 
@@ -1340,6 +1378,7 @@ int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host
       }
     }
     }, 64);
+    raw.release_later();
     return FDP_OK;
   };
   return c->prec == 8 ? body(0.0) : body(0.0f);
