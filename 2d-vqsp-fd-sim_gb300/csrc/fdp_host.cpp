@@ -238,20 +238,35 @@ template <class T> int run(const Opts& o) {
     qf.push_back(D + "REC_Q_" + std::to_string(j) + ".asc");
     sf.push_back(D + "REC_STRESS_" + std::to_string(j) + ".asc");
   }
-  for (int it0 = 1; it0 <= MT2;) {
-    // time_loop.F90:79-86: a file STOP in the job directory ends the run
-    // before level it0 (looked for before every chunk of levels); the level
-    // is written into it, list-directed, and the files written so far stay
-    if (exists(D + "STOP")) {
-      if (FILE* sf = std::fopen((D + "STOP").c_str(), "w")) {
-        std::fprintf(sf, "%12d\n", it0);
-        std::fclose(sf);
-      }
-      break;
-    }
+  // time_loop.F90:79-86: a file STOP in the job directory ends the run
+  // before the next level; the level is written into it, list-directed,
+  // and the files of the levels run so far are written.  The reference
+  // looks before every level; here the levels of a chunk run in steps of
+  // kStep (one captured graph each), the host waiting for each step and
+  // looking before the next, so a stop lands at most kStep levels after
+  // the file appears (the wait costs the device about 20 us per step).
+  const int kStep = 32;
+  bool stopped = false;
+  for (int it0 = 1; it0 <= MT2 && !stopped;) {
     int it1 = std::min(MT2, it0 + chunk - 1);
     if (SNV) it1 = std::min(it1, (it0 / IPAS2 + 1) * IPAS2);
-    ck(fdp_run(ctx, it0, it1), "fdp_run");
+    int it = it0;
+    while (it <= it1) {
+      if (exists(D + "STOP")) {
+        if (FILE* stf = std::fopen((D + "STOP").c_str(), "w")) {
+          std::fprintf(stf, "%12d\n", it);
+          std::fclose(stf);
+        }
+        stopped = true;
+        break;
+      }
+      const int e = std::min(it1, it + kStep - 1);
+      ck(fdp_run(ctx, it, e), "fdp_run");
+      ck(fdp_synchronize(ctx), "fdp_synchronize");
+      it = e + 1;
+    }
+    if (it == it0) break;
+    it1 = it - 1;
     const int n = it1 - it0 + 1;
     if (MR > 0 && (TLV || TLP)) {
       ck(fdp_get_receivers(ctx, it0, n, rec.data()), "fdp_get_receivers");
@@ -273,7 +288,7 @@ template <class T> int run(const Opts& o) {
         if (fs) std::fclose(fs);
       }
     }
-    if (SNV && it1 % IPAS2 == 0) {
+    if (SNV && it1 % IPAS2 == 0 && !stopped) {
       char name[32];
       std::snprintf(name, sizeof name, "SNAP.V%06d", it1);
       ck(fdp_get_snapshot(ctx, FDP_SNAP_UM | FDP_SNAP_WM, snap.data()), "fdp_get_snapshot");
