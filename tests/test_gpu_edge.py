@@ -1,8 +1,11 @@
 """The learned absorbing edge on the GPU against its CPU oracle.
 
 * forward pass and gradients of the networks (bf16 operands, FP32
-  accumulation) against oracle/edge_ref.py, within tolerances that cover
-  FP32 accumulation order and one-ulp bf16 rounding flips;
+  accumulation, the back-propagated errors rounded to bf16 as the oracle
+  rounds them) against oracle/edge_ref.py, within tolerances that cover
+  FP32 accumulation order and rare one-ulp bf16 rounding flips (measured:
+  at most 7.4e-4 relative per weight block, 3.5e-4 per bias block over
+  three seeds; a missing term would be of order one);
 * an Adam step against the oracle's Adam on the oracle's gradient;
 * a fresh edge (zero output layer) leaves a run bit-identical;
 * training on a few small media lowers the reflected energy of a held-out
@@ -39,8 +42,8 @@ def test_forward_matches_oracle():
     np.testing.assert_array_equal(e.params(), params)
     y = e.forward(sets, x)
     ref = R.forward(params, sets, x)
-    assert _rel(y, ref) < 2e-3
-    assert np.max(np.abs(y - ref)) < 2e-2 * np.max(np.abs(ref))
+    assert _rel(y, ref) < 3e-4
+    assert np.max(np.abs(y - ref)) < 3e-3 * np.max(np.abs(ref))
 
 
 def test_gradients_match_oracle():
@@ -51,12 +54,12 @@ def test_gradients_match_oracle():
     e.set_params(params)
     g, loss = e.gradients(sets, x, t)
     gr, lr_ = R.gradients(params, sets, x, t)
-    assert abs(loss - lr_) <= 1e-3 * lr_
+    assert abs(loss - lr_) <= 1e-5 * lr_
     for s in range(R.SETS):
         for name, (o, m) in R.OFF.items():
             a = g[s * R.SET_PARAMS + o:s * R.SET_PARAMS + o + m]
             b = gr[s * R.SET_PARAMS + o:s * R.SET_PARAMS + o + m]
-            assert _rel(a, b) < 2e-2, (s, name, _rel(a, b))
+            assert _rel(a, b) < 3e-3, (s, name, _rel(a, b))
 
 
 def test_adam_step_and_descent():
