@@ -262,9 +262,12 @@ int fdp_core_info(fdp_ctx* ctx, int32_t* rect8);
  * launch, warps per CTA.  All zero when the context's levels do not run as
  * march levels (another variant, FP64, a medium not held as Biot planes, a
  * grid too small, a batch's work-queue kernels or an attached learned edge
- * holding it).  No
- * counterpart in the reference (a kernel arrangement of
- * time_loop.F90:93-179). */
+ * holding it).  The launch shape is chosen at fdp_create; environment
+ * variables read then override it, for measurements and tests:
+ * FDP_MARCH_ROWS (4, 6 or 8 rows per band), FDP_MARCH_CTAS (that many
+ * CTAs, the strips' rows split evenly among them) and FDP_MARCH_SMS (plan
+ * for that many SMs).  No counterpart in the reference (a kernel
+ * arrangement of time_loop.F90:93-179). */
 int fdp_march_info(fdp_ctx* ctx, int32_t* region8, int32_t* shape4);
 
 /* Last error message of the context (or of the last failed call that has
