@@ -345,6 +345,7 @@ def run_gpu(args) -> None:
         avg_ms = prof[kern][0] / prof[kern][1]
         phase_gbs = {k: alg[k] / (prof[k][0] / prof[k][1] / 1e3) / 1e9 for k in ("stress", "velocity")}
     achieved = alg[kern] / (avg_ms / 1e3) / 1e9
+    level_bytes = alg["level"] if march else alg["stress"] + alg["velocity"]
     eng.close()
 
     # ---- end to end through the C ABI: one whole shot (create, upload, run, download)
@@ -427,6 +428,10 @@ def run_gpu(args) -> None:
                      "alg_bytes_per_cell": {"stress": alg["per_cell_stress"], "velocity": alg["per_cell_velocity"]},
                      "kernel_ms": {k: prof[k][0] / max(prof[k][1], 1) for k in prof},
                      "phase_gbs": phase_gbs, "phase_frac": {k: v / peak for k, v in phase_gbs.items()},
+                     # the whole level's compulsory bytes over the timed level
+                     # (the timed region's graphs, frame and core side by side)
+                     "level_gbs_timed": level_bytes / (ms_max / args.steps / 1e3) / 1e9,
+                     "level_frac_timed": level_bytes / (ms_max / args.steps / 1e3) / 1e9 / peak,
                      "core_cells": alg.get("core_cells"), "march": march, "march_cells": alg.get("march_cells"),
                      "medium": medium, "phase_share": shares},
         "e2e": e2e,
