@@ -326,11 +326,11 @@ template <class T, bool SI, int MODE> void launch_kind(fdp_ctx* c, const Params<
       fdp::k_velocity_frame<T, SI, MODE><<<c->nframe_v + ((mode & kFrameSamples) ? mr_blocks : 0), blk, 0, fs>>>(
           p, (const int4*)c->frame_v.p, c->nframe_v, it_off);
     if (core) {
-      if (c->core_ev[kind][0]) cudaEventRecordWithFlags(c->core_ev[kind][0], c->stream, cudaEventRecordExternal);
+      if (c->core_ev[kind][0]) cudaEventRecord(c->core_ev[kind][0], c->stream);
       if (launch_core_tma<T, MODE>(c, p, kind)) {}
       else if (kind == 0) fdp::k_stress_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
       else fdp::k_velocity_core<T, MODE><<<core_grid(r), blk, 0, c->stream>>>(p);
-      if (c->core_ev[kind][1]) cudaEventRecordWithFlags(c->core_ev[kind][1], c->stream, cudaEventRecordExternal);
+      if (c->core_ev[kind][1]) cudaEventRecord(c->core_ev[kind][1], c->stream);
       cudaEventRecord(c->join, c->side);
       cudaStreamWaitEvent(c->stream, c->join, 0);
       c->launches += 1;
@@ -636,7 +636,7 @@ void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool firs
   // kernels first 0.0840 ms)
   cudaEventRecord(c->fork, c->stream);
   cudaStreamWaitEvent(c->side, c->fork, 0);
-  if (c->core_ev[0][0]) cudaEventRecordWithFlags(c->core_ev[0][0], c->stream, cudaEventRecordExternal);
+  if (c->core_ev[0][0]) cudaEventRecord(c->core_ev[0][0], c->stream);
   if constexpr (std::is_same<T, float>::value && MODE == fdp::M_BIOT) {
     if (c->march_rows == 8)
       fdp::k_march<MODE, 8><<<c->march_ctas, fdp::MarchShape<8>::kThreads, fdp::MarchShape<8>::kSmem, c->stream>>>(
@@ -652,7 +652,7 @@ void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool firs
       ps, (const int4*)c->mframe_s.p, c->nmframe_s, it_off, defer ? 2 : 0);
   fdp::k_velocity_frame<T, SI, MODE><<<c->nmframe_v, blk, 0, c->side>>>(pv, (const int4*)c->mframe_v.p,
                                                                           c->nmframe_v, it_off);
-  if (c->core_ev[0][1]) cudaEventRecordWithFlags(c->core_ev[0][1], c->stream, cudaEventRecordExternal);
+  if (c->core_ev[0][1]) cudaEventRecord(c->core_ev[0][1], c->stream);
   cudaEventRecord(c->join, c->side);
   cudaStreamWaitEvent(c->stream, c->join, 0);
   c->launches += 3;
@@ -1514,23 +1514,17 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
     const int nedge = edge_threads(c);
     const bool core[2] = {use_march(c) || (c->use_core && !c->fused[0] && c->cs[1] > c->cs[0]),
                           !use_march(c) && c->use_core && !c->fused[1] && c->cv[1] > c->cv[0]};
-    // every level is captured into one graph, launched once, with timing
-    // events as event-record nodes (per level around the two phases and the
-    // edge, and around each phase's core kernel): the kernels run as a
-    // replayed run of levels runs them, and each window holds device time
-    // only
+    // every level is enqueued before the one synchronisation at the end, so
+    // the device never waits for the host and each window holds device time
+    // only: per level, events around the two phases and the edge, and
+    // around each phase's core kernel
     const int n = it_end - it_begin + 1;
     std::vector<cudaEvent_t> ev((size_t)n * 8, nullptr);
     int rc = FDP_OK;
     for (auto& e : ev)
       if (cudaEventCreate(&e) != cudaSuccess) { e = nullptr; rc = fail(c, FDP_ERR_CUDA, "cudaEventCreate failed"); break; }
-    auto rec = [&](cudaEvent_t e) { cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal); };
     if (rc == FDP_OK) {
       fdp::k_set_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, it_begin);
-      cudaError_t ce = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
-      if (ce != cudaSuccess) rc = fail(c, FDP_ERR_CUDA, "profile capture: %s", cudaGetErrorString(ce));
-    }
-    if (rc == FDP_OK) {
       for (int it = it_begin; it <= it_end && use_march(c); ++it) {
         // march levels: entry 0 the whole level (frames beside the march
         // kernel), entry 2 its k_edge, entry 3 the march kernel
@@ -1538,16 +1532,16 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
         cudaEvent_t* e = &ev[(size_t)off * 8];
         c->core_ev[0][0] = e[4];
         c->core_ev[0][1] = e[5];
-        rec(e[0]);
+        cudaEventRecord(e[0], c->stream);
         launch_level_any<T>(c, p, off, true, false);
-        rec(e[1]);
-        rec(e[2]);
+        cudaEventRecord(e[1], c->stream);
+        cudaEventRecord(e[2], c->stream);
         if (nedge > 0) {
           Params<T> pe = p;
           set_fields(c, pe, c->fields, c->fields);
           launch<T>(c, pe, 2, off);
         }
-        rec(e[3]);
+        cudaEventRecord(e[3], c->stream);
       }
       for (int it = it_begin; it <= it_end && !use_march(c); ++it) {
         const int off = it - it_begin;
@@ -1556,27 +1550,20 @@ int fdp_profile_run(fdp_ctx* c, int32_t it_begin, int32_t it_end, double* ms_out
           c->core_ev[k][0] = core[k] ? e[4 + 2 * k] : nullptr;
           c->core_ev[k][1] = core[k] ? e[5 + 2 * k] : nullptr;
         }
-        rec(e[0]);
+        cudaEventRecord(e[0], c->stream);
         launch<T>(c, p, 0, off);
-        rec(e[1]);
+        cudaEventRecord(e[1], c->stream);
         launch<T>(c, p, 1, off);
-        rec(e[2]);
+        cudaEventRecord(e[2], c->stream);
         if (nedge > 0) launch<T>(c, p, 2, off);
         c->launches += fdp::edge_launch(c, off);
-        rec(e[3]);
+        cudaEventRecord(e[3], c->stream);
       }
       fdp::k_add_base<<<1, 1, 0, c->stream>>>((int*)c->itbase.p, n);
       c->launches += 2;
       for (auto& pair : c->core_ev) pair[0] = pair[1] = nullptr;
-      cudaGraph_t gr = nullptr;
-      cudaGraphExec_t gx = nullptr;
-      cudaError_t err = cudaStreamEndCapture(c->stream, &gr);
-      if (err == cudaSuccess) err = cudaGraphInstantiate(&gx, gr, 0);
-      if (err == cudaSuccess) err = cudaGraphLaunch(gx, c->stream);
-      if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
+      cudaError_t err = cudaStreamSynchronize(c->stream);
       if (err == cudaSuccess) err = cudaGetLastError();
-      if (gx) cudaGraphExecDestroy(gx);
-      if (gr) cudaGraphDestroy(gr);
       if (err != cudaSuccess) rc = fail(c, FDP_ERR_CUDA, "profile run: %s", cudaGetErrorString(err));
       for (int off = 0; off < n && rc == FDP_OK; ++off) {
         const cudaEvent_t* e = &ev[(size_t)off * 8];

@@ -217,17 +217,16 @@ int fdp_synchronize(fdp_ctx* ctx);
  * work, or record its own events, after the engine's. */
 int fdp_get_stream(fdp_ctx* ctx, void** stream);
 
-/* Diagnostics: advances levels it_begin..it_end like fdp_run, each level
- * finished by its own row-1/receiver launch, captured into one CUDA graph
- * with timing events as event-record nodes around each part of a level
- * (so the windows hold device time as a replayed run spends it), and
- * returns the summed device time in milliseconds in ms_out[0..4] and the
- * number of timed launches in launches_out[0..4]: {stress phase, velocity
- * phase, row 1 and receivers (and an attached learned edge), stress core
- * kernel, velocity core kernel}.  A phase is its frame and core kernels
- * together (one kernel with FDP_KERNEL_VARIANT=global or tma, when the core
- * entries stay 0).  With march levels entry 0 is the whole level, entry 1
- * stays 0 and entry 3 is the march kernel. */
+/* Diagnostics: advances levels it_begin..it_end like fdp_run but without
+ * graphs, with CUDA events around each part of a level (all levels are
+ * enqueued before one wait, so the windows hold device time, not host
+ * launch latency), and returns
+ * the summed device time in milliseconds in ms_out[0..4] and the number of
+ * timed launches in launches_out[0..4]: {stress phase, velocity phase,
+ * row 1 and receivers (and an attached learned edge), stress core kernel,
+ * velocity core kernel}.  A phase is its frame and core kernels together
+ * (one kernel with FDP_KERNEL_VARIANT=global or tma, when the core entries
+ * stay 0). */
 int fdp_profile_run(fdp_ctx* ctx, int32_t it_begin, int32_t it_end, double* ms_out, int64_t* launches_out);
 
 /* Number of CUDA kernel launches this context has enqueued since creation
