@@ -1,13 +1,16 @@
-"""Every reference citation in the tracked sources resolves.
+"""Every reference citation in the project's files resolves.
 
 The oracle's fidelity, and the parity claims of the kernels, rest on
 file:line citations of the reference's Fortran (``name.F90:N``,
 ``name.F90:N-M``, ``name.F90:N,M-K``).  This test reads the reference's
-source tree (``FDP_REFERENCE_DIR``, default the reference checkout next to
-this build) and checks that each cited file exists, each cited range lies
-inside it and holds at least one statement (not only blank or comment
-lines), and that a set of anchor citations on the hot path holds the
-statement it names.  Skipped where the reference's sources are absent.
+source tree (``FDP_REFERENCE_DIR``, default the reference checkout) and
+checks that each cited file exists, each cited range lies inside it and
+holds at least one statement (not only blank or comment lines), and that a
+set of anchor citations on the hot path holds the statement it names.
+The project's files are every tracked file in a subdirectory, the Python
+files at the top, and the top-level documents whose title names the GB300
+engine (records kept beside them, such as measurement logs, are not
+sources).  Skipped where the reference's sources are absent.
 """
 import os
 import re
@@ -19,8 +22,6 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 REF = Path(os.environ.get("FDP_REFERENCE_DIR", "/root/reference"))
 
-# records written by the build's reviewers and its driver, not sources
-SKIP = re.compile(r"^(VERDICT|ADVICE|SURVEY|BASELINE|GPUTEST|BENCH|SCALE|MULTICHIP|PROGRESS)")
 CITE = re.compile(r"\b([A-Za-z_][A-Za-z0-9_]*\.(?:F90|F)):(\d+(?:-\d+)?(?:,\d+(?:-\d+)?)*)")
 
 # citations of code the reference keeps commented out, on purpose
@@ -50,9 +51,18 @@ ANCHORS = {
 }
 
 
+def _project_file(t: str) -> bool:
+    if "/" in t or t.endswith(".py"):
+        return True
+    if not t.endswith(".md"):
+        return False
+    with open(ROOT / t, errors="replace") as f:
+        return "GB300" in f.readline()
+
+
 def _tracked():
     out = subprocess.run(["git", "ls-files"], cwd=ROOT, capture_output=True, text=True).stdout.split()
-    return [ROOT / t for t in out if not SKIP.match(t)]
+    return [ROOT / t for t in out if _project_file(t)]
 
 
 def _ranges(spec):
