@@ -420,16 +420,28 @@ bool plan_march(fdp_ctx* c) {
   m.nvec = nvec;
   m.nstrips = (nvec + fdp::kMarchVec - 1) / fdp::kMarchVec;
   m.total = (long long)m.nstrips * (fz1 - fz0);
+  c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
+  c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
+  return true;
+}
+
+// The march launch for the context's medium, once it is set: whether its
+// levels run as march levels, the band height and the CTAs.
+template <int MODE> bool march_shape_for(fdp_ctx* c) {
+  fdp::MarchGrid& m = c->mg;
   int sms = 152, l2 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->g.device);
   if (const char* es = std::getenv("FDP_MARCH_SMS")) sms = std::max(1, std::min(sms, std::atoi(es)));  // plan for fewer SMs
   cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->g.device);
   // Unless named, march levels run only where a level's data outgrow L2:
   // below that the split's second phase finds the first phase's output in
-  // L2.  Measured on layered grids: 1280^2 (166 MB per level in the march
-  // kernel, L2 129 MB) split 0.0379 ms, march 0.0410; 1408^2 (204 MB) 0.0476
-  // and 0.0472; 2048^2 0.0967 and 0.0833.
-  const double level_bytes = (double)nvec * 4 * (fz1 - fz0) * 104.0;
+  // L2.  Measured on layered grids with Biot planes (104 B per cell of F):
+  // 1280^2 (166 MB per level in the march kernel, L2 129 MB) split 0.0379
+  // ms, march 0.0410; 1408^2 (204 MB) 0.0476 and 0.0472; 2048^2 0.0967 and
+  // 0.0833.  Other media: the 16 field values and a material index (table)
+  // or the distinct coefficient planes (planes mode) per cell.
+  const double per_cell = 64.0 + (MODE == fdp::M_BIOT ? 40.0 : MODE == fdp::M_TABLE ? 4.0 : 4.0 * c->nplanes);
+  const double level_bytes = (double)m.nvec * 4 * (m.fz1 - m.fz0) * per_cell;
   if (!c->march_forced && level_bytes < 1.5 * l2) return false;
   // the same number of CTAs on every strip, each a contiguous range of the
   // strip's rows (or, with more strips than CTA slots, the same number of
@@ -440,7 +452,7 @@ bool plan_march(fdp_ctx* c) {
   // (six per strip) 0.145 ms.  aligned(slots) = the CTAs and the range of
   // each (0: the strips' rows split evenly), and the share of the slots'
   // time they fill.
-  const int H = fz1 - fz0;
+  const int H = m.fz1 - m.fz0;
   struct Split { long long ctas, span; double fill; };
   auto aligned = [&](long long slots) -> Split {
     if (m.nstrips <= slots) {
@@ -450,16 +462,23 @@ bool plan_march(fdp_ctx* c) {
     const long long q = (m.nstrips + slots - 1) / slots;  // strips per CTA
     return {(m.nstrips + q - 1) / q, q * H, (double)m.nstrips / ((double)q * slots)};
   };
+  using S4 = fdp::MarchShapeOf<MODE, 4>;
+  using S6 = fdp::MarchShapeOf<MODE, 6>;
+  using S8 = fdp::MarchShapeOf<MODE, 8>;
   // bands of 8 rows (one CTA of eight warps per SM) or of 4 (two CTAs of
-  // four warps per SM), whichever leaves fewer SM slots idle (8 on a tie);
-  // 6 (six warps) on request.  2048^2 (17 strips): 136 CTAs of 8 rows
-  // 0.0853 ms, 289 of 4 rows 0.0833; 4096^2 (34 strips): 136 CTAs of 8
-  // rows 0.2900 ms, 272 of 4 rows 0.2955.
+  // four warps per SM with the Biot planes staged, three without),
+  // whichever keeps more warps busy: warps per SM times the share of the
+  // slots the strips fill (8 on a near tie); 6 (six warps) on request.
+  // Biot planes: 2048^2 (17 strips) 136 CTAs of 8 rows 0.0853 ms per level,
+  // 289 of 4 rows 0.0833; 4096^2 (34 strips) 136 CTAs of 8 rows 0.2900 ms,
+  // 272 of 4 rows 0.2955.
   const char* er = std::getenv("FDP_MARCH_ROWS");
   const int rows = er ? std::atoi(er) : 0;
   if (rows == 4 || rows == 6 || rows == 8) c->march_rows = rows;
   else {
-    c->march_rows = aligned(2LL * sms).fill > aligned(sms).fill + 0.02 ? 4 : 8;
+    const double w4 = 4.0 * S4::kCtasPerSm * aligned((long long)sms * S4::kCtasPerSm).fill;
+    const double w8 = 8.0 * S8::kCtasPerSm * aligned((long long)sms * S8::kCtasPerSm).fill;
+    c->march_rows = w4 > 1.02 * w8 ? 4 : 8;
   }
   int per_sm = 1;
   cudaError_t e = cudaSuccess;
@@ -467,17 +486,23 @@ bool plan_march(fdp_ctx* c) {
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     per_sm = ctas_per_sm;
   };
-  if (c->march_rows == 4) shape(fdp::k_march<fdp::M_BIOT, 4>, fdp::MarchShape<4>::kSmem, fdp::MarchShape<4>::kCtasPerSm);
-  else if (c->march_rows == 6) shape(fdp::k_march<fdp::M_BIOT, 6>, fdp::MarchShape<6>::kSmem, fdp::MarchShape<6>::kCtasPerSm);
-  else shape(fdp::k_march<fdp::M_BIOT, 8>, fdp::MarchShape<8>::kSmem, fdp::MarchShape<8>::kCtasPerSm);
+  if (c->march_rows == 4) shape(fdp::k_march<MODE, 4>, S4::kSmem, S4::kCtasPerSm);
+  else if (c->march_rows == 6) shape(fdp::k_march<MODE, 6>, S6::kSmem, S6::kCtasPerSm);
+  else shape(fdp::k_march<MODE, 8>, S8::kSmem, S8::kCtasPerSm);
   if (e != cudaSuccess) return false;
   const Split sp = aligned((long long)sms * per_sm);
   const char* ec = std::getenv("FDP_MARCH_CTAS");
   m.span = ec ? 0 : sp.span;
   c->march_ctas = (int)std::min<long long>(ec ? std::max(1, std::atoi(ec)) : sp.ctas, m.total);
-  c->ms[0] = m.sx0; c->ms[1] = m.sx1; c->ms[2] = m.sz0; c->ms[3] = m.sz1;
-  c->mv[0] = fx0; c->mv[1] = fx1; c->mv[2] = fz0; c->mv[3] = fz1;
   return true;
+}
+
+bool march_shape(fdp_ctx* c) {
+  switch (c->medium_mode) {
+    case fdp::M_BIOT: return march_shape_for<fdp::M_BIOT>(c);
+    case fdp::M_TABLE: return march_shape_for<fdp::M_TABLE>(c);
+    default: return march_shape_for<fdp::M_PLANES>(c);
+  }
 }
 
 // The second buffer of each wavefield array, made as a copy of the first
@@ -503,13 +528,17 @@ bool alloc_alt(fdp_ctx* c) {
   return true;
 }
 
-// The march kernel's tensor maps for each of the two buffers of the fields
-// (indexed like cur); the march levels run only once the medium is held as
-// Biot planes (a medium of another kind leaves the context on the
-// frame/core split).
+// The march launch and the march kernel's tensor maps for each of the two
+// buffers of the fields (indexed like cur) and, for a medium held as Biot
+// planes, of the planes; the march levels run once the medium is set and
+// its launch chosen (a grid whose levels stay in L2, or a device without
+// room for the second buffers, leaves the context on the frame/core split).
 int make_march_maps(fdp_ctx* c) {
   c->march_ready = false;
-  if (!c->march || c->medium_mode != fdp::M_BIOT || !c->planes.p) return FDP_OK;
+  if (!c->march) return FDP_OK;
+  const bool biot = c->medium_mode == fdp::M_BIOT;
+  if (biot && !c->planes.p) return FDP_OK;
+  if (!march_shape(c)) return FDP_OK;
   if (!alloc_alt(c)) return FDP_OK;
   const size_t pstride = (size_t)c->rows_alloc * c->pitch;
   int rc;
@@ -518,7 +547,7 @@ int make_march_maps(fdp_ctx* c) {
     fdp::MarchMaps& m = c->mmaps[b];
     for (int k = 0; k < 8; ++k)
       if ((rc = make_field_map(c, &m.f[k], f[k].p, fdp::kMarchW, c->march_rows)) != FDP_OK) return rc;
-    for (int k = 0; k < 10; ++k)
+    for (int k = 0; k < 10 && biot; ++k)
       if ((rc = make_field_map(c, &m.pl[k], (float*)c->planes.p + (size_t)k * pstride, fdp::kMarchW,
                                c->march_rows)) != FDP_OK)
         return rc;
@@ -637,16 +666,19 @@ void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool firs
   cudaEventRecord(c->fork, c->stream);
   cudaStreamWaitEvent(c->side, c->fork, 0);
   if (c->core_ev[0][0]) cudaEventRecord(c->core_ev[0][0], c->stream);
-  if constexpr (std::is_same<T, float>::value && MODE == fdp::M_BIOT) {
+  if constexpr (std::is_same<T, float>::value) {
+    using S4 = fdp::MarchShapeOf<MODE, 4>;
+    using S6 = fdp::MarchShapeOf<MODE, 6>;
+    using S8 = fdp::MarchShapeOf<MODE, 8>;
     if (c->march_rows == 8)
-      fdp::k_march<MODE, 8><<<c->march_ctas, fdp::MarchShape<8>::kThreads, fdp::MarchShape<8>::kSmem, c->stream>>>(
-          pm, c->mmaps[c->cur], c->mg, it_off);
+      fdp::k_march<MODE, 8><<<c->march_ctas, S8::kThreads, S8::kSmem, c->stream>>>(pm, c->mmaps[c->cur], c->mg,
+                                                                                    it_off);
     else if (c->march_rows == 6)
-      fdp::k_march<MODE, 6><<<c->march_ctas, fdp::MarchShape<6>::kThreads, fdp::MarchShape<6>::kSmem, c->stream>>>(
-          pm, c->mmaps[c->cur], c->mg, it_off);
+      fdp::k_march<MODE, 6><<<c->march_ctas, S6::kThreads, S6::kSmem, c->stream>>>(pm, c->mmaps[c->cur], c->mg,
+                                                                                    it_off);
     else
-      fdp::k_march<MODE, 4><<<c->march_ctas, fdp::MarchShape<4>::kThreads, fdp::MarchShape<4>::kSmem, c->stream>>>(
-          pm, c->mmaps[c->cur], c->mg, it_off);
+      fdp::k_march<MODE, 4><<<c->march_ctas, S4::kThreads, S4::kSmem, c->stream>>>(pm, c->mmaps[c->cur], c->mg,
+                                                                                    it_off);
   }
   fdp::k_stress_frame<T, SI, MODE><<<c->nmframe_s + (defer ? mr_blocks : 0), blk, 0, c->side>>>(
       ps, (const int4*)c->mframe_s.p, c->nmframe_s, it_off, defer ? 2 : 0);
@@ -668,9 +700,21 @@ void launch_level_march(fdp_ctx* c, const Params<T>& base, int it_off, bool firs
 // Level it_off of a run of levels; `first` and `last` mark the run's ends.
 template <class T> int launch_level_any(fdp_ctx* c, const Params<T>& p, int it_off, bool first, bool last) {
   if (use_march(c)) {
-    // the march levels run FP32 contexts with a Biot-plane medium only
-    if (c->g.stress_imaging) launch_level_march<T, true, fdp::M_BIOT>(c, p, it_off, first, last);
-    else launch_level_march<T, false, fdp::M_BIOT>(c, p, it_off, first, last);
+    // the march levels run FP32 contexts only
+    const bool si = c->g.stress_imaging != 0;
+    switch (c->medium_mode) {
+      case fdp::M_BIOT:
+        if (si) launch_level_march<T, true, fdp::M_BIOT>(c, p, it_off, first, last);
+        else launch_level_march<T, false, fdp::M_BIOT>(c, p, it_off, first, last);
+        break;
+      case fdp::M_TABLE:
+        if (si) launch_level_march<T, true, fdp::M_TABLE>(c, p, it_off, first, last);
+        else launch_level_march<T, false, fdp::M_TABLE>(c, p, it_off, first, last);
+        break;
+      default:
+        if (si) launch_level_march<T, true, fdp::M_PLANES>(c, p, it_off, first, last);
+        else launch_level_march<T, false, fdp::M_PLANES>(c, p, it_off, first, last);
+    }
     return FDP_OK;
   }
   const bool defer = defer_edge(c);

@@ -44,8 +44,11 @@
 // sequence (one CTA per SM, two with bands of four rows): the same number
 // of CTAs on every strip, or, with more strips than CTAs, whole strips per
 // CTA, so that the CTAs march down the same rows together.  A CTA whose
-// range crosses into the next strip starts again there.  FP32 with the ten
-// planes of a Biot medium.
+// range crosses into the next strip starts again there.  FP32; a medium
+// held as the ten Biot planes has them staged with the stresses, any other
+// reaches its coefficients through the kernels' lookup (a material index
+// read per cell into a cached table, or constants folded into the
+// parameters).
 #pragma once
 
 #include "fdp_core_tma.cuh"
@@ -55,24 +58,31 @@ namespace fdp {
 constexpr int kMarchVec = 30;  // vectors a strip updates (lanes 1..30)
 constexpr int kMarchW = 128;   // box width: the strip's 32 vectors
 
-constexpr int kMarchDirect = 14;  // boxes of a stage: stresses (4), stress planes (5), velocity planes (5)
+// Boxes of a stage: the old stresses (4) and, for a medium held as the ten
+// Biot planes, the five stress planes and the five velocity planes; other
+// media reach their coefficients through the kernels' coefficient lookup
+// (a material index into a cached table, or constants).
+__host__ __device__ constexpr int march_boxes(int mode) { return mode == M_BIOT ? 14 : 4; }
 
-// Sizes of a CTA of R warps marching bands of R rows (R = 4, 6 or 8).  A
-// step reads 3R+4 rows of the velocity ring while the next band's R rows
-// arrive, and 2R+4 rows of the stress ring (R written, R+4 read).
-template <int R> struct MarchShape {
+// Sizes of a CTA of R warps marching bands of R rows (R = 4, 6 or 8) with
+// stages of NB boxes.  A step reads 3R+4 rows of the velocity ring while
+// the next band's R rows arrive, and 2R+4 rows of the stress ring (R
+// written, R+4 read).
+template <int R, int NB> struct MarchShape {
   static constexpr int kThreads = 32 * R;
   static constexpr int kVRows = 4 * R;      // velocity ring rows (slots of R)
   static constexpr int kSRows = 2 * R + 4;  // stress ring rows
   static constexpr int kBox = R * kMarchW;  // floats per box
   static constexpr int kVRing = 4 * kVRows * kMarchW;
-  static constexpr int kStage = kMarchDirect * kBox;
+  static constexpr int kStage = NB * kBox;
   static constexpr int kSRing = 4 * kSRows * kMarchW;
   static constexpr size_t kSmem = (size_t)(kVRing + 2 * kStage + kSRing) * sizeof(float) + 128;
-  static constexpr int kCtasPerSm = kSmem <= 113 * 1024 ? 2 : 1;
+  // CTAs of this shape that fit an SM's 228 KB (1 KB reserved per CTA)
+  static constexpr int kCtasPerSm = kSmem <= 74 * 1024 ? 3 : kSmem <= 113 * 1024 ? 2 : 1;
   static_assert(kSmem <= 227 * 1024, "march stages exceed the shared memory of a CTA");
   static_assert(R >= 4, "a band's stencils reach four rows back");
 };
+template <int MODE, int R> using MarchShapeOf = MarchShape<R, march_boxes(MODE)>;
 
 // Tensor maps (boxes of 128 columns by R rows): the eight wavefield arrays
 // a level reads (UM WM QX QZ TXX TZZ TXZ PRES) and the ten Biot planes.
@@ -115,10 +125,11 @@ __device__ __forceinline__ void sts4s(float* s, const V4<float>& v) {
 }
 
 template <int MODE, int R>
-__global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasPerSm)
+__global__ void __launch_bounds__(MarchShapeOf<MODE, R>::kThreads, MarchShapeOf<MODE, R>::kCtasPerSm)
     k_march(const __grid_constant__ Params<float> p, const __grid_constant__ MarchMaps maps, const MarchGrid g,
             int it_off) {
-  using Sh = MarchShape<R>;
+  using Sh = MarchShapeOf<MODE, R>;
+  constexpr bool kPlanes = MODE == M_BIOT;  // coefficient planes staged with the stresses
   extern __shared__ unsigned char march_raw[];
   float* const vring = reinterpret_cast<float*>(((uintptr_t)march_raw + 127) & ~(uintptr_t)127);
   float* const stages = vring + Sh::kVRing;
@@ -166,7 +177,8 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
     const int x = g.fx0 + 4 * kMarchVec * b.strip - 4 - p.PMLL + kPadX;  // padded column of the box
     const int r = b.vlo - 2 + R * b.k;                                      // band k's first stress row
     const bool s_ = b.k < nbands(b), v_ = b.k >= 1;
-    mbar_expect_tx(bar, (uint32_t)(((s_ ? (b.k == 0 ? 17 : 13) : 0) + (v_ ? 5 : 0)) * Sh::kBox * sizeof(float)));
+    const int boxes = (s_ ? (b.k == 0 ? 12 : 8) + (kPlanes ? 5 : 0) : 0) + (v_ && kPlanes ? 5 : 0);
+    mbar_expect_tx(bar, (uint32_t)(boxes * Sh::kBox * sizeof(float)));
     if (s_) {
       const int slot = ((j + 1) & 3) * R, pro = (j & 3) * R;
 #pragma unroll
@@ -177,10 +189,12 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
       }
 #pragma unroll
       for (int f = 0; f < 4; ++f) tma_load_2d(st + f * Sh::kBox, &maps.f[4 + f], x, r + kPadZ, bar);
+      if constexpr (kPlanes) {
 #pragma unroll
-      for (int s = 0; s < 5; ++s) tma_load_2d(st + (4 + s) * Sh::kBox, &maps.pl[s], x, r + kPadZ, bar);
+        for (int s = 0; s < 5; ++s) tma_load_2d(st + (4 + s) * Sh::kBox, &maps.pl[s], x, r + kPadZ, bar);
+      }
     }
-    if (v_) {
+    if (v_ && kPlanes) {
       // band k-1's velocity rows [r-R-2, r-2)
 #pragma unroll
       for (int s = 0; s < 5; ++s) tma_load_2d(st + (9 + s) * Sh::kBox, &maps.pl[5 + s], x, r - R - 2 + kPadZ, bar);
@@ -256,9 +270,11 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
     if (!mbar_wait_bounded(&full[j & 1], (uint32_t)((j >> 1) & 1))) failed = 1;
     if (vel) {
       V4<float> bio[5];
-      const float* prow = S + 9 * Sh::kBox + warp * kMarchW + 4 * lane;
+      if constexpr (kPlanes) {
+        const float* prow = S + 9 * Sh::kBox + warp * kMarchW + 4 * lane;
 #pragma unroll
-      for (int s = 0; s < 5; ++s) bio[s] = lds4s(prow + s * Sh::kBox);
+        for (int s = 0; s < 5; ++s) bio[s] = lds4s(prow + s * Sh::kBox);
+      }
       const long long c0 = (long long)Lv * P + (I0 - p.PMLL);
       velocity_core_math<float, MODE>(p, c0, va, bio, oqx, oum, oqz, owm);
       st4(p.oQX + c0, oqx);
@@ -287,8 +303,10 @@ __global__ void __launch_bounds__(MarchShape<R>::kThreads, MarchShape<R>::kCtasP
       V4<float> oxx = lds4s(srow0), ozz = lds4s(srow0 + Sh::kBox), oxz = lds4s(srow0 + 2 * Sh::kBox),
                 opr = lds4s(srow0 + 3 * Sh::kBox);
       V4<float> bio[5];
+      if constexpr (kPlanes) {
 #pragma unroll
-      for (int s = 0; s < 5; ++s) bio[s] = lds4s(srow0 + (4 + s) * Sh::kBox);
+        for (int s = 0; s < 5; ++s) bio[s] = lds4s(srow0 + (4 + s) * Sh::kBox);
+      }
       const long long c0 = (long long)Ls * P + (I0 - p.PMLL);
       const int src_j = (Ls == p.LIN_Z && p.LIN_X >= I0 && p.LIN_X < I0 + 4) ? p.LIN_X - I0 : -1;
       stress_core_math<float, MODE>(p, c0, a, bio, oxz, oxx, ozz, opr, src_j, srcS, srcF);

@@ -1,16 +1,18 @@
 """The march variant against the oracle.
 
-By default (or with FDP_KERNEL_VARIANT=march), an FP32 context whose
-medium is held as the ten Biot planes runs each level's deep interior as one kernel pass (the
-stress phase, then the velocity phase, from bands of rows staged in shared
-memory by bulk tensor copies), beside the frame kernels on the side stream,
-and the levels alternate between two buffers of each wavefield array.
-Every field, PML memory variable, the bottom history and every receiver
-value must equal the oracle's bit for bit: from random states and from
-rest, both free-surface modes, grids whose width leaves a partial strip,
-sources inside the march region, runs of odd length (which end in the
-other buffers), any split of the rows among the CTAs, and the full 2048^2
-layered grid.
+By default on grids whose levels outgrow 1.5x L2 (or with
+FDP_KERNEL_VARIANT=march on any grid large enough), an FP32 context runs
+each level's deep interior as one kernel pass (the stress phase, then the
+velocity phase, from bands of rows staged in shared memory by bulk tensor
+copies), beside the frame kernels on the side stream, and the levels
+alternate between two buffers of each wavefield array.  Every field, PML
+memory variable, the bottom history and every receiver value must equal
+the oracle's bit for bit: from random states and from rest, both
+free-surface modes, grids whose width leaves a partial strip, sources
+inside the march region, runs of odd length (which end in the other
+buffers), any split of the rows among the CTAs, every medium
+representation (Biot planes, material table, generic planes, constants)
+and the full 2048^2 layered grid.
 """
 import os
 
@@ -159,13 +161,50 @@ def test_default_on_a_large_grid(monkeypatch):
     assert info["band_rows"] in (4, 8)
 
 
-def test_fp64_and_table_media_keep_the_split():
+def test_fp64_keeps_the_split():
     cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=10, per_cell=True, seed=5)
     _, e64, _ = _pair(cfg, med, "f64")
     assert e64.march_info() is None
-    cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=10, per_cell=False, seed=5)
-    _, etab, _ = _pair(cfg, med)
-    assert etab.march_info() is None
+
+
+def _planes_medium(med):
+    """The medium with an anisotropic perturbation: SIG_ZZ_1 no longer
+    equals SIG_XX_2, so the engine holds it as generic coefficient planes
+    rather than the ten Biot planes."""
+    from fdporo import media
+    t = np.array(med.table, copy=True)
+    t[:, media.COL["SIG_ZZ_1"]] *= 1.0 + 0.05 * np.linspace(0.0, 1.0, t.shape[0])
+    return media.Medium(med.jm_rows, t)
+
+
+@pytest.mark.parametrize("kind", ["table", "planes", "homogeneous"])
+@pytest.mark.parametrize("rows", [4, 8])
+@pytest.mark.parametrize("si", [True, False])
+def test_other_media(kind, rows, si, monkeypatch):
+    """March levels for a medium held as a material table (a material index
+    per cell), as generic coefficient planes, and as constants (one
+    material): the coefficients come through the kernels' lookup instead of
+    staged planes.  Random states and a source inside the march region,
+    against the oracle bit for bit."""
+    from fdporo import job, media
+    monkeypatch.setenv("FDP_MARCH_ROWS", str(rows))
+    cfg, med = small_job(mx=251, mz=90, tpml=6, nsteps=17, si=si, per_cell=(kind == "planes"), seed=80 + rows,
+                         n_rec=7)
+    if kind == "planes":
+        med = _planes_medium(med)
+    elif kind == "homogeneous":
+        med = media.Medium(np.ones_like(np.asarray(med.jm_rows)), np.asarray(med.table)[:1])
+    inp, eng, orc = _pair(cfg, med)
+    want = {"table": "table", "planes": "planes", "homogeneous": "planes"}[kind]
+    assert eng.medium_info()["mode"] == want
+    info = eng.march_info()
+    assert info is not None and info["band_rows"] == rows
+    randomize_state([eng, orc], inp, seed=81)
+    for a, b in ((1, 5), (6, 17)):
+        eng.time_loop(a, b)
+        orc.time_loop(a, b)
+    compare_state(eng, orc)
+    np.testing.assert_array_equal(eng.receivers(1, 17), orc.receivers(1, 17))
 
 
 def test_layered_2048_full_grid():

@@ -123,17 +123,20 @@ def test_kernel_launch_count(kernel_variant):
     level-counter reset.  The frame/core split (also with TMA-staged cores)
     launches a frame and a core kernel per phase and level, with the row-1
     and receiver step folded into the next level's stress frame kernel and
-    one k_edge for the last level of each run; the other variants one kernel
-    per phase and a k_edge per level."""
+    one k_edge for the last level of each run (march levels: the march kernel
+    and the two frame kernels per level); the other variants one kernel per
+    phase and a k_edge per level."""
     cfg, med = small_job(mx=72, mz=56, tpml=6, nsteps=70, seed=31)
     inp, eng, _ = _pair(cfg, med, "f32")
     n0 = eng.kernel_launches()
     eng.time_loop(1, 70)
     eng.synchronize()
     runs = 3
-    if kernel_variant in ("split", "coretma", "march"):
-        # (a table medium: the march variant leaves it to the split)
-        assert eng.march_info() is None
+    if kernel_variant == "march":
+        # per level the march kernel and the two frame kernels
+        assert eng.march_info() is not None
+        expected = 70 * 3 + runs * 2 + 1
+    elif kernel_variant in ("split", "coretma"):
         core = eng.core_info()
         assert all(x1 > x0 and z1 > z0 for x0, x1, z0, z1 in core.values())
         expected = 70 * 4 + runs * 2 + 1
