@@ -101,10 +101,9 @@ enum fdp_field_id {
  * PPML and ALLOC_NR do (tl_alloc.F90:44-56, ppml.F90:115-153,
  * alloc_nr.F90:42-54).  Replaces the allocations of TL_ALLOC/PPML/ALLOC_NR.
  * The environment variable FDP_KERNEL_VARIANT, read here, selects the
- * kernels, all bit-identical.  Unset: FP32 contexts whose medium is held
- * as Biot planes and whose levels outgrow one and a half times the L2 cache
- * run both phases of each level's deep interior in one pass
- * (fdp_march_info), every other context the split; "march" runs them so
+ * kernels, all bit-identical.  Unset: FP32 contexts whose levels outgrow
+ * one and a half times the L2 cache run both phases of each level's deep
+ * interior in one pass (fdp_march_info), every other context the split; "march" runs them so
  * on any grid large enough for the pass.
  * "split": the interior ("core") of each phase runs vectorised beside a
  * frame kernel for the PML, free-surface, source and bottom cells on a
@@ -250,7 +249,7 @@ int fdp_medium_info(fdp_ctx* ctx, int32_t* mode, int32_t* planes_stress, int32_t
  * the velocity core; zeros when the context runs other kernels. */
 int fdp_core_info(fdp_ctx* ctx, int32_t* rect8);
 
-/* The march levels (by default for FP32 Biot media on grids whose levels
+/* The march levels (by default for FP32 contexts on grids whose levels
  * outgrow one and a half times the L2 cache): each level's deep
  * interior in one kernel pass (stress phase, then velocity phase, from
  * bands of rows staged in shared memory by bulk tensor copies), the levels
@@ -260,9 +259,9 @@ int fdp_core_info(fdp_ctx* ctx, int32_t* rect8);
  * stresses (the frame kernels write a band along the edges); shape4 =
  * strips of 30 four-cell vectors across, rows per band, CTAs of the
  * launch, warps per CTA.  All zero when the context's levels do not run as
- * march levels (another variant, FP64, a medium not held as Biot planes, a
- * grid too small, a batch's work-queue kernels or an attached learned edge
- * holding it).  The launch shape is chosen at fdp_create; environment
+ * march levels (another variant, FP64, a grid too small, a batch's
+ * work-queue kernels or an attached learned edge holding it).  The launch
+ * shape is chosen when the medium is set; environment
  * variables read then override it, for measurements and tests:
  * FDP_MARCH_ROWS (4, 6 or 8 rows per band), FDP_MARCH_CTAS (that many
  * CTAs, the strips' rows split evenly among them) and FDP_MARCH_SMS (plan
