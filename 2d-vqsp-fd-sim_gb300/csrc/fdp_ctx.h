@@ -82,7 +82,7 @@ struct fdp_ctx {
   // set while jm, coef, planes and aux belong to a share with other
   // contexts (the share frees them, not this context)
   std::shared_ptr<MediumShare> medium_share;
-  // march levels (the default for FP32 Biot media whose levels outgrow L2;
+  // march levels (the default for FP32 contexts whose levels outgrow L2;
   // FDP_KERNEL_VARIANT=march forces them): each level's interior in one
   // pass, the levels alternating between the two buffers of each wavefield
   // array.  fields[] always holds the current level's buffers and alt[] the
@@ -98,7 +98,7 @@ struct fdp_ctx {
   DevArr mframe_s, mframe_v;
   int nmframe_s = 0, nmframe_v = 0;
   // tensor maps of the march kernel, per current buffer; ready once the
-  // medium is held as Biot planes
+  // medium is set and its launch chosen
   fdp::MarchMaps mmaps[2]{};
   bool march_ready = false;
   // set while a batch holds the context (its kernels update in place);

@@ -130,7 +130,7 @@ def test_launch_count():
 
 @pytest.mark.parametrize("variant,march", [(None, False), ("", False), ("split", False), ("march", True)])
 def test_variant_choice_on_a_small_grid(variant, march, monkeypatch):
-    """Without FDP_KERNEL_VARIANT an FP32 Biot context runs march levels only
+    """Without FDP_KERNEL_VARIANT an FP32 context runs march levels only
     where its levels outgrow one and a half times L2 (the 2048^2 parity
     test of test_gpu_configs.py runs them so); this small grid keeps the
     split unless march levels are named.  Every choice equals the oracle

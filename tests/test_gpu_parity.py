@@ -21,8 +21,8 @@ def kernel_variant(request, monkeypatch):
     launch per phase, the unit kernels over the whole grid, the TMA-staged
     kernels, the split with TMA-staged persistent core kernels (FP32 Biot
     media; the others keep the per-thread-load core), and the march kernel
-    doing both phases of the deep interior in one pass (the default; FP32
-    Biot media, the others keep the split)."""
+    doing both phases of the deep interior in one pass (the default on
+    grids whose levels outgrow L2; FP32, FP64 keeps the split)."""
     monkeypatch.setenv("FDP_KERNEL_VARIANT", request.param)
     return request.param
 
