@@ -476,13 +476,20 @@ __global__ void k_grad_reduce(const int4* __restrict__ tiles, int ntiles, const 
   }
   if (k >= kSets * kSetP) return;
   const int set = k / kSetP, e = k % kSetP;
-  int lo = 0, hi = ntiles;  // first tile of the set
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (tiles[mid].x < set) lo = mid + 1; else hi = mid;
-  }
+  // the set's tiles [first, end): known up front, so the loads of the
+  // partials go out ahead of the additions, which stay in tile order
+  auto bound = [&](int s) {  // first tile of a set >= s
+    int lo = 0, hi = ntiles;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (tiles[mid].x < s) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+  };
+  const int first = bound(set), end = bound(set + 1);
   float g = grad[k];
-  for (int q = lo; q < ntiles && tiles[q].x == set; ++q) g += part[(size_t)q * kSetP + e];
+#pragma unroll 8
+  for (int q = first; q < end; ++q) g += part[(size_t)q * kSetP + e];
   grad[k] = g;
 }
 
