@@ -847,9 +847,15 @@ template <class T> struct HostBuf {
   T* data() { return p.get(); }
   size_t size() const { return n; }
   // hands the memory to a thread of its own that frees it, so that the
-  // caller does not wait for hundreds of megabytes to be unmapped
+  // caller does not wait for hundreds of megabytes to be unmapped (freed
+  // here when no thread can be started)
   void release_later() {
-    if (n >= ((size_t)1 << 24)) std::thread([q = std::move(p)]() mutable { q.reset(); }).detach();
+    if (n >= ((size_t)1 << 24)) {
+      try {
+        std::thread([q = std::move(p)]() mutable { q.reset(); }).detach();
+      } catch (...) {
+      }
+    }
     p.reset();
     n = 0;
   }
