@@ -1226,8 +1226,14 @@ int fdp_set_medium(fdp_ctx* c, const int32_t* jm, int32_t nx, int32_t nz, int32_
   int rc;
   CK(c, cudaStreamSynchronize(c->stream));
   unshare_medium(c);
-  rc = (c->prec == 8) ? build_medium<double>(c, jm, jmnum, (const double*)table24)
-                      : build_medium<float>(c, jm, jmnum, (const float*)table24);
+  // host scratch of the size of the grid: a failed allocation is an error
+  // code, not an exception across the ABI
+  try {
+    rc = (c->prec == 8) ? build_medium<double>(c, jm, jmnum, (const double*)table24)
+                        : build_medium<float>(c, jm, jmnum, (const float*)table24);
+  } catch (const std::bad_alloc&) {
+    return fail(c, FDP_ERR_ALLOC, "host memory for the medium's set-up");
+  }
   if (rc != FDP_OK) return rc;
   CK(c, cudaStreamSynchronize(c->stream));
   if ((rc = make_core_maps(c)) != FDP_OK) return rc;
@@ -1431,7 +1437,11 @@ int fdp_get_receivers(fdp_ctx* c, int32_t it_first, int32_t n_levels, void* host
     raw.release_later();
     return FDP_OK;
   };
-  return c->prec == 8 ? body(0.0) : body(0.0f);
+  try {
+    return c->prec == 8 ? body(0.0) : body(0.0f);
+  } catch (const std::bad_alloc&) {
+    return fail(c, FDP_ERR_ALLOC, "host memory for the receiver samples");
+  }
 }
 
 int fdp_field_bounds(fdp_ctx* c, int32_t id, int32_t* b4) {
